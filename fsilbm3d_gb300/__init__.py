@@ -1,0 +1,17 @@
+"""GB300 (sm_103a) implementation of FSILBM3D's per-time-step hot path.
+
+The compute lives in libfsi_gpu.so (CUDA kernels behind the C-ABI of
+include/fsi_gpu.h). This package is the host layer above that ABI: it loads
+the library, mirrors the reference's block and body interfaces
+(FluidDomain.f90 LBMBlock, Solidbody.f90 VirtualBody) and the per-step
+orchestration of LBMBlockComm.f90:279-338.
+
+There is no CPU fallback: if the CUDA library cannot be loaded, or no GPU is
+present, every compute call raises.
+"""
+from .abi import (FsiError, Block, Pair, lib, load_library, library_path, PREC_F64, PREC_F64_FAST,
+                  PREC_F32, PREC_F16, PREC_BF16, PRECISIONS, device_info)
+from .d3q19 import E, OPPO, WT, Q
+
+__all__ = ["FsiError", "Block", "Pair", "lib", "load_library", "library_path", "PREC_F64", "PREC_F64_FAST",
+           "PREC_F32", "PREC_F16", "PREC_BF16", "PRECISIONS", "device_info", "E", "OPPO", "WT", "Q"]

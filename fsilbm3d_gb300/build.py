@@ -1,0 +1,76 @@
+"""Build libfsi_gpu.so (sm_103a) in-tree with nvcc.
+
+Three translation units, compiled in parallel:
+  k_f64_exact.cu  -fmad=false  FP64 kernels in the reference's operation order
+  k_fast.cu                    FP64 regrouped and FP32/FP16/BF16 storage forms
+  fsi_abi.cu                   host implementation of include/fsi_gpu.h
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libfsi_gpu.so")
+ROOT = os.path.dirname(HERE)
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+          "-I" + os.path.join(ROOT, "include")]
+UNITS = {
+    "k_f64_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
+    "k_fast.cu": [],
+    "fsi_abi.cu": [],
+}
+HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "bc_impl.cuh"]
+
+
+def _nvcc():
+    for cand in ("/usr/local/cuda/bin/nvcc", "nvcc"):
+        if os.path.sep not in cand or os.path.exists(cand):
+            return cand
+    return "nvcc"
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "fsi_gpu.h")]
+    jobs = []
+    objs = []
+    for src, extra in UNITS.items():
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(o)
+        if force or _stale(o, [s, __file__] + hdrs):
+            jobs.append([nvcc] + ARCH + COMMON + extra + ["-c", s, "-o", o])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed:\n%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+        return r.stderr
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        for msg in ex.map(run, jobs):
+            if verbose and msg:
+                print(msg)
+    if force or jobs or _stale(LIB, objs):
+        run([nvcc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

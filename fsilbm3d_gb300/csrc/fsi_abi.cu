@@ -1,0 +1,788 @@
+// fsi_abi.cu -- host implementation of the C-ABI declared in include/fsi_gpu.h.
+//
+// A block handle owns the device state of one LBMBlock (FluidDomain.f90:17-56):
+// two distribution buffers (A/B, swapped every step), full-size den/uuu,
+// half-way face copies, the immersed-boundary marker arrays and the IB window.
+// Everything a time step needs stays resident in HBM; the host exchanges only
+// marker data, the Lagrangian force and scalars.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/fsi_gpu.h"
+#include "fsi_kernels.h"
+
+using namespace fsi;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                             \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) return fail(FSI_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+bool valid_code(int c) {
+    switch (c) {
+    case 0: case 1: case 101: case 102: case 103: case 104:
+    case 201: case 202: case 203: case 204: case 301: case 302: return true;
+    default: return false;
+    }
+}
+
+size_t elem_size(int prec) {
+    switch (prec) {
+    case FSI_PREC_F64: case FSI_PREC_F64_FAST: return 8;
+    case FSI_PREC_F32: return 4;
+    default: return 2;
+    }
+}
+
+// calculate_MRT_params (FluidDomain.f90:466-522): M from the Gram-Schmidt
+// moment basis, M^-1 = M^T / diag(M M^T), M_COLLID = M^-1 S M, M_FORCE = I - M_COLLID/2.
+void build_mrt(double omega, double *mc, double *mf) {
+    const int Q_ = 19;
+    double M[19][19], Mi[19][19], D[19], T[19][19];
+    for (int i = 0; i < Q_; i++) {
+        double ex = ex_(i), ey = ey_(i), ez = ez_(i);
+        double e2 = ex * ex + ey * ey + ez * ez;
+        M[0][i] = 1.0;
+        M[1][i] = 19.0 * e2 - 30.0;
+        M[2][i] = (21.0 * e2 * e2 - 53.0 * e2 + 24.0) / 2.0;
+        M[3][i] = ex; M[5][i] = ey; M[7][i] = ez;
+        M[4][i] = (5.0 * e2 - 9.0) * ex;
+        M[6][i] = (5.0 * e2 - 9.0) * ey;
+        M[8][i] = (5.0 * e2 - 9.0) * ez;
+        M[9][i] = 3.0 * ex * ex - e2;
+        M[10][i] = (3.0 * e2 - 5.0) * (3.0 * ex * ex - e2);
+        M[11][i] = ey * ey - ez * ez;
+        M[12][i] = (3.0 * e2 - 5.0) * (ey * ey - ez * ez);
+        M[13][i] = ex * ey;
+        M[14][i] = ey * ez;
+        M[15][i] = ez * ex;
+        M[16][i] = (ey * ey - ez * ez) * ex;
+        M[17][i] = (ez * ez - ex * ex) * ey;
+        M[18][i] = (ex * ex - ey * ey) * ez;
+    }
+    for (int r = 0; r < Q_; r++) {
+        double s = 0.0;
+        for (int k = 0; k < Q_; k++) s += M[r][k] * M[r][k];
+        D[r] = s;
+    }
+    for (int r = 0; r < Q_; r++)
+        for (int c = 0; c < Q_; c++) Mi[r][c] = M[c][r] / D[c];
+    const double s0 = 0.0, s1 = 1.19, s2 = 1.4, s4 = 1.2, s10 = 1.4, s16 = 1.98;  // ConstParams.f90:28
+    const double S[19] = {s0, s1, s2, s0, s4, s0, s4, s0, s4, omega, s10, omega, s10, omega, omega, omega, s16, s16, s16};
+    for (int r = 0; r < Q_; r++)
+        for (int c = 0; c < Q_; c++) T[r][c] = Mi[r][c] * S[c];
+    for (int r = 0; r < Q_; r++)
+        for (int c = 0; c < Q_; c++) {
+            double s = 0.0;
+            for (int k = 0; k < Q_; k++) s += T[r][k] * M[k][c];
+            mc[r + Q_ * c] = s;
+            mf[r + Q_ * c] = (r == c ? 1.0 : 0.0) - 0.5 * s;
+        }
+}
+
+}  // namespace
+
+struct fsi_block {
+    fsi_block_desc d{};
+    int X = 0, Y = 0, Z = 0;
+    long long N = 0;
+    double tau = 0, omega = 0, xmax = 0, ymax = 0, zmax = 0;
+    int periodic[3] = {0, 0, 0};
+    MrtMats mm{};
+    int prec = 0;
+    size_t esz = 8;
+    void *fa = nullptr, *fb = nullptr;
+    double *den = nullptr, *u = nullptr;
+    double *stage = nullptr;  // FP64 staging for converted storage forms
+    double *hw[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int hw_ready[6] = {0, 0, 0, 0, 0, 0};
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // immersed boundary
+    int nb = 0, Mtot = 0;
+    std::vector<int> M, offs;
+    int ibbc[6] = {0, 0, 0, 0, 0, 0};
+    int *d_offs = nullptr, *d_err = nullptr;
+    double *d_xyz = nullptr, *d_vel = nullptr, *d_area = nullptr, *d_eforce = nullptr, *d_fet = nullptr;
+    double *d_tolm = nullptr, *d_tol = nullptr;
+    int16_t *d_ei = nullptr;
+    float *d_ew = nullptr;
+    double *h_tol = nullptr;  // pinned
+    int *h_err = nullptr;     // pinned
+    // IB window
+    IbGeom geom{};
+    long long Nw = 0, Nw_cap = 0;
+    double *wden = nullptr, *wu = nullptr, *wforce = nullptr;
+    int *cnt = nullptr, *start = nullptr, *fillc = nullptr, *list = nullptr;
+    long long list_cap = 0;
+    bool win_valid = false;
+    // captured graph of two steps (A->B, B->A)
+    cudaGraphExec_t gexec = nullptr;
+    double g_vf[3] = {0, 0, 0};
+    void *g_src = nullptr;
+};
+
+struct fsi_pair {
+    fsi_block_t fa = nullptr, so = nullptr;
+    PairGeom p{};
+    int scheme = 1;
+    double *buf[6][2] = {};
+    double *buft[6][2] = {};
+    double *scr_f = nullptr, *scr_t = nullptr;
+};
+
+namespace {
+
+bool is_fast(const fsi_block *h) { return h->prec != FSI_PREC_F64; }
+
+Vel make_vel(const fsi_block *h, double blktime) {
+    Vel v{};
+    v.kind = h->d.velocityKind;
+    for (int i = 0; i < 3; i++) { v.vin[i] = h->d.uvwIn[i]; v.sr[i] = h->d.shearRateIn[i]; }
+    // evaluate_oscillatory_velocity (FluidDomain.f90:1813-1824), uniform in space
+    const double pi = 3.141592653589793;
+    v.osc[0] = h->d.uvwIn[0] + h->d.shearRateIn[0] * cos(((2.0 * pi) * h->d.shearRateIn[1]) * blktime +
+                                                         (h->d.shearRateIn[2] / 180.0) * pi);
+    v.osc[1] = h->d.uvwIn[1];
+    v.osc[2] = h->d.uvwIn[2];
+    return v;
+}
+
+void face_dims(const fsi_block *h, int k, int &A, int &B) {
+    int ax = k >> 1;
+    A = (ax < 2) ? h->Z : h->Y;
+    B = (ax == 0) ? h->Y : h->X;
+}
+
+int apply_bcs(fsi_block *h, void *f, double blktime) {
+    for (int k = 0; k < 6; k++) {
+        int code = h->d.bndConds[k];
+        if (code == BC_PERIODIC || code == BC_FLUID || code == BC_FLUID_FATHER) continue;
+        if (code == BC_WALL_HW || code == BC_MWALL_HW) {
+            // allocate-on-first-call semantics, FluidDomain.f90:660-662
+            if (!h->hw_ready[k]) { h->hw_ready[k] = 1; continue; }
+        }
+        BcArgs a{};
+        a.f = f;
+        a.X = h->X; a.Y = h->Y; a.Z = h->Z; a.N = h->N;
+        a.face = k; a.code = code;
+        a.dh = h->d.dh; a.xmin = h->d.xmin; a.ymin = h->d.ymin; a.zmin = h->d.zmin;
+        a.xmax = h->xmax; a.ymax = h->ymax; a.zmax = h->zmax;
+        a.denIn = h->d.denIn;
+        a.vel = make_vel(h, blktime);
+        a.hw = h->hw[k];
+        a.den = h->den;
+        a.u = h->u;
+        cudaError_t e = is_fast(h) ? launch_bc_fast(a, h->prec, h->st) : launch_bc_f64(a, h->st);
+        if (e != cudaSuccess) return fail(FSI_E_CUDA, "boundary kernel: %s", cudaGetErrorString(e));
+    }
+    return FSI_OK;
+}
+
+int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_window) {
+    StepArgs a{};
+    a.src = h->fa;
+    a.dst = h->fb;
+    a.X = h->X; a.Y = h->Y; a.Z = h->Z; a.N = h->N;
+    a.dh = h->d.dh;
+    a.omega = h->omega;
+    for (int i = 0; i < 3; i++) a.vf[i] = vf[i];
+    if (use_window && h->win_valid) {
+        a.win.x0 = h->geom.wx0; a.win.x1 = h->geom.wx1;
+        a.win.y0 = h->geom.wy0; a.win.y1 = h->geom.wy1;
+        a.win.z0 = h->geom.wz0; a.win.z1 = h->geom.wz1;
+        a.win.WY = h->geom.WY; a.win.WZ = h->geom.WZ;
+        a.win.n = h->Nw;
+        a.win.den = h->wden; a.win.u = h->wu; a.win.force = h->wforce;
+    } else {
+        a.win.x0 = 0; a.win.x1 = -1; a.win.y0 = 0; a.win.y1 = -1; a.win.z0 = 0; a.win.z1 = -1;
+    }
+    for (int k = 0; k < 6; k++) {
+        int code = h->d.bndConds[k];
+        a.hw[k] = (code == BC_WALL_HW || code == BC_MWALL_HW) ? h->hw[k] : nullptr;
+        a.l2[k] = (code == BC_NEQ) ? 1 : 0;
+    }
+    a.den = h->den;
+    a.u = h->u;
+    cudaError_t e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
+                               : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
+    if (e != cudaSuccess) return fail(FSI_E_CUDA, "step kernel: %s", cudaGetErrorString(e));
+    int rc = apply_bcs(h, h->fb, blktime);
+    if (rc) return rc;
+    std::swap(h->fa, h->fb);
+    return FSI_OK;
+}
+
+void free_block(fsi_block *h) {
+    if (!h) return;
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
+                    h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
+                    h->cnt, h->start, h->fillc, h->list};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (int k = 0; k < 6; k++)
+        if (h->hw[k]) cudaFree(h->hw[k]);
+    if (h->h_tol) cudaFreeHost(h->h_tol);
+    if (h->h_err) cudaFreeHost(h->h_err);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsi_last_error(char *buf, int len) {
+    int n = (int)g_err.size();
+    if (buf && len > 0) {
+        int m = std::min(n, len - 1);
+        memcpy(buf, g_err.data(), m);
+        buf[m] = 0;
+    }
+    return n;
+}
+
+int fsi_device_info(int *sm_count, int *cc_major, int *cc_minor) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    CK(cudaGetDeviceProperties(&p, dev));
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    if (cc_major) *cc_major = p.major;
+    if (cc_minor) *cc_minor = p.minor;
+    return FSI_OK;
+}
+
+int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
+    if (!out || !d) return fail(FSI_E_ARG, "null argument");
+    *out = nullptr;
+    if (d->xDim < 3 || d->yDim < 3 || d->zDim < 3) return fail(FSI_E_ARG, "block dimensions must be >= 3");
+    // FluidDomain.f90:88-91: marker stencil indices are int16
+    if (d->xDim > 32767 || d->yDim > 32767 || d->zDim > 32767)
+        return fail(FSI_E_ARG, "Grid number exceeds 32767, please try to reduced the grid size.");
+    if (!(d->dh > 0.0)) return fail(FSI_E_ARG, "dh must be positive");
+    if (d->iCollidModel != 1 && d->iCollidModel != 3)
+        return fail(FSI_E_ARG, "iCollidModel %d not supported (1 SRT, 3 MRT)", d->iCollidModel);
+    if (d->precision < FSI_PREC_F64 || d->precision > FSI_PREC_BF16) return fail(FSI_E_ARG, "unknown precision");
+    if (d->velocityKind != 0 && d->velocityKind != 2)
+        return fail(FSI_E_ARG, "velocityKind %d not supported (0 shear, 2 oscillatory)", d->velocityKind);
+    for (int k = 0; k < 6; k++)
+        if (!valid_code(d->bndConds[k])) return fail(FSI_E_BC, "face %d has no such boundary condition %d", k, d->bndConds[k]);
+    // check_periodic_boundary_ (FluidDomain.f90:110-125)
+    for (int i = 0; i < 3; i++) {
+        int a = d->bndConds[2 * i], b = d->bndConds[2 * i + 1];
+        if ((a == BC_PERIODIC || b == BC_PERIODIC) && a != b)
+            return fail(FSI_E_BC, "Stop! Periodic boundaries must apper in pairs: %d %d", a, b);
+    }
+    fsi_block *h = new fsi_block();
+    h->d = *d;
+    h->d.m_collid = nullptr;
+    h->d.m_force = nullptr;
+    h->X = d->xDim; h->Y = d->yDim; h->Z = d->zDim;
+    h->N = (long long)h->X * h->Y * h->Z;
+    for (int i = 0; i < 3; i++) h->periodic[i] = (d->bndConds[2 * i] == BC_PERIODIC) ? 1 : 0;
+    // FluidDomain.f90:94-105
+    h->xmax = d->xmin + d->dh * (double)(h->X - 1);
+    h->ymax = d->ymin + d->dh * (double)(h->Y - 1);
+    h->zmax = d->zmin + d->dh * (double)(h->Z - 1);
+    if (h->periodic[0]) h->xmax = h->xmax + d->dh;
+    if (h->periodic[1]) h->ymax = h->ymax + d->dh;
+    if (h->periodic[2]) h->zmax = h->zmax + d->dh;
+    // calculate_SRT_params, FluidDomain.f90:450-456
+    h->tau = d->nu / (d->dh * (1.0 / 3.0)) + 0.5;
+    h->omega = 1.0 / h->tau;
+    if (d->m_collid && d->m_force) {
+        memcpy(h->mm.mc, d->m_collid, sizeof(double) * 361);
+        memcpy(h->mm.mf, d->m_force, sizeof(double) * 361);
+    } else {
+        build_mrt(h->omega, h->mm.mc, h->mm.mf);
+    }
+    h->prec = d->precision;
+    h->esz = elem_size(h->prec);
+    size_t fbytes = h->esz * 19 * (size_t)h->N;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    chk(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    chk(cudaEventCreate(&h->ev0));
+    chk(cudaEventCreate(&h->ev1));
+    chk(cudaMalloc(&h->fa, fbytes));
+    chk(cudaMalloc(&h->fb, fbytes));
+    chk(cudaMalloc((void **)&h->den, sizeof(double) * h->N));
+    chk(cudaMalloc((void **)&h->u, sizeof(double) * 3 * h->N));
+    if (h->prec != FSI_PREC_F64 && h->prec != FSI_PREC_F64_FAST)
+        chk(cudaMalloc((void **)&h->stage, sizeof(double) * 19 * (size_t)h->N));
+    for (int k = 0; k < 6; k++) {
+        int code = d->bndConds[k];
+        if (code == BC_WALL_HW || code == BC_MWALL_HW) {
+            int A, B;
+            face_dims(h, k, A, B);
+            chk(cudaMalloc((void **)&h->hw[k], sizeof(double) * 19 * (size_t)A * B));
+            if (e == cudaSuccess) chk(cudaMemset(h->hw[k], 0, sizeof(double) * 19 * (size_t)A * B));
+        }
+    }
+    chk(cudaHostAlloc((void **)&h->h_tol, sizeof(double) * 64, cudaHostAllocDefault));
+    chk(cudaHostAlloc((void **)&h->h_err, sizeof(int), cudaHostAllocDefault));
+    chk(cudaMalloc((void **)&h->d_err, sizeof(int)));
+    if (e == cudaSuccess) chk(cudaMemset(h->den, 0, sizeof(double) * h->N));
+    if (e == cudaSuccess) chk(cudaMemset(h->u, 0, sizeof(double) * 3 * h->N));
+    if (e == cudaSuccess) chk(cudaMemset(h->fa, 0, fbytes));
+    if (e == cudaSuccess) chk(cudaMemset(h->fb, 0, fbytes));
+    if (e != cudaSuccess) {
+        free_block(h);
+        return fail(FSI_E_CUDA, "block allocation: %s", cudaGetErrorString(e));
+    }
+    *out = h;
+    return FSI_OK;
+}
+
+int fsi_block_destroy(fsi_block_t h) {
+    if (!h) return FSI_OK;
+    cudaStreamSynchronize(h->st);
+    free_block(h);
+    return FSI_OK;
+}
+
+int fsi_block_get_params(fsi_block_t h, double *tau, double *omega, double *m_collid, double *m_force) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    if (tau) *tau = h->tau;
+    if (omega) *omega = h->omega;
+    if (m_collid) memcpy(m_collid, h->mm.mc, sizeof(double) * 361);
+    if (m_force) memcpy(m_force, h->mm.mf, sizeof(double) * 361);
+    return FSI_OK;
+}
+
+int fsi_block_upload_f(fsi_block_t h, const double *fIn) {
+    if (!h || !fIn) return fail(FSI_E_ARG, "null argument");
+    size_t n = 19 * (size_t)h->N;
+    if (h->esz == 8) {
+        CK(cudaMemcpyAsync(h->fa, fIn, n * 8, cudaMemcpyHostToDevice, h->st));
+    } else {
+        CK(cudaMemcpyAsync(h->stage, fIn, n * 8, cudaMemcpyHostToDevice, h->st));
+        CK(launch_convert_to_store(h->stage, h->fa, h->N, h->prec, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return FSI_OK;
+}
+
+int fsi_block_download_f(fsi_block_t h, double *fIn) {
+    if (!h || !fIn) return fail(FSI_E_ARG, "null argument");
+    size_t n = 19 * (size_t)h->N;
+    if (h->esz == 8) {
+        CK(cudaMemcpyAsync(fIn, h->fa, n * 8, cudaMemcpyDeviceToHost, h->st));
+    } else {
+        CK(launch_convert_from_store(h->fa, h->stage, h->N, h->prec, h->st));
+        CK(cudaMemcpyAsync(fIn, h->stage, n * 8, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return FSI_OK;
+}
+
+int fsi_block_initialise(fsi_block_t h, double time) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    Vel v = make_vel(h, time);
+    double *dst = (h->esz == 8) ? (double *)h->fa : h->stage;
+    CK(launch_init_f64(dst, h->den, h->u, h->X, h->Y, h->Z, h->d.dh, h->d.xmin, h->d.ymin, h->d.zmin, h->d.denIn, v,
+                       time, h->st));
+    if (h->esz != 8) CK(launch_convert_to_store(h->stage, h->fa, h->N, h->prec, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FSI_OK;
+}
+
+int fsi_block_set_boundary_conditions(fsi_block_t h, double blktime) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    int rc = apply_bcs(h, h->fa, blktime);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    return FSI_OK;
+}
+
+int fsi_block_macro(fsi_block_t h, const double vf[3], double *den, double *uuu) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    double z3[3] = {0, 0, 0};
+    const double *v = vf ? vf : z3;
+    if (h->esz == 8 && h->prec == FSI_PREC_F64) {
+        CK(launch_macro_f64((const double *)h->fa, h->den, h->u, h->X, h->Y, h->Z, h->d.dh, v, h->st));
+    } else {
+        CK(launch_macro_fast(h->fa, h->prec, h->den, h->u, h->X, h->Y, h->Z, h->d.dh, v, h->st));
+    }
+    if (den) CK(cudaMemcpyAsync(den, h->den, sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->st));
+    if (uuu) CK(cudaMemcpyAsync(uuu, h->u, sizeof(double) * 3 * h->N, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return FSI_OK;
+}
+
+int fsi_block_step(fsi_block_t h, const double vf[3], double blktime) {
+    if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    int rc = enqueue_step(h, vf, blktime, true);
+    h->win_valid = false;
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    return FSI_OK;
+}
+
+int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps, float *ms) {
+    if (!h || !vf || nsteps < 0) return fail(FSI_E_ARG, "invalid argument");
+    h->win_valid = false;
+    // a captured pair of steps is valid when no kernel argument changes from
+    // step to step: no boundary depends on time (oscillatory inflow)
+    bool time_dep = false;
+    for (int k = 0; k < 6; k++) {
+        int c = h->d.bndConds[k];
+        if (h->d.velocityKind == 2 && (c == BC_EQ || c == BC_NEQ || c == BC_MWALL || c == BC_MWALL_HW)) time_dep = true;
+        // the first application of a half-way face only marks it ready
+        if ((c == BC_WALL_HW || c == BC_MWALL_HW) && !h->hw_ready[k]) time_dep = true;
+    }
+    bool use_graph = !time_dep && nsteps >= 2;
+    if (use_graph && h->gexec && (memcmp(h->g_vf, vf, sizeof(h->g_vf)) != 0 || h->g_src != h->fa)) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    if (use_graph && !h->gexec) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step(h, vf, blktime0, false);
+        if (!rc) rc = enqueue_step(h, vf, blktime0, false);
+        cudaError_t ce = cudaStreamEndCapture(h->st, &g);
+        if (rc) return rc;
+        if (ce != cudaSuccess) return fail(FSI_E_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        CK(cudaGraphInstantiate(&h->gexec, g, 0));
+        cudaGraphDestroy(g);
+        memcpy(h->g_vf, vf, sizeof(h->g_vf));
+        // capture swapped the buffers twice: the state is unchanged and the
+        // graph's first step reads fa
+        h->g_src = h->fa;
+    }
+    CK(cudaEventRecord(h->ev0, h->st));
+    int done = 0;
+    if (use_graph) {
+        // the graph was captured with fa as the source of its first step
+        for (; done + 2 <= nsteps; done += 2) CK(cudaGraphLaunch(h->gexec, h->st));
+    }
+    // an odd remainder (or a time-dependent boundary) runs eagerly
+    for (; done < nsteps; done++) {
+        int rc = enqueue_step(h, vf, blktime0 + h->d.dh * (double)done, false);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(h->ev1, h->st));
+    CK(cudaEventSynchronize(h->ev1));
+    if (ms) CK(cudaEventElapsedTime(ms, h->ev0, h->ev1));
+    return FSI_OK;
+}
+
+// ------------------------------------------------------------------------ IB
+
+int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6]) {
+    if (!h || nbodies < 0 || (nbodies > 0 && !M)) return fail(FSI_E_ARG, "invalid argument");
+    if (nbodies > 64) return fail(FSI_E_ARG, "at most 64 bodies per block");
+    h->nb = nbodies;
+    h->M.assign(M, M + nbodies);
+    h->offs.assign(nbodies + 1, 0);
+    for (int b = 0; b < nbodies; b++) {
+        if (M[b] <= 0) return fail(FSI_E_ARG, "body %d has no markers", b);
+        h->offs[b + 1] = h->offs[b] + M[b];
+    }
+    h->Mtot = h->offs[nbodies];
+    if ((long long)h->Mtot * 64 > 0x7fffffffLL) return fail(FSI_E_ARG, "too many markers");
+    for (int k = 0; k < 6; k++) h->ibbc[k] = bc ? bc[k] : h->d.bndConds[k];
+    void *ptrs[] = {h->d_offs, h->d_xyz, h->d_vel, h->d_area, h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    int Mt = std::max(1, h->Mtot);
+    CK(cudaMalloc((void **)&h->d_offs, sizeof(int) * (nbodies + 1)));
+    CK(cudaMalloc((void **)&h->d_xyz, sizeof(double) * 3 * Mt));
+    CK(cudaMalloc((void **)&h->d_vel, sizeof(double) * 3 * Mt));
+    CK(cudaMalloc((void **)&h->d_area, sizeof(double) * Mt));
+    CK(cudaMalloc((void **)&h->d_eforce, sizeof(double) * 3 * Mt));
+    CK(cudaMalloc((void **)&h->d_fet, sizeof(double) * 3 * Mt));
+    CK(cudaMalloc((void **)&h->d_tolm, sizeof(double) * Mt));
+    CK(cudaMalloc((void **)&h->d_tol, sizeof(double) * 64));
+    CK(cudaMalloc((void **)&h->d_ei, sizeof(int16_t) * 12 * Mt));
+    CK(cudaMalloc((void **)&h->d_ew, sizeof(float) * 12 * Mt));
+    CK(cudaMemcpy(h->d_offs, h->offs.data(), sizeof(int) * (nbodies + 1), cudaMemcpyHostToDevice));
+    return FSI_OK;
+}
+
+namespace {
+
+// The IB window: a box holding every cell any marker's 4x4x4 support can
+// reach. Computed on the host from floor((x - xmin)/dh) with a one-cell
+// margin on each side (the reference's stencil origin arithmetic,
+// Solidbody.f90:771-780, may differ from this estimate by one cell). A box
+// that crosses a periodic face spans the whole axis. The stencil kernel
+// checks every index against the box.
+int compute_window(fsi_block *h, const double *xyz) {
+    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
+    const double mins[3] = {h->d.xmin, h->d.ymin, h->d.zmin};
+    const int dims[3] = {h->X, h->Y, h->Z};
+    for (int m = 0; m < h->Mtot; m++)
+        for (int a = 0; a < 3; a++) {
+            double v = xyz[3 * m + a];
+            if (!std::isfinite(v)) return fail(FSI_E_NAN, "non-finite marker coordinate");
+            double t = std::floor((v - mins[a]) / h->d.dh);
+            if (t < -1e9 || t > 1e9) return fail(FSI_E_RANGE, "marker far outside the block");
+            int i = (int)t;
+            lo[a] = std::min(lo[a], i - 2);
+            hi[a] = std::max(hi[a], i + 3);
+        }
+    int box[6];
+    for (int a = 0; a < 3; a++) {
+        if (lo[a] < 0 || hi[a] > dims[a] - 1) {
+            if (h->ibbc[2 * a] == BC_PERIODIC) { lo[a] = 0; hi[a] = dims[a] - 1; }
+            else { lo[a] = std::max(lo[a], 0); hi[a] = std::min(hi[a], dims[a] - 1); }
+        }
+        if (lo[a] > hi[a]) return fail(FSI_E_RANGE, "markers outside the block");
+        box[2 * a] = lo[a];
+        box[2 * a + 1] = hi[a];
+    }
+    IbGeom &g = h->geom;
+    g.X = h->X; g.Y = h->Y; g.Z = h->Z;
+    g.dh = h->d.dh; g.xmin = h->d.xmin; g.ymin = h->d.ymin; g.zmin = h->d.zmin;
+    for (int k = 0; k < 6; k++) g.bc[k] = h->ibbc[k];
+    g.wx0 = box[0]; g.wx1 = box[1]; g.wy0 = box[2]; g.wy1 = box[3]; g.wz0 = box[4]; g.wz1 = box[5];
+    g.WY = box[3] - box[2] + 1;
+    g.WZ = box[5] - box[4] + 1;
+    h->Nw = (long long)(box[1] - box[0] + 1) * g.WY * g.WZ;
+    if (h->Nw > h->Nw_cap) {
+        void *ptrs[] = {h->wden, h->wu, h->wforce, h->cnt, h->start, h->fillc};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+        long long cap = h->Nw + h->Nw / 2 + 1024;
+        CK(cudaMalloc((void **)&h->wden, sizeof(double) * cap));
+        CK(cudaMalloc((void **)&h->wu, sizeof(double) * 3 * cap));
+        CK(cudaMalloc((void **)&h->wforce, sizeof(double) * 3 * cap));
+        CK(cudaMalloc((void **)&h->cnt, sizeof(int) * cap));
+        CK(cudaMalloc((void **)&h->start, sizeof(int) * (cap + 1)));
+        CK(cudaMalloc((void **)&h->fillc, sizeof(int) * cap));
+        h->Nw_cap = cap;
+    }
+    long long E = (long long)h->Mtot * 64;
+    if (E > h->list_cap) {
+        if (h->list) cudaFree(h->list);
+        CK(cudaMalloc((void **)&h->list, sizeof(int) * std::max(1LL, E)));
+        h->list_cap = E;
+    }
+    return FSI_OK;
+}
+
+}  // namespace
+
+int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
+                 double denIn, double dt, double Uref, int ntol, double dtol, double *eforce, int *iters,
+                 double *residual) {
+    if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    h->win_valid = false;
+    if (iters) *iters = 0;
+    if (residual) *residual = 0.0;
+    if (h->nb == 0 || h->Mtot == 0) return FSI_OK;
+    if (!xyz || !vel || !area || !eforce) return fail(FSI_E_ARG, "null marker array");
+    int rc = compute_window(h, xyz);
+    if (rc) return rc;
+    const int Mt = h->Mtot;
+    CK(cudaMemcpyAsync(h->d_xyz, xyz, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_vel, vel, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_area, area, sizeof(double) * Mt, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
+    CK(cudaMemsetAsync(h->d_eforce, 0, sizeof(double) * 3 * Mt, h->st));
+    // calculate_macro_quantities_ + ResetVolumeForce_ restricted to the window
+    if (h->prec == FSI_PREC_F64) CK(launch_win_macro_f64(h->fa, h->prec, h->wden, h->wu, h->geom, h->N, vf, h->st));
+    else CK(launch_win_macro_fast(h->fa, h->prec, h->wden, h->wu, h->geom, h->N, vf, h->st));
+    CK(launch_ib_stencil(h->d_xyz, h->d_offs, h->nb, Mt, h->geom, h->d_ei, h->d_ew, h->d_err, h->st));
+    CK(launch_ib_csr(h->d_ei, Mt, h->geom, h->Nw, h->cnt, h->start, h->fillc, h->list, h->st));
+    // PenaltyForce_ constants, Solidbody.f90:996 and :936
+    const double ih = 1.0 / h->d.dh;
+    const double invh3p = ((0.5 * dt) * ((ih * ih) * ih)) / denIn;
+    const double invh3s = (ih * ih) * ih;
+    int it = 0;
+    double dmax = 1e10;
+    CK(cudaMemcpyAsync(h->h_err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (*h->h_err) {
+        return fail(FSI_E_RANGE, (*h->h_err & 1) ? "index out of block bounds in IB stencil"
+                                                 : "IB stencil outside the IB window");
+    }
+    while (it < ntol && dmax > dtol) {
+        for (int b = 0; b < h->nb; b++) {
+            int m0 = h->offs[b], m1 = h->offs[b + 1];
+            CK(launch_ib_interp(h->d_ei, h->d_ew, h->d_vel, h->d_area, h->wu, h->geom, m0, m1, invh3p, h->d_eforce,
+                                h->d_fet, h->d_tolm, h->st));
+            CK(launch_ib_reduce(h->d_tolm, m0, m1, h->d_tol + b, h->st));
+            CK(launch_ib_correct(h->d_ew, h->start, h->list, h->Nw, m0, m1, h->d_fet, h->wu, h->st));
+        }
+        CK(cudaMemcpyAsync(h->h_tol, h->d_tol, sizeof(double) * h->nb, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        // calculate_interaction_force, Solidbody.f90:896-905
+        dmax = 0.0;
+        double dsum = 0.0;
+        for (int b = 0; b < h->nb; b++) {
+            if (!std::isfinite(h->h_tol[b])) return fail(FSI_E_NAN, "Nan found in PenaltyForce");
+            dmax = dmax + h->h_tol[b];
+            dsum = dsum + (double)h->M[b];
+        }
+        dmax = dmax / (dsum * Uref);
+        it = it + 1;
+    }
+    CK(launch_ib_spread(h->d_ew, h->start, h->list, h->Nw, h->d_eforce, invh3s, vf, h->wforce, h->st));
+    CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * Mt, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (iters) *iters = it;
+    if (residual) *residual = dmax;
+    h->win_valid = true;
+    return FSI_OK;
+}
+
+int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    if (h->Mtot == 0) return FSI_OK;
+    if (ei) CK(cudaMemcpy(ei, h->d_ei, sizeof(int16_t) * 12 * h->Mtot, cudaMemcpyDeviceToHost));
+    if (ew) CK(cudaMemcpy(ew, h->d_ew, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost));
+    return FSI_OK;
+}
+
+int fsi_ib_get_window(fsi_block_t h, int box[6]) {
+    if (!h || !box) return fail(FSI_E_ARG, "null argument");
+    box[0] = h->geom.wx0; box[1] = h->geom.wx1; box[2] = h->geom.wy0;
+    box[3] = h->geom.wy1; box[4] = h->geom.wz0; box[5] = h->geom.wz1;
+    return FSI_OK;
+}
+
+// ---------------------------------------------------------- block refinement
+
+int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme) {
+    if (!out || !fa || !so) return fail(FSI_E_ARG, "null argument");
+    *out = nullptr;
+    if (fa->prec != FSI_PREC_F64 || so->prec != FSI_PREC_F64)
+        return fail(FSI_E_ARG, "block refinement is built for the FP64 form");
+    fsi_pair *p = new fsi_pair();
+    p->fa = fa;
+    p->so = so;
+    p->scheme = scheme;
+    PairGeom &g = p->p;
+    // build_blocks_comunication, LBMBlockComm.f90:48-91
+    for (int j = 0; j < 6; j++) g.sds[j] = (so->d.bndConds[j] == BC_FLUID) ? ((j % 2 == 0) ? 1 : -1) : 0;
+    int sxD = so->X - so->periodic[0], syD = so->Y - so->periodic[1], szD = so->Z - so->periodic[2];
+    g.s[0] = 1; g.s[2] = 1; g.s[4] = 1;
+    g.s[1] = sxD; g.s[3] = syD; g.s[5] = szD;
+    g.f[0] = (int)floor((so->d.xmin - fa->d.xmin) / fa->d.dh + 1.5);
+    g.f[2] = (int)floor((so->d.ymin - fa->d.ymin) / fa->d.dh + 1.5);
+    g.f[4] = (int)floor((so->d.zmin - fa->d.zmin) / fa->d.dh + 1.5);
+    int ratio = (int)floor(fa->d.dh / so->d.dh + 0.5);
+    if (ratio != 2) { delete p; return fail(FSI_E_ARG, "refinement ratio must be 2 (m_gridDelta)"); }
+    g.f[1] = g.f[0] + (sxD - 1) / ratio;
+    g.f[3] = g.f[2] + (syD - 1) / ratio;
+    g.f[5] = g.f[4] + (szD - 1) / ratio;
+    for (int j = 0; j < 6; j++) { g.si[j] = g.s[j] + g.sds[j] * ratio; g.fi[j] = g.f[j] + g.sds[j]; }
+    g.xDimS = so->X; g.xDimF = g.f[1] - g.f[0] + 1;
+    g.yDimS = so->Y; g.yDimF = g.f[3] - g.f[2] + 1;
+    g.zDimS = so->Z; g.zDimF = g.f[5] - g.f[4] + 1;
+    if (g.f[0] < 1 || g.f[2] < 1 || g.f[4] < 1 || g.f[1] > fa->X || g.f[3] > fa->Y || g.f[5] > fa->Z) {
+        delete p;
+        return fail(FSI_E_ARG, "son block does not lie inside its father");
+    }
+    size_t maxS = 0;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 6; k++) {
+        if (so->d.bndConds[k] != BC_FLUID) continue;
+        int ax = k >> 1;
+        size_t AF = ax == 2 ? g.yDimF : g.zDimF, BF = ax == 0 ? g.yDimF : g.xDimF;
+        size_t AS = ax == 2 ? g.yDimS : g.zDimS, BS = ax == 0 ? g.yDimS : g.xDimS;
+        maxS = std::max(maxS, AS * BS);
+        for (int t = 0; t < 2; t++) {
+            if (e == cudaSuccess) e = cudaMalloc((void **)&p->buf[k][t], sizeof(double) * 19 * AF * BF);
+            if (e == cudaSuccess) e = cudaMalloc((void **)&p->buft[k][t], sizeof(double) * AF * BF);
+        }
+    }
+    if (maxS) {
+        if (e == cudaSuccess) e = cudaMalloc((void **)&p->scr_f, sizeof(double) * 19 * maxS);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&p->scr_t, sizeof(double) * maxS);
+    }
+    if (e != cudaSuccess) {
+        fsi_pair_destroy(p);
+        return fail(FSI_E_CUDA, "pair allocation: %s", cudaGetErrorString(e));
+    }
+    *out = p;
+    return FSI_OK;
+}
+
+int fsi_pair_destroy(fsi_pair_t p) {
+    if (!p) return FSI_OK;
+    for (int k = 0; k < 6; k++)
+        for (int t = 0; t < 2; t++) {
+            if (p->buf[k][t]) cudaFree(p->buf[k][t]);
+            if (p->buft[k][t]) cudaFree(p->buft[k][t]);
+        }
+    if (p->scr_f) cudaFree(p->scr_f);
+    if (p->scr_t) cudaFree(p->scr_t);
+    delete p;
+    return FSI_OK;
+}
+
+int fsi_pair_extract(fsi_pair_t p, int time_level) {
+    if (!p || (time_level != 1 && time_level != 2)) return fail(FSI_E_ARG, "invalid argument");
+    fsi_block *fa = p->fa;
+    for (int k = 0; k < 6; k++) {
+        if (p->so->d.bndConds[k] != BC_FLUID) continue;
+        CK(launch_pair_extract((const double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, p->p, k, p->buf[k][time_level - 1],
+                               p->buft[k][time_level - 1], fa->st));
+        if (time_level == 2) {
+            int ax = k >> 1;
+            long long A = ax == 2 ? p->p.yDimF : p->p.zDimF, B = ax == 0 ? p->p.yDimF : p->p.xDimF;
+            CK(launch_pair_average(p->buf[k][0], p->buf[k][1], 19 * A * B, fa->st));
+            CK(launch_pair_average(p->buft[k][0], p->buft[k][1], A * B, fa->st));
+        }
+    }
+    CK(cudaStreamSynchronize(fa->st));
+    return FSI_OK;
+}
+
+int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]) {
+    if (!p || !vf) return fail(FSI_E_ARG, "invalid argument");
+    fsi_block *so = p->so, *fa = p->fa;
+    CK(cudaStreamSynchronize(fa->st));
+    for (int k = 0; k < 6; k++) {
+        if (p->p.sds[k] == 0) continue;
+        int lvl = (n_timeStep == 0) ? 0 : 1;
+        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
+                           p->scheme, p->scr_f, p->scr_t, vf, fa->d.dh, so->st));
+    }
+    CK(cudaStreamSynchronize(so->st));
+    return FSI_OK;
+}
+
+int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
+    if (!p || !vf) return fail(FSI_E_ARG, "invalid argument");
+    fsi_block *so = p->so, *fa = p->fa;
+    CK(cudaStreamSynchronize(so->st));
+    for (int k = 0; k < 6; k++) {
+        int want = (k % 2 == 0) ? 1 : -1;
+        if (p->p.sds[k] != want) continue;
+        CK(launch_pair_s2f((double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, (const double *)so->fa, so->X, so->Y, so->Z,
+                           so->tau, p->p, k, vf, so->d.dh, fa->st));
+    }
+    CK(cudaStreamSynchronize(fa->st));
+    return FSI_OK;
+}
+
+}  // extern "C"

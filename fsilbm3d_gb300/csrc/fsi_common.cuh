@@ -1,0 +1,111 @@
+// fsi_common.cuh -- D3Q19 lattice tables and kernel argument structs shared
+// by the CUDA translation units of libfsi_gpu.
+//
+// Lattice: ConstParams.f90:9-34 (directions ee, opposites oppo, weights wt,
+// boundary codes). Distribution layout on the device is the reference's
+// Fortran fIn(z,y,x,0:18): element (z,y,x,q) at z + Z*(y + Y*(x + X*q)).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fsi {
+
+constexpr int Q = 19;
+
+__host__ __device__ constexpr int ex_(int i) {
+    return (i == 1 || i == 7 || i == 9 || i == 11 || i == 13) ? 1
+         : (i == 2 || i == 8 || i == 10 || i == 12 || i == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int ey_(int i) {
+    return (i == 3 || i == 7 || i == 8 || i == 15 || i == 17) ? 1
+         : (i == 4 || i == 9 || i == 10 || i == 16 || i == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int ez_(int i) {
+    return (i == 5 || i == 11 || i == 12 || i == 15 || i == 16) ? 1
+         : (i == 6 || i == 13 || i == 14 || i == 17 || i == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int opp_(int i) {
+    return i == 0 ? 0 : ((i <= 6) ? ((i % 2) ? i + 1 : i - 1)
+                                  : (i <= 10 ? 17 - i : (i <= 14 ? 25 - i : 33 - i)));
+}
+// weights as exact binary64 values of 1/3, 1/18, 1/36
+__host__ __device__ constexpr double wt_(int i) {
+    return i == 0 ? 1.0 / 3.0 : (i <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
+}
+
+// incoming population sets per face (x-, x+, y-, y+, z-, z+), FluidDomain.f90:645-1065
+__host__ __device__ constexpr int inc_(int k, int j) {
+    return k == 0 ? (j == 0 ? 1 : j == 1 ? 7 : j == 2 ? 9 : j == 3 ? 11 : 13)
+         : k == 1 ? (j == 0 ? 2 : j == 1 ? 8 : j == 2 ? 10 : j == 3 ? 12 : 14)
+         : k == 2 ? (j == 0 ? 3 : j == 1 ? 7 : j == 2 ? 8 : j == 3 ? 15 : 17)
+         : k == 3 ? (j == 0 ? 4 : j == 1 ? 9 : j == 2 ? 10 : j == 3 ? 16 : 18)
+         : k == 4 ? (j == 0 ? 5 : j == 1 ? 11 : j == 2 ? 12 : j == 3 ? 15 : 16)
+                  : (j == 0 ? 6 : j == 1 ? 13 : j == 2 ? 14 : j == 3 ? 17 : 18);
+}
+// the symmetric (302) source of incoming population j of face k: the mirror
+// across the face normal (FluidDomain.f90:697,781,865,949,1033,1117)
+// (the incoming set of the opposite face, in the same order)
+__host__ __device__ constexpr int mir_(int k, int j) { return inc_(k ^ 1, j); }
+
+// boundary codes, ConstParams.f90:31-34
+enum : int {
+    BC_EQ = 101, BC_NEQ = 102, BC_EXT1 = 103, BC_EXT2 = 104,
+    BC_WALL = 201, BC_MWALL = 202, BC_WALL_HW = 203, BC_MWALL_HW = 204,
+    BC_PERIODIC = 301, BC_SYMMETRIC = 302, BC_FLUID = 0, BC_FLUID_FATHER = 1
+};
+
+// inflow-velocity model of evaluate_velocity (FluidDomain.f90:1791-1824).
+// kind 0: shear profile evaluated per point; kind 2: spatially uniform value
+// osc (computed on the host with the host cos()).
+struct Vel {
+    int kind;
+    double vin[3];
+    double sr[3];
+    double osc[3];
+};
+
+// IB window: the box of cells whose den/u/force come from the IB stage
+struct Win {
+    int x0, x1, y0, y1, z0, z1;   // inclusive, 0-based; x1 < x0 means empty
+    int WY, WZ;
+    long long n;
+    const double *den;  // n
+    const double *u;    // 3n
+    const double *force;// 3n
+};
+
+// MRT matrices passed by value (kernel parameter space, uniform reads)
+struct MrtMats {
+    double mc[361];       // M_COLLID, column-major
+    double mf[361];       // M_FORCE
+};
+
+struct StepArgs {
+    const void *src;
+    void *dst;
+    int X, Y, Z;
+    long long N;
+    double dh, omega;
+    double vf[3];
+    Win win;
+    double *hw[6];        // half-way face copies (19 per face cell), NULL = off
+    double *den;          // full-size den/u, written on layer-2 planes of 102 faces
+    double *u;
+    int l2[6];            // 1 if face k has code 102
+};
+
+struct BcArgs {
+    void *f;
+    int X, Y, Z;
+    long long N;
+    int face;             // 0..5
+    int code;
+    double dh, xmin, ymin, zmin, xmax, ymax, zmax;
+    double denIn;
+    Vel vel;
+    const double *hw;     // half-way copy of this face
+    const double *den;    // full-size den/u (102)
+    const double *u;
+};
+
+}  // namespace fsi

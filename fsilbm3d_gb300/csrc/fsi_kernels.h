@@ -1,0 +1,69 @@
+// fsi_kernels.h -- host-side launchers of the CUDA kernels of libfsi_gpu.
+// Each launcher enqueues on `st` and returns the launch status.
+#pragma once
+#include "fsi_common.cuh"
+
+namespace fsi {
+
+// ---- exact FP64 translation unit (k_f64_exact.cu, built with -fmad=false) ----
+cudaError_t launch_init_f64(double *f, double *den, double *u, int X, int Y, int Z,
+                            double dh, double xmin, double ymin, double zmin,
+                            double denIn, const Vel &vel, double blktime, cudaStream_t st);
+cudaError_t launch_macro_f64(const double *f, double *den, double *u, int X, int Y, int Z,
+                             double dh, const double vf[3], cudaStream_t st);
+cudaError_t launch_step_f64_exact(const StepArgs &a, const MrtMats *mm, int model, cudaStream_t st);
+cudaError_t launch_bc_f64(const BcArgs &a, cudaStream_t st);
+cudaError_t launch_halfway_f64(const double *f, double *hw, int X, int Y, int Z, int face,
+                               cudaStream_t st);
+
+// IB (exact order)
+struct IbGeom {
+    int X, Y, Z;
+    double dh, xmin, ymin, zmin;
+    int bc[6];
+    int wx0, wx1, wy0, wy1, wz0, wz1, WY, WZ;
+};
+cudaError_t launch_win_macro_f64(const void *f, int prec, double *wden, double *wu,
+                                 const IbGeom &g, long long N, const double vf[3], cudaStream_t st);
+cudaError_t launch_ib_stencil(const double *xyz, const int *offs, int nb, int Mtot, const IbGeom &g,
+                              int16_t *ei, float *ew, int *err, cudaStream_t st);
+cudaError_t launch_ib_csr(const int16_t *ei, int Mtot, const IbGeom &g, long long Nw,
+                          int *cnt, int *start, int *fillc, int *list, cudaStream_t st);
+cudaError_t launch_ib_interp(const int16_t *ei, const float *ew, const double *vel, const double *area,
+                             const double *wu, const IbGeom &g, int m0, int m1, double invh3,
+                             double *eforce, double *fet, double *tolm, cudaStream_t st);
+cudaError_t launch_ib_reduce(const double *tolm, int m0, int m1, double *out, cudaStream_t st);
+cudaError_t launch_ib_correct(const float *ew, const int *start, const int *list, long long Nw,
+                              int m0, int m1, const double *fet, double *wu, cudaStream_t st);
+cudaError_t launch_ib_spread(const float *ew, const int *start, const int *list, long long Nw,
+                             const double *eforce, double invh3, const double vf[3],
+                             double *wforce, cudaStream_t st);
+
+// ---- block refinement (k_f64_exact.cu) ----
+struct PairGeom {
+    int sds[6], s[6], f[6], si[6], fi[6];
+    int xDimS, xDimF, yDimS, yDimF, zDimS, zDimF;
+};
+cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f,
+                                const PairGeom &p, int face, double *buf, double *buft,
+                                cudaStream_t st);
+cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaStream_t st);
+cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const PairGeom &p,
+                            int face, const double *buf, const double *buft, int scheme,
+                            double *scratch_f, double *scratch_t, const double vf[3], double dh,
+                            cudaStream_t st);
+cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *fs,
+                            int SX, int SY, int SZ, double tau_s, const PairGeom &p, int face,
+                            const double vf[3], double dh, cudaStream_t st);
+
+// ---- fast kernels (k_fast.cu): FP64 regrouped, FP32/FP16/BF16 storage ----
+cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st);
+cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st);
+cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st);
+cudaError_t launch_convert_from_store(const void *fs, double *f64, long long N, int prec, cudaStream_t st);
+cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, int X, int Y, int Z, double dh,
+                              const double vf[3], cudaStream_t st);
+cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double *wu, const IbGeom &g, long long N,
+                                  const double vf[3], cudaStream_t st);
+
+}  // namespace fsi

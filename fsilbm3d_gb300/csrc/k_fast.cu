@@ -1,0 +1,401 @@
+// k_fast.cu -- the throughput forms of the fused collide+stream step.
+//
+//  FSI_PREC_F64_FAST  FP64 storage of f, FP64 arithmetic regrouped around the
+//                     nine opposite-direction pairs (ConstParams.f90:19-20)
+//                     with fused multiply-add.
+//  FSI_PREC_F32/F16/BF16
+//                     storage of the offsets g_i = f_i - w_i (w_i: lattice
+//                     weights, ConstParams.f90:22-25) in FP32, FP16 or BF16;
+//                     all arithmetic in FP32 on the offsets, so that the
+//                     density enters as 1 + sum(g) and no precision is spent
+//                     on the constant part of f.
+//
+// Physics and step order are those of the exact form (collision_ SRT/MRT
+// with Guo forcing, FluidDomain.f90:1208-1238; streaming_ :1514-1625; the
+// IB window and face hooks of k_f64_exact.cu); only rounding differs.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "bc_impl.cuh"
+#include "fsi_kernels.h"
+#include "../../include/fsi_gpu.h"
+
+namespace fsi {
+namespace {
+
+constexpr int TPB = 256;
+
+template <int P> struct ST;
+template <> struct ST<FSI_PREC_F64_FAST> {
+    using S = double; using C = double;
+    static constexpr bool OFF = false;
+    static __device__ __forceinline__ C dec(S s) { return s; }
+    static __device__ __forceinline__ S enc(C c) { return c; }
+};
+template <> struct ST<FSI_PREC_F32> {
+    using S = float; using C = float;
+    static constexpr bool OFF = true;
+    static __device__ __forceinline__ C dec(S s) { return s; }
+    static __device__ __forceinline__ S enc(C c) { return c; }
+};
+template <> struct ST<FSI_PREC_F16> {
+    using S = __half; using C = float;
+    static constexpr bool OFF = true;
+    static __device__ __forceinline__ C dec(S s) { return __half2float(s); }
+    static __device__ __forceinline__ S enc(C c) { return __float2half_rn(c); }
+};
+template <> struct ST<FSI_PREC_BF16> {
+    using S = __nv_bfloat16; using C = float;
+    static constexpr bool OFF = true;
+    static __device__ __forceinline__ C dec(S s) { return __bfloat162float(s); }
+    static __device__ __forceinline__ S enc(C c) { return __float2bfloat16_rn(c); }
+};
+
+// accessor for the boundary kernels: FP64 distribution values in and out
+template <int P> struct AccS {
+    using T = ST<P>;
+    static __device__ __forceinline__ double load(const void *f, long long i, int q) {
+        double v = (double)T::dec(((const typename T::S *)f)[i]);
+        return T::OFF ? v + wt_(q) : v;
+    }
+    static __device__ __forceinline__ void store(void *f, long long i, int q, double v) {
+        ((typename T::S *)f)[i] = T::enc((typename T::C)(T::OFF ? v - wt_(q) : v));
+    }
+};
+
+__device__ __forceinline__ long long cidx(int z, int y, int x, int Z, int Y) {
+    return (long long)z + (long long)Z * ((long long)y + (long long)Y * (long long)x);
+}
+
+// +v, -v or the additive identity -0 for lattice component e
+template <typename C> __device__ __forceinline__ C sel(int e, C v) { return e > 0 ? v : (e < 0 ? -v : C(-0.0)); }
+
+// representatives of the nine opposite pairs (positivedirs, ConstParams.f90:19)
+__host__ __device__ constexpr int pr_(int k) {
+    return k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 5 : k == 3 ? 7 : k == 4 ? 8 : k == 5 ? 11 : k == 6 ? 12 : k == 7 ? 15 : 16;
+}
+
+// density (and its offset from 1) and velocity of one cell,
+// calculate_macro_quantities_ (FluidDomain.f90:1136-1139) regrouped
+template <int P>
+__device__ __forceinline__ void macro_fast(const typename ST<P>::C g[Q], const typename ST<P>::C vf[3],
+                                           typename ST<P>::C dh, typename ST<P>::C &rho, typename ST<P>::C &drho,
+                                           typename ST<P>::C &u0, typename ST<P>::C &u1, typename ST<P>::C &u2) {
+    using C = typename ST<P>::C;
+    C s = g[0], jx = C(-0.0), jy = C(-0.0), jz = C(-0.0);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int i = pr_(k), o = opp_(i);
+        const C sk = g[i] + g[o], dk = g[i] - g[o];
+        s += sk;
+        jx += sel(ex_(i), dk);
+        jy += sel(ey_(i), dk);
+        jz += sel(ez_(i), dk);
+    }
+    if (ST<P>::OFF) { drho = s; rho = C(1) + s; }
+    else { rho = s; drho = s - C(1); }
+    const C inv = C(1) / rho;
+    const C h = C(0.5) * dh;
+    u0 = (jx + h * vf[0]) * inv;
+    u1 = (jy + h * vf[1]) * inv;
+    u2 = (jz + h * vf[2]) * inv;
+}
+
+// SRT/BGK with Guo forcing (FluidDomain.f90:1218-1227) on pairs
+template <int P, bool FORCED>
+__device__ __forceinline__ void collide_srt(typename ST<P>::C g[Q], typename ST<P>::C rho, typename ST<P>::C drho,
+                                            typename ST<P>::C u0, typename ST<P>::C u1, typename ST<P>::C u2,
+                                            typename ST<P>::C F0, typename ST<P>::C F1, typename ST<P>::C F2,
+                                            typename ST<P>::C om, typename ST<P>::C dh3) {
+    using C = typename ST<P>::C;
+    constexpr bool OFF = ST<P>::OFF;
+    const C usq = u0 * u0 + u1 * u1 + u2 * u2;
+    const C k15 = C(1.5) * usq;
+    const C cf = (C(1) - C(0.5) * om) * dh3;
+    C uF = C(0);
+    if (FORCED) uF = u0 * F0 + u1 * F1 + u2 * F2;
+    {
+        const C w = C(wt_(0));
+        const C eq = OFF ? w * (drho - rho * k15) : (w * rho) * (C(1) - k15);
+        g[0] = g[0] + om * (eq - g[0]);
+        if (FORCED) g[0] = g[0] - (cf * w) * uF;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int i = pr_(k), o = opp_(i);
+        const C w = C(wt_(i));
+        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C wr = w * rho;
+        const C sym = OFF ? w * drho + wr * (C(4.5) * eu * eu - k15) : wr * ((C(1) - k15) + C(4.5) * eu * eu);
+        const C asym = (C(3) * wr) * eu;
+        const C gi = g[i], go = g[o];
+        C ni = gi + om * ((sym + asym) - gi);
+        C no = go + om * ((sym - asym) - go);
+        if (FORCED) {
+            const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+            const C cw = cf * w;
+            const C Fs = cw * (C(3) * eu * eF - uF), Fa = cw * eF;
+            ni += Fs + Fa;
+            no += Fs - Fa;
+        }
+        g[i] = ni;
+        g[o] = no;
+    }
+}
+
+template <typename C> struct MatsT { C mc[361]; C mf[361]; };
+
+// MRT (FluidDomain.f90:1236-1238): g += M_COLLID (feq - f) + M_FORCE Flb
+template <int P>
+__device__ __forceinline__ void collide_mrt(typename ST<P>::C g[Q], typename ST<P>::C rho, typename ST<P>::C drho,
+                                            typename ST<P>::C u0, typename ST<P>::C u1, typename ST<P>::C u2,
+                                            typename ST<P>::C F0, typename ST<P>::C F1, typename ST<P>::C F2,
+                                            bool forced, typename ST<P>::C dh3,
+                                            const MatsT<typename ST<P>::C> &mm) {
+    using C = typename ST<P>::C;
+    constexpr bool OFF = ST<P>::OFF;
+    const C usq = u0 * u0 + u1 * u1 + u2 * u2;
+    const C k15 = C(1.5) * usq;
+    C neq[Q], flb[Q];
+    const C uF = u0 * F0 + u1 * F1 + u2 * F2;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const C w = C(wt_(i));
+        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eq = OFF ? w * drho + (w * rho) * ((C(3) + C(4.5) * eu) * eu - k15)
+                         : (w * rho) * ((C(1) - k15) + (C(3) + C(4.5) * eu) * eu);
+        neq[i] = eq - g[i];
+        const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+        flb[i] = (dh3 * w) * (eF - uF + C(3) * eu * eF);
+    }
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        C s = g[i];
+#pragma unroll
+        for (int j = 0; j < Q; j++) s += mm.mc[i + Q * j] * neq[j];
+        if (forced) {
+#pragma unroll
+            for (int j = 0; j < Q; j++) s += mm.mf[i + Q * j] * flb[j];
+        }
+        g[i] = s;
+    }
+}
+
+template <int P, int MODEL>
+__global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST<P>::C> mm) {
+    using T = ST<P>;
+    using S = typename T::S;
+    using C = typename T::C;
+    int z = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    int x = blockIdx.z;
+    if (z >= a.Z || y >= a.Y) return;
+    const int X = a.X, Y = a.Y, Z = a.Z;
+    const long long N = a.N;
+    const long long c = cidx(z, y, x, Z, Y);
+    const S *__restrict__ src = (const S *)a.src;
+    S *__restrict__ dst = (S *)a.dst;
+
+    C g[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) g[i] = T::dec(src[c + N * i]);
+
+    C rho, drho, u0, u1, u2, F0, F1, F2;
+    bool forced;
+    const Win &w = a.win;
+    if (x >= w.x0 && x <= w.x1 && y >= w.y0 && y <= w.y1 && z >= w.z0 && z <= w.z1) {
+        long long wc = (long long)(z - w.z0) + (long long)w.WZ * ((long long)(y - w.y0) + (long long)w.WY * (x - w.x0));
+        const double d = w.den[wc];
+        if (T::OFF) { drho = (C)(d - 1.0); rho = C(1) + drho; }
+        else { rho = (C)d; drho = rho - C(1); }
+        u0 = (C)w.u[wc]; u1 = (C)w.u[wc + w.n]; u2 = (C)w.u[wc + 2 * w.n];
+        F0 = (C)w.force[wc]; F1 = (C)w.force[wc + w.n]; F2 = (C)w.force[wc + 2 * w.n];
+        forced = true;
+    } else {
+        const C vf[3] = {(C)a.vf[0], (C)a.vf[1], (C)a.vf[2]};
+        macro_fast<P>(g, vf, (C)a.dh, rho, drho, u0, u1, u2);
+        F0 = vf[0]; F1 = vf[1]; F2 = vf[2];
+        forced = (a.vf[0] != 0.0) || (a.vf[1] != 0.0) || (a.vf[2] != 0.0);
+    }
+    if ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
+        (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2)) {
+        a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
+        a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
+    }
+    const C om = (C)a.omega, dh3 = C(3) * (C)a.dh;
+    if (MODEL == 1) {
+        if (forced) collide_srt<P, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, om, dh3);
+        else collide_srt<P, false>(g, rho, drho, u0, u1, u2, F0, F1, F2, om, dh3);
+    } else {
+        collide_mrt<P>(g, rho, drho, u0, u1, u2, F0, F1, F2, forced, dh3, mm);
+    }
+
+    // halfwayBCset_ (FluidDomain.f90:567-614): post-collision faces as FP64 f
+#define FSI_HW(K, COND, OFS)                                                       \
+    if (a.hw[K] && (COND)) {                                                       \
+        double *h = a.hw[K] + (long long)Q * (OFS);                                \
+        _Pragma("unroll") for (int i = 0; i < Q; i++)                              \
+            h[i] = T::OFF ? (double)g[i] + wt_(i) : (double)g[i];                  \
+    }
+    FSI_HW(0, x == 0, z + (long long)Z * y)
+    FSI_HW(1, x == X - 1, z + (long long)Z * y)
+    FSI_HW(2, y == 0, z + (long long)Z * x)
+    FSI_HW(3, y == Y - 1, z + (long long)Z * x)
+    FSI_HW(4, z == 0, y + (long long)Y * x)
+    FSI_HW(5, z == Z - 1, y + (long long)Y * x)
+#undef FSI_HW
+
+    const int zp = (z + 1 == Z) ? 0 : z + 1, zm = (z == 0) ? Z - 1 : z - 1;
+    const int yp = (y + 1 == Y) ? 0 : y + 1, ym = (y == 0) ? Y - 1 : y - 1;
+    const int xp = (x + 1 == X) ? 0 : x + 1, xm = (x == 0) ? X - 1 : x - 1;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const int zd = ez_(i) > 0 ? zp : (ez_(i) < 0 ? zm : z);
+        const int yd = ey_(i) > 0 ? yp : (ey_(i) < 0 ? ym : y);
+        const int xd = ex_(i) > 0 ? xp : (ex_(i) < 0 ? xm : x);
+        dst[cidx(zd, yd, xd, Z, Y) + N * i] = T::enc(g[i]);
+    }
+}
+
+template <int P>
+__global__ void k_macro_fast(const void *__restrict__ fs, double *den, double *u, int Y, int Z, long long N, double dh,
+                             double vf0, double vf1, double vf2) {
+    using T = ST<P>;
+    using C = typename T::C;
+    int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
+    if (z >= Z) return;
+    long long c = cidx(z, y, x, Z, Y);
+    const typename T::S *src = (const typename T::S *)fs;
+    C g[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) g[i] = T::dec(src[c + N * i]);
+    const C vf[3] = {(C)vf0, (C)vf1, (C)vf2};
+    C rho, drho, u0, u1, u2;
+    macro_fast<P>(g, vf, (C)dh, rho, drho, u0, u1, u2);
+    den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
+    u[c] = u0; u[c + N] = u1; u[c + 2 * N] = u2;
+}
+
+template <int P>
+__global__ void k_win_macro_fast(const void *__restrict__ fs, double *wden, double *wu, IbGeom g, long long N,
+                                 long long Nw, double vf0, double vf1, double vf2) {
+    using T = ST<P>;
+    using C = typename T::C;
+    long long wc = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (wc >= Nw) return;
+    int wz = (int)(wc % g.WZ);
+    long long t = wc / g.WZ;
+    int wy = (int)(t % g.WY), wx = (int)(t / g.WY);
+    long long c = cidx(wz + g.wz0, wy + g.wy0, wx + g.wx0, g.Z, g.Y);
+    const typename T::S *src = (const typename T::S *)fs;
+    C gl[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) gl[i] = T::dec(src[c + N * i]);
+    const C vf[3] = {(C)vf0, (C)vf1, (C)vf2};
+    C rho, drho, u0, u1, u2;
+    macro_fast<P>(gl, vf, (C)g.dh, rho, drho, u0, u1, u2);
+    wden[wc] = T::OFF ? 1.0 + (double)drho : (double)rho;
+    wu[wc] = u0; wu[wc + Nw] = u1; wu[wc + 2 * Nw] = u2;
+}
+
+template <int P>
+__global__ void k_to_store(const double *__restrict__ f, void *fs, long long N) {
+    using T = ST<P>;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= N * Q) return;
+    int q = (int)(i / N);
+    double v = f[i];
+    ((typename T::S *)fs)[i] = T::enc((typename T::C)(T::OFF ? v - wt_(q) : v));
+}
+
+template <int P>
+__global__ void k_from_store(const void *__restrict__ fs, double *f, long long N) {
+    using T = ST<P>;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= N * Q) return;
+    int q = (int)(i / N);
+    double v = (double)T::dec(((const typename T::S *)fs)[i]);
+    f[i] = T::OFF ? v + wt_(q) : v;
+}
+
+template <int P, int MODEL>
+cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
+    using C = typename ST<P>::C;
+    MatsT<C> m{};
+    if (MODEL == 3)
+        for (int i = 0; i < 361; i++) { m.mc[i] = (C)mm->mc[i]; m.mf[i] = (C)mm->mf[i]; }
+    int bz = a.Z >= 128 ? 128 : ((a.Z + 31) / 32) * 32;
+    int by = TPB / bz;
+    if (by < 1) by = 1;
+    dim3 blk(bz, by), grd((a.Z + bz - 1) / bz, (a.Y + by - 1) / by, a.X);
+    k_step_fast<P, MODEL><<<grd, blk, 0, st>>>(a, m);
+    return cudaGetLastError();
+}
+
+template <int P>
+cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
+    const int A = (a.face < 4) ? a.Z : a.Y;
+    const int B = (a.face < 2) ? a.Y : a.X;
+    dim3 blk(64, 4), grd((A + 63) / 64, (B + 3) / 4);
+    switch (a.face) {
+    case 0: k_bc<AccS<P>, 0><<<grd, blk, 0, st>>>(a); break;
+    case 1: k_bc<AccS<P>, 1><<<grd, blk, 0, st>>>(a); break;
+    case 2: k_bc<AccS<P>, 2><<<grd, blk, 0, st>>>(a); break;
+    case 3: k_bc<AccS<P>, 3><<<grd, blk, 0, st>>>(a); break;
+    case 4: k_bc<AccS<P>, 4><<<grd, blk, 0, st>>>(a); break;
+    default: k_bc<AccS<P>, 5><<<grd, blk, 0, st>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+#define FSI_DISPATCH(prec, ...)                                                    \
+    switch (prec) {                                                                \
+    case FSI_PREC_F64_FAST: { constexpr int PP = FSI_PREC_F64_FAST; __VA_ARGS__; } \
+    case FSI_PREC_F32: { constexpr int PP = FSI_PREC_F32; __VA_ARGS__; }           \
+    case FSI_PREC_F16: { constexpr int PP = FSI_PREC_F16; __VA_ARGS__; }           \
+    case FSI_PREC_BF16: { constexpr int PP = FSI_PREC_BF16; __VA_ARGS__; }         \
+    default: return cudaErrorInvalidValue;                                         \
+    }
+
+cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st) {
+    if (model == 3) { FSI_DISPATCH(prec, return (step_inst<PP, 3>(a, mm, st))) }
+    FSI_DISPATCH(prec, return (step_inst<PP, 1>(a, mm, st)))
+}
+
+cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
+    FSI_DISPATCH(prec, return bc_inst<PP>(a, st))
+}
+
+cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st) {
+    long long n = N * Q;
+    unsigned nb = (unsigned)((n + 255) / 256);
+    FSI_DISPATCH(prec, k_to_store<PP><<<nb, 256, 0, st>>>(f64, fs, N); return cudaGetLastError())
+}
+
+cudaError_t launch_convert_from_store(const void *fs, double *f64, long long N, int prec, cudaStream_t st) {
+    long long n = N * Q;
+    unsigned nb = (unsigned)((n + 255) / 256);
+    FSI_DISPATCH(prec, k_from_store<PP><<<nb, 256, 0, st>>>(fs, f64, N); return cudaGetLastError())
+}
+
+cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, int X, int Y, int Z, double dh,
+                              const double vf[3], cudaStream_t st) {
+    int bz = Z >= 256 ? 256 : ((Z + 31) / 32) * 32;
+    dim3 g((Z + bz - 1) / bz, Y, X);
+    long long N = (long long)X * Y * Z;
+    FSI_DISPATCH(prec, k_macro_fast<PP><<<g, bz, 0, st>>>(fs, den, u, Y, Z, N, dh, vf[0], vf[1], vf[2]);
+                 return cudaGetLastError())
+}
+
+cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double *wu, const IbGeom &g, long long N,
+                                  const double vf[3], cudaStream_t st) {
+    long long Nw = (long long)(g.wx1 - g.wx0 + 1) * g.WY * g.WZ;
+    if (Nw <= 0) return cudaSuccess;
+    unsigned nb = (unsigned)((Nw + 255) / 256);
+    FSI_DISPATCH(prec, k_win_macro_fast<PP><<<nb, 256, 0, st>>>(fs, wden, wu, g, N, Nw, vf[0], vf[1], vf[2]);
+                 return cudaGetLastError())
+}
+
+}  // namespace fsi

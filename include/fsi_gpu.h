@@ -1,0 +1,157 @@
+/*
+ * fsi_gpu.h -- C-ABI of the GB300 (sm_103a) implementation of FSILBM3D's
+ * per-time-step hot path: D3Q19 collide-stream, face boundary conditions,
+ * block-refinement face exchange and immersed-boundary coupling.
+ *
+ * The reference has no plugin or FFI layer: its hot path is a set of
+ * Fortran type-bound procedures called from the tree recursion in
+ * LBMBlockComm.f90:279-338. Each entry point below replaces the body of one
+ * or more of those procedures; the comment on each names the reference
+ * routine (file:line) it stands in for. A Fortran host binds these through
+ * ISO_C_BINDING; any C, C++ or Python (ctypes) host can
+ * call them directly.
+ *
+ * Conventions
+ *  - Every function returns FSI_OK (0) or a negative FSI_E_* code; the
+ *    message of the last failure on the calling thread is available from
+ *    fsi_last_error(). No function calls exit(), abort() or a device trap:
+ *    where the reference stops (e.g. Solidbody.f90:1028-1031 on NaN,
+ *    FluidDomain.f90:704 on an unknown boundary code) the call returns an
+ *    error code and the caller decides.
+ *  - Host arrays are plain pointers in the reference's Fortran layout:
+ *    fIn(z,y,x,0:18), uuu(z,y,x,1:3), den(z,y,x) column-major, marker arrays
+ *    (3,M) column-major. Indices are 0-based in C; the stencil indices
+ *    returned by fsi_ib_get_stencil keep the reference's 1-based values.
+ *  - Calls are synchronous at the ABI level unless stated otherwise; a
+ *    handle is used by one host thread at a time.
+ *  - Device memory is owned by the handle; host memory by the caller.
+ */
+#ifndef FSI_GPU_H
+#define FSI_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSI_OK         0
+#define FSI_E_ARG     -1   /* invalid argument or unsupported option        */
+#define FSI_E_CUDA    -2   /* CUDA runtime error                            */
+#define FSI_E_NAN     -3   /* non-finite IB residual (Solidbody.f90:1028)   */
+#define FSI_E_TIMEOUT -4   /* a bounded device wait ran out                 */
+#define FSI_E_BC      -5   /* unknown boundary code (FluidDomain.f90:704)   */
+#define FSI_E_RANGE   -6   /* IB stencil leaves the block (Solidbody.f90:850) */
+#define FSI_E_STATE   -7   /* call order violated                           */
+
+/* Storage / arithmetic forms of the distributions. */
+#define FSI_PREC_F64       0  /* FP64 storage, FP64 arithmetic in the reference's
+                                 operation order (no fused multiply-add): bitwise
+                                 equal to an FP64 CPU run of the same order     */
+#define FSI_PREC_F64_FAST  1  /* FP64 storage and arithmetic, regrouped with FMA */
+#define FSI_PREC_F32       2  /* FP32 storage of f - w_i, FP32 arithmetic        */
+#define FSI_PREC_F16       3  /* FP16 storage of f - w_i, FP32 arithmetic        */
+#define FSI_PREC_BF16      4  /* BF16 storage of f - w_i, FP32 arithmetic        */
+
+typedef struct fsi_block *fsi_block_t;
+
+/* Parameters of one LBM block: LBMBlock (FluidDomain.f90:17-56), the block
+ * section of inFlow.dat (FluidDomain.f90:61-108) and the flow conditions the
+ * hot path reads (FlowCondition.f90:11-26). */
+typedef struct {
+    int    xDim, yDim, zDim;
+    double dh, xmin, ymin, zmin;
+    int    bndConds[6];      /* x-, x+, y-, y+, z-, z+ codes (ConstParams.f90:31-34) */
+    int    iCollidModel;     /* 1 SRT/BGK, 3 MRT */
+    double nu;               /* flow%nu; tau = nu/(dh/3) + 1/2 (FluidDomain.f90:452) */
+    const double *m_collid;  /* optional 19x19 column-major M_COLLID (NULL: built here) */
+    const double *m_force;   /* optional 19x19 column-major M_FORCE  (NULL: built here) */
+    int    precision;        /* FSI_PREC_* */
+    double denIn;
+    double uvwIn[3];
+    double shearRateIn[3];
+    int    velocityKind;     /* 0 shear profile, 2 oscillatory (FluidDomain.f90:1791-1824) */
+} fsi_block_desc;
+
+/* message of the last error on this thread ("" if none); returns its length */
+int fsi_last_error(char *buf, int len);
+
+/* library and device information: sm count, arch, build flags */
+int fsi_device_info(int *sm_count, int *cc_major, int *cc_minor);
+
+/* allocate_fluid_ + calculate_SRT/MRT_params (FluidDomain.f90:378-522) */
+int fsi_block_create(fsi_block_t *out, const fsi_block_desc *desc);
+int fsi_block_destroy(fsi_block_t h);
+
+/* tau, Omega and the MRT matrices in use (FluidDomain.f90:450-522) */
+int fsi_block_get_params(fsi_block_t h, double *tau, double *omega,
+                         double *m_collid, double *m_force);
+
+/* copy fIn(z,y,x,0:18) between host and device (write_continue_/read_continue_,
+ * FluidDomain.f90:1770-1789, keep this exact layout) */
+int fsi_block_upload_f(fsi_block_t h, const double *fIn);
+int fsi_block_download_f(fsi_block_t h, double *fIn);
+
+/* initialise_flow: den = denIn, uuu = inflow profile, fIn = feq (FluidDomain.f90:524-544) */
+int fsi_block_initialise(fsi_block_t h, double time);
+
+/* set_boundary_conditions_ on the current state (FluidDomain.f90:616-1126);
+ * the first call marks half-way faces ready without applying them, as the
+ * reference's allocate-on-first-call does (FluidDomain.f90:660-662) */
+int fsi_block_set_boundary_conditions(fsi_block_t h, double blktime);
+
+/* calculate_macro_quantities_ over the whole block (FluidDomain.f90:1128-1145);
+ * den (N) and uuu (3N) are written to the host if non-NULL */
+int fsi_block_macro(fsi_block_t h, const double vf[3], double *den, double *uuu);
+
+/* The fluid part of one time step, LBMBlockComm.f90:288-303:
+ * add_volume_force_ (FluidDomain.f90:1182), collision_ (:1208),
+ * halfwayBCset_ (:567), streaming_ (:1514), set_boundary_conditions_ (:616).
+ * macro (:1128) and ResetVolumeForce_ (:1195) are folded in: cells outside
+ * the IB window take den/u from their own distributions and force = vf;
+ * cells inside take the IB-corrected values from the last fsi_ib_solve. */
+int fsi_block_step(fsi_block_t h, const double vf[3], double blktime);
+
+/* run nsteps of fsi_block_step with constant vf and blktime advanced by dh per
+ * step, launched from a captured CUDA graph; *ms = device time (CUDA events) */
+int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps, float *ms);
+
+/* Immersed boundary (Solidbody.f90:869-1049). Bodies are stored back to back:
+ * marker m of body b is global marker offs[b]+m, offs = prefix sums of M. */
+int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6]);
+
+/* One call per time step (FSInteraction_force -> calculate_interaction_force,
+ * Solidbody.f90:589-918, for a block's carried bodies): UpdateElmtInterp_
+ * (:760), macro and force reset in the IB window, the PenaltyForce_ loop
+ * (:893-906, at most ntol iterations, stop when residual <= dtol) and the
+ * spreading of FluidVolumeForce_ (:968-977), then add_volume_force_.
+ * xyz/vel (3,Mtot), area (Mtot) in; eforce (3,Mtot) out (v_Eforce, FP64);
+ * iters and residual out (both may be NULL). */
+int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const double *area,
+                 const double vf[3], double denIn, double dt, double Uref,
+                 int ntol, double dtol, double *eforce, int *iters, double *residual);
+
+/* the stencil of the last fsi_ib_solve: v_Ei (12,Mtot) 1-based, v_Ew (12,Mtot) */
+int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew);
+
+/* the IB window of the last fsi_ib_solve (0-based inclusive x0,x1,y0,y1,z0,z1) */
+int fsi_ib_get_window(fsi_block_t h, int box[6]);
+
+/* Block refinement, LBMBlockComm.f90:340-979. A pair links a father and a
+ * son block; the son's faces with code 0 (BCfluid) receive father data. */
+typedef struct fsi_pair *fsi_pair_t;
+/* build_blocks_comunication for one pair (LBMBlockComm.f90:42-92);
+ * scheme = flow%interpolateScheme (1 linear, 2 third/fourth order) */
+int fsi_pair_create(fsi_pair_t *out, fsi_block_t father, fsi_block_t son, int scheme);
+int fsi_pair_destroy(fsi_pair_t p);
+/* extract_interpolate_layer for this pair, time level 1 or 2 (LBMBlockComm.f90:340-505) */
+int fsi_pair_extract(fsi_pair_t p, int time_level);
+/* interpolation_father_to_son (LBMBlockComm.f90:655-806); vf = father volume force */
+int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]);
+/* deliver_son_to_father (LBMBlockComm.f90:546-653); vf = son volume force */
+int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSI_GPU_H */

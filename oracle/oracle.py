@@ -1,0 +1,226 @@
+"""ctypes binding of the CPU FP64 oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module. It restates FSILBM3D's hot path on the CPU (see fsi_oracle.h
+for the parity status) and is never part of the product path.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import build_oracle  # noqa: E402
+
+Q = 19
+
+
+class OrFlow(C.Structure):
+    _fields_ = [
+        ("denIn", C.c_double),
+        ("uvwIn", C.c_double * 3),
+        ("shearRateIn", C.c_double * 3),
+        ("velocityKind", C.c_int),
+        ("interpolateScheme", C.c_int),
+        ("volumeForceIn", C.c_double * 3),
+        ("volumeForceAmp", C.c_double),
+        ("volumeForceFreq", C.c_double),
+        ("volumeForcePhi", C.c_double),
+        ("nu", C.c_double),
+    ]
+
+
+DP = C.POINTER(C.c_double)
+
+
+class OrBlock(C.Structure):
+    _fields_ = [
+        ("X", C.c_int), ("Y", C.c_int), ("Z", C.c_int),
+        ("dh", C.c_double), ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double),
+        ("xmax", C.c_double), ("ymax", C.c_double), ("zmax", C.c_double),
+        ("bnd", C.c_int * 6),
+        ("periodic", C.c_int * 3),
+        ("model", C.c_int),
+        ("tau", C.c_double), ("omega", C.c_double),
+        ("mc", C.c_double * 361), ("mf", C.c_double * 361),
+        ("volumeForce", C.c_double * 3),
+        ("blktime", C.c_double),
+        ("f", DP), ("u", DP), ("den", DP), ("force", DP), ("tau_all", DP),
+        ("hw", DP * 6),
+        ("hw_ready", C.c_int * 6),
+    ]
+
+
+class OrBody(C.Structure):
+    _fields_ = [
+        ("M", C.c_int),
+        ("xyz", DP), ("vel", DP), ("area", DP), ("eforce", DP),
+        ("ei", C.POINTER(C.c_int16)), ("ew", C.POINTER(C.c_float)),
+    ]
+
+
+class OrPair(C.Structure):
+    _fields_ = [
+        ("sds", C.c_int * 6), ("s", C.c_int * 6), ("f", C.c_int * 6),
+        ("si", C.c_int * 6), ("fi", C.c_int * 6),
+        ("xDimS", C.c_int), ("xDimF", C.c_int), ("yDimS", C.c_int),
+        ("yDimF", C.c_int), ("zDimS", C.c_int), ("zDimF", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        BP, FP, BDP = C.POINTER(OrBlock), C.POINTER(OrFlow), C.POINTER(OrBody)
+        L.or_evaluate_velocity.argtypes = [FP, C.c_double, C.c_double, C.c_double, C.c_double, DP]
+        L.or_feq_dist.argtypes = [C.c_double, DP, DP]
+        L.or_mrt_matrices.argtypes = [C.c_double, DP, DP]
+        L.or_block_setup.argtypes = [BP, FP]
+        L.or_initialise_flow.argtypes = [BP, FP, C.c_double]
+        L.or_init_tgv.argtypes = [BP, C.c_double, C.c_double]
+        L.or_update_volume_force.argtypes = [BP, FP]
+        for name in ("or_macro", "or_reset_force", "or_add_force", "or_collide", "or_halfway_set"):
+            getattr(L, name).argtypes = [BP]
+        L.or_stream.argtypes = [BP, DP]
+        L.or_set_bc.argtypes = [BP, FP]
+        L.or_set_bc.restype = C.c_int
+        L.or_ib_stencil.argtypes = [BDP, BP]
+        L.or_ib_stencil.restype = C.c_int
+        L.or_ib_penalty.argtypes = [BDP, C.c_int, BP, C.c_double, C.c_double, C.c_double,
+                                    C.c_int, C.c_double, C.POINTER(C.c_int), DP]
+        L.or_ib_spread.argtypes = [BDP, C.c_int, BP]
+        L.or_step.argtypes = [BP, FP, BDP, C.c_int, C.c_double, C.c_int, C.c_double, DP,
+                              C.POINTER(C.c_int), DP]
+        L.or_step.restype = C.c_int
+        L.or_field_stat.argtypes = [BP, C.c_double, DP, DP]
+        L.or_build_pair.argtypes = [BP, BP, C.POINTER(OrPair)]
+        L.or_grid_transform.argtypes = [DP, C.c_double, DP, C.c_double]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(DP)
+
+
+def make_flow(denIn=1.0, uvwIn=(0.0, 0.0, 0.0), shearRateIn=(0.0, 0.0, 0.0), velocityKind=0,
+              interpolateScheme=1, volumeForceIn=(0.0, 0.0, 0.0), volumeForceAmp=0.0,
+              volumeForceFreq=0.0, volumeForcePhi=0.0, nu=0.01):
+    fl = OrFlow()
+    fl.denIn = denIn
+    fl.uvwIn[:] = list(uvwIn)
+    fl.shearRateIn[:] = list(shearRateIn)
+    fl.velocityKind = velocityKind
+    fl.interpolateScheme = interpolateScheme
+    fl.volumeForceIn[:] = list(volumeForceIn)
+    fl.volumeForceAmp = volumeForceAmp
+    fl.volumeForceFreq = volumeForceFreq
+    fl.volumeForcePhi = volumeForcePhi
+    fl.nu = nu
+    return fl
+
+
+class Block:
+    """One oracle block; numpy arrays in the reference's (z,y,x,q) order,
+    exposed with shape (q, x, y, z) in C order (same memory)."""
+
+    def __init__(self, X, Y, Z, dh, origin, bnd, model, flow, with_tau=True):
+        self.b = OrBlock()
+        b = self.b
+        b.X, b.Y, b.Z = X, Y, Z
+        b.dh = dh
+        b.xmin, b.ymin, b.zmin = origin
+        b.bnd[:] = list(bnd)
+        b.model = model
+        n = X * Y * Z
+        self.n = n
+        self.f = np.zeros(Q * n)
+        self.u = np.zeros(3 * n)
+        self.den = np.zeros(n)
+        self.force = np.zeros(3 * n)
+        self.tau_all = np.zeros(n) if with_tau else None
+        self.tmp = np.zeros(Q * n)
+        b.f, b.u, b.den, b.force = _dp(self.f), _dp(self.u), _dp(self.den), _dp(self.force)
+        b.tau_all = _dp(self.tau_all) if with_tau else DP()
+        self.hw = []
+        for k in range(6):
+            ax = k // 2
+            A, B = [(Z, Y), (Z, X), (Y, X)][ax]
+            h = np.zeros(Q * A * B)
+            self.hw.append(h)
+            b.hw[k] = _dp(h)
+        self.flow = flow
+        lib().or_block_setup(C.byref(b), C.byref(flow))
+
+    # views in (q, x, y, z) index order over the Fortran (z,y,x,q) memory
+    def fview(self):
+        return self.f.reshape(Q, self.b.X, self.b.Y, self.b.Z)
+
+    def initialise(self, time=0.0):
+        lib().or_initialise_flow(C.byref(self.b), C.byref(self.flow), time)
+
+    def init_tgv(self, u0, rho0=1.0):
+        lib().or_init_tgv(C.byref(self.b), u0, rho0)
+
+    def set_bc(self):
+        rc = lib().or_set_bc(C.byref(self.b), C.byref(self.flow))
+        if rc != 0:
+            raise RuntimeError("oracle: unknown boundary condition")
+
+    def macro(self):
+        lib().or_macro(C.byref(self.b))
+
+    def step(self, bodies=(), Uref=1.0, ntol=0, dtol=0.0):
+        arr = (OrBody * max(1, len(bodies)))()
+        for i, bd in enumerate(bodies):
+            arr[i] = bd.s
+        it = C.c_int(0)
+        res = C.c_double(0.0)
+        rc = lib().or_step(C.byref(self.b), C.byref(self.flow), arr, len(bodies), Uref, ntol, dtol,
+                           _dp(self.tmp), C.byref(it), C.byref(res))
+        if rc != 0:
+            raise RuntimeError("oracle step failed (%d)" % rc)
+        return it.value, res.value
+
+    def field_stat(self, Uref):
+        l2 = np.zeros(3)
+        li = np.zeros(3)
+        lib().or_field_stat(C.byref(self.b), Uref, _dp(l2), _dp(li))
+        return l2, li
+
+
+class Body:
+    def __init__(self, xyz, vel, area):
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        self.vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        self.area = np.ascontiguousarray(area, dtype=np.float64).reshape(-1)
+        M = self.area.size
+        self.eforce = np.zeros(3 * M)
+        self.ei = np.zeros(12 * M, dtype=np.int16)
+        self.ew = np.zeros(12 * M, dtype=np.float32)
+        s = OrBody()
+        s.M = M
+        s.xyz, s.vel, s.area, s.eforce = _dp(self.xyz), _dp(self.vel), _dp(self.area), _dp(self.eforce)
+        s.ei = self.ei.ctypes.data_as(C.POINTER(C.c_int16))
+        s.ew = self.ew.ctypes.data_as(C.POINTER(C.c_float))
+        self.s = s
+
+
+def feq(density, vel):
+    out = np.zeros(Q)
+    v = np.asarray(vel, dtype=np.float64)
+    lib().or_feq_dist(density, _dp(v), _dp(out))
+    return out
+
+
+def mrt_matrices(omega):
+    mc = np.zeros(361)
+    mf = np.zeros(361)
+    lib().or_mrt_matrices(omega, _dp(mc), _dp(mf))
+    return mc.reshape(19, 19, order="F"), mf.reshape(19, 19, order="F")

@@ -1,0 +1,201 @@
+"""GPU parity against the CPU oracle, through the C-ABI.
+
+FSI_PREC_F64 runs the reference's operation order without fused
+multiply-add, so its distributions, Lagrangian forces and stencils must be
+bitwise equal to the oracle's after every step. The other forms are checked
+against tolerances stated in each test.
+"""
+import numpy as np
+import pytest
+
+import fsilbm3d_gb300 as F
+from paired import Case, plate_in
+
+pytestmark = pytest.mark.gpu
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def first_diff(a, b):
+    d = np.argwhere(a.view(np.uint64) != b.view(np.uint64))
+    if d.size == 0:
+        return None
+    i = tuple(d[0])
+    return i, a[i], b[i], int(len(d))
+
+
+@pytest.mark.parametrize("model", [1, 3])
+def test_periodic_tgv_bitwise(gpu_lib, model):
+    c = Case((16, 12, 10), model=model, nu=0.02)
+    c.init_tgv(0.05)
+    for s in range(4):
+        c.step()
+        fo, fg = c.f_pair()
+        assert bits_equal(fo, fg), ("step", s, first_diff(fo, fg))
+
+
+BC_CASES = {
+    "inflow_ext2": dict(bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.0, 0.0),
+                        shearRateIn=(0.0, 0.002, 0.001)),
+    "neq_walls": dict(bnd=(102, 103, 201, 202, 302, 302), uvwIn=(0.04, 0.01, 0.0),
+                      shearRateIn=(0.0005, 0.001, 0.0)),
+    "halfway": dict(bnd=(101, 104, 203, 204, 301, 301), uvwIn=(0.05, 0.0, 0.0)),
+    "oscillatory": dict(bnd=(101, 104, 302, 302, 201, 201), uvwIn=(0.03, 0.0, 0.0),
+                        shearRateIn=(0.01, 0.05, 30.0), velocityKind=2),
+    "forced_channel": dict(bnd=(301, 301, 203, 203, 302, 302), volumeForceIn=(2e-5, 0.0, 1e-6),
+                           volumeForceAmp=1e-5, volumeForceFreq=0.1, volumeForcePhi=15.0),
+    "zfaces": dict(bnd=(301, 301, 302, 302, 102, 104), uvwIn=(0.0, 0.0, 0.03)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(BC_CASES))
+@pytest.mark.parametrize("model", [1, 3])
+def test_boundaries_bitwise(gpu_lib, name, model):
+    c = Case((14, 11, 9), model=model, nu=0.01, **BC_CASES[name])
+    c.init_equilibrium()
+    fo, fg = c.f_pair()
+    assert bits_equal(fo, fg), ("init", first_diff(fo, fg))
+    for s in range(4):
+        c.step()
+        fo, fg = c.f_pair()
+        assert bits_equal(fo, fg), ("step", s, first_diff(fo, fg))
+
+
+def test_macro_bitwise(gpu_lib):
+    c = Case((12, 10, 8), bnd=(101, 104, 201, 201, 302, 302), uvwIn=(0.05, 0.0, 0.0), nu=0.01)
+    c.init_equilibrium()
+    for _ in range(3):
+        c.step()
+    vf = np.array([1e-5, -2e-6, 0.0])
+    c.ob.b.volumeForce[:] = list(vf)
+    c.ob.macro()
+    den, uuu = c.gb.calculate_macro_quantities(vf)
+    assert bits_equal(c.ob.den.reshape(den.shape), den)
+    assert bits_equal(c.ob.u.reshape(uuu.shape), uuu)
+
+
+@pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("nplates", [1, 2])
+def test_ib_plate_bitwise(gpu_lib, model, nplates):
+    dims = (40, 24, 20)
+    plates = [plate_in(dims, n=5, heave=1.5, freq=0.02)]
+    if nplates == 2:
+        plates.append(plate_in(dims, n=4, heave=-1.0, freq=0.03, center=(26.4, 11.7, 9.6)))
+    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), model=model, uvwIn=(0.05, 0.0, 0.0), nu=0.02,
+             plates=plates, ntol=4, dtol=1e-12, Uref=0.05)
+    c.init_equilibrium()
+    for s in range(4):
+        r = c.step()
+        assert r["it_o"] == r["it_g"]
+        assert r["it_g"] > 0
+        assert np.isclose(r["res_o"], r["res_g"], rtol=1e-12, atol=0.0)
+        assert bits_equal(r["ef_o"], r["ef_g"]), ("eforce step", s)
+        fo, fg = c.f_pair()
+        assert bits_equal(fo, fg), ("step", s, first_diff(fo, fg))
+    # the stencil (int16 indices, real(4) weights) is the reference's
+    ei, ew = c.gb.ib_stencil()
+    bodies = c.last["bodies"]
+    assert np.array_equal(ei, np.concatenate([b.ei for b in bodies]).reshape(-1, 12))
+    assert np.array_equal(ew.view(np.uint32), np.concatenate([b.ew for b in bodies]).reshape(-1, 12).view(np.uint32))
+
+
+def test_ib_converges_to_dtol(gpu_lib):
+    dims = (36, 24, 20)
+    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.0, 0.0), nu=0.02,
+             plates=[plate_in(dims, n=5)], ntol=200, dtol=1e-3, Uref=0.05)
+    c.init_equilibrium()
+    r = c.step()
+    assert r["it_o"] == r["it_g"] and 1 < r["it_g"] < 200
+    assert r["res_g"] <= 1e-3
+
+
+def test_graph_run_matches_steps(gpu_lib):
+    a = F.Block(16, 12, 10, bndConds=(101, 104, 201, 202, 302, 302), nu=0.01, uvwIn=(0.05, 0, 0))
+    b = F.Block(16, 12, 10, bndConds=(101, 104, 201, 202, 302, 302), nu=0.01, uvwIn=(0.05, 0, 0))
+    for blk in (a, b):
+        blk.initialise(0.0)
+        blk.set_boundary_conditions(0.0)
+    for s in range(7):
+        a.step(blktime=(s + 1) * 1.0)
+    b.run(7, blktime0=1.0)
+    assert bits_equal(a.download_f(), b.download_f())
+
+
+# ---------------------------------------------------------------- fast forms
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def test_f64_fast_within_1e12(gpu_lib):
+    c = Case((24, 20, 16), model=1, nu=0.02, precision=F.PREC_F64_FAST)
+    c.init_tgv(0.05)
+    for s in range(10):
+        c.step()
+    fo, fg = c.f_pair()
+    # FP64 with regrouped sums and FMA: relative error per step well below 1e-12
+    assert _rel(fg, fo) < 1e-12
+
+
+@pytest.mark.parametrize("prec,tol", [(F.PREC_F32, 2e-5), (F.PREC_F16, 5e-3), (F.PREC_BF16, 5e-2)])
+def test_mixed_velocity_error(gpu_lib, prec, tol):
+    c = Case((24, 20, 16), model=1, nu=0.02, precision=prec)
+    c.init_tgv(0.05)
+    for s in range(20):
+        c.step()
+    c.ob.macro()
+    den, uuu = c.gb.calculate_macro_quantities()
+    uo = c.ob.u.reshape(uuu.shape)
+    # velocity error relative to the peak velocity, after 20 steps
+    assert _rel(uuu, uo) < tol
+
+
+@pytest.mark.parametrize("prec", [F.PREC_F64_FAST, F.PREC_F32, F.PREC_F16])
+def test_mixed_ib_force(gpu_lib, prec):
+    dims = (40, 24, 20)
+    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.0, 0.0), nu=0.02,
+             plates=[plate_in(dims, n=5, heave=1.0, freq=0.02)], ntol=4, dtol=1e-12, Uref=0.05,
+             precision=prec)
+    c.init_equilibrium()
+    for s in range(6):
+        r = c.step()
+    Fo = r["ef_o"].sum(axis=0)
+    Fg = r["ef_g"].sum(axis=0)
+    tol = {F.PREC_F64_FAST: 1e-10, F.PREC_F32: 1e-4, F.PREC_F16: 1e-2}[prec]
+    assert np.max(np.abs(Fg - Fo)) <= tol * np.max(np.abs(Fo))
+
+
+# --------------------------------------------------------------- error paths
+
+def test_errors_are_status_codes(gpu_lib):
+    with pytest.raises(F.FsiError) as e:
+        F.Block(8, 8, 8, bndConds=(999, 301, 301, 301, 301, 301))
+    assert e.value.code == -5
+    with pytest.raises(F.FsiError) as e:
+        F.Block(8, 8, 8, bndConds=(301, 101, 301, 301, 301, 301))
+    assert e.value.code == -5
+    b = F.Block(16, 16, 16, bndConds=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0, 0))
+    b.initialise(0.0)
+    b.ib_set_bodies([4])
+    xyz = np.array([[8.2, 8.1, 8.3], [8.7, 8.1, 8.3], [9.2, 8.1, 8.3], [9.7, 8.1, 8.3]])
+    vel = np.zeros((4, 3))
+    area = -2.0 * np.ones(4)
+    ef, it, res = b.ib_solve(xyz, vel, area, ntol=2, dtol=0.0, Uref=0.05)
+    assert it == 2 and np.all(np.isfinite(ef))
+    bad = vel.copy()
+    bad[1, 0] = np.nan
+    with pytest.raises(F.FsiError) as e:
+        b.ib_solve(xyz, bad, area, ntol=2, dtol=0.0, Uref=0.05)
+    assert e.value.code == -3
+    far = xyz.copy()
+    far[0, 0] = 0.2  # stencil reaches x index -1 with an inflow face: out of bounds
+    with pytest.raises(F.FsiError) as e:
+        b.ib_solve(far, vel, area, ntol=2, dtol=0.0, Uref=0.05)
+    assert e.value.code == -6
+    # the context is still usable after the reported errors
+    b.step(blktime=1.0)
+    assert np.all(np.isfinite(b.download_f()))

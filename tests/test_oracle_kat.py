@@ -1,0 +1,158 @@
+"""Known-answer tests of the CPU oracle (runs without a GPU).
+
+The reference has no tests or fixtures, so the oracle is held to physics
+with analytic answers: conservation, equilibrium invariance, viscous decay,
+Guo forcing, Poiseuille flow, the delta-kernel moments, the MRT/SRT
+reduction, and block refinement of a uniform flow.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+Q = 19
+
+
+def total_momentum(b):
+    f = b.fview()
+    ex = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0], dtype=float)
+    ey = np.array([0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1], dtype=float)
+    ez = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1], dtype=float)
+    s = f.reshape(Q, -1).sum(axis=1)
+    return np.array([s @ ex, s @ ey, s @ ez])
+
+
+def test_uniform_flow_stays_uniform():
+    fl = O.make_flow(uvwIn=(0.05, 0.01, -0.02), nu=0.01)
+    b = O.Block(10, 8, 6, 1.0, (0, 0, 0), [101] * 6, 1, fl)
+    b.initialise(0.0)
+    b.set_bc()
+    f0 = b.fview().copy()
+    for _ in range(5):
+        b.step()
+    assert np.max(np.abs(b.fview() - f0)) < 1e-15
+
+
+@pytest.mark.parametrize("model", [1, 3])
+def test_tgv_mass_conservation(model):
+    fl = O.make_flow(nu=0.02)
+    b = O.Block(16, 16, 16, 1.0, (0, 0, 0), [301] * 6, model, fl)
+    b.init_tgv(0.05)
+    m0 = b.f.sum()
+    for _ in range(20):
+        b.step()
+    assert abs(b.f.sum() - m0) / m0 < 1e-13
+
+
+def test_shear_wave_viscous_decay():
+    # u_x = u0 sin(2 pi y / Y): an exact solution decaying as exp(-nu k^2 t)
+    N = 32
+    nu_phys = 0.05
+    fl = O.make_flow(nu=nu_phys)
+    b = O.Block(4, N, 4, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    u0 = 1e-3
+    f = b.fview()
+    for y in range(N):
+        fe = O.feq(1.0, (u0 * np.sin(2 * np.pi * y / N), 0.0, 0.0))
+        f[:, :, y, :] = fe[:, None, None]
+    nsteps = 400
+    for _ in range(nsteps):
+        b.step()
+    b.macro()
+    ux = b.u.reshape(3, 4, N, 4)[0, 0, :, 0]
+    amp = np.sum(ux * np.sin(2 * np.pi * np.arange(N) / N)) * 2 / N
+    nu = (b.b.tau - 0.5) / 3.0
+    expect = u0 * np.exp(-nu * (2 * np.pi / N) ** 2 * nsteps)
+    assert abs(amp / expect - 1.0) < 1e-2  # O((k dx)^2) lattice error at N=32
+
+
+def test_guo_forcing_momentum_growth():
+    F_ = (2e-5, -1e-5, 3e-6)
+    fl = O.make_flow(nu=0.03, volumeForceIn=F_)
+    b = O.Block(6, 5, 4, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    b.initialise(0.0)
+    p0 = total_momentum(b)
+    n = 25
+    for _ in range(n):
+        b.step()
+    dp = total_momentum(b) - p0
+    assert np.allclose(dp, np.array(F_) * n * b.n, rtol=1e-9, atol=1e-15)
+
+
+def test_poiseuille_profile():
+    # half-way bounce-back walls (203) at y = -1/2 and y = Y - 1/2
+    Y = 10
+    Fx = 1e-6
+    fl = O.make_flow(nu=0.1, volumeForceIn=(Fx, 0, 0))
+    b = O.Block(4, Y, 4, 1.0, (0, 0, 0), [301, 301, 203, 203, 301, 301], 1, fl)
+    b.initialise(0.0)
+    b.set_bc()
+    for _ in range(3000):
+        b.step()
+    b.macro()
+    ux = b.u.reshape(3, 4, Y, 4)[0, 1, :, 1]
+    nu = (b.b.tau - 0.5) / 3.0
+    y = np.arange(Y)
+    exact = Fx / (2 * nu) * (y + 0.5) * (Y - 0.5 - y)
+    assert np.max(np.abs(ux - exact)) / np.max(exact) < 1e-2
+
+
+def test_delta_kernel_moments():
+    fl = O.make_flow(nu=0.01)
+    b = O.Block(20, 20, 20, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    rng = np.random.default_rng(5)
+    xyz = 5.0 + 10.0 * rng.random((50, 3))
+    body = O.Body(xyz, np.zeros_like(xyz), np.ones(50))
+    assert O.lib().or_ib_stencil(body.s, b.b) == 0
+    w = body.ew.reshape(50, 12).astype(np.float64)
+    ei = body.ei.reshape(50, 12)
+    for a in range(3):
+        ws = w[:, 4 * a:4 * a + 4]
+        assert np.allclose(ws.sum(axis=1), 1.0, atol=1e-6)  # partition of unity (real(4) weights)
+        pos = (ei[:, 4 * a:4 * a + 4] - 1).astype(float)
+        first = np.sum(ws * (pos - xyz[:, a:a + 1]), axis=1)
+        assert np.allclose(first, 0.0, atol=1e-6)  # zero first moment
+
+
+def test_mrt_with_srt_rates_equals_srt():
+    fl = O.make_flow(nu=0.02)
+    a = O.Block(8, 7, 6, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    b = O.Block(8, 7, 6, 1.0, (0, 0, 0), [301] * 6, 3, fl)
+    om = a.b.omega
+    b.b.mc[:] = list((om * np.eye(Q)).ravel(order="F"))
+    b.b.mf[:] = list(((1.0 - 0.5 * om) * np.eye(Q)).ravel(order="F"))
+    a.init_tgv(0.05)
+    b.init_tgv(0.05)
+    for _ in range(3):
+        a.step()
+        b.step()
+    assert np.array_equal(a.f, b.f)
+
+
+def test_mrt_matrix_conserves_mass_and_momentum():
+    mc, mf = O.mrt_matrices(1.0 / 0.6)
+    E = np.array([[0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0],
+                  [0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1],
+                  [0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1]], dtype=float)
+    assert np.max(np.abs(mc.sum(axis=0))) < 1e-12
+    assert np.max(np.abs(E @ mc)) < 1e-12
+    assert np.allclose(mf, np.eye(Q) - 0.5 * mc)
+
+
+def test_ib_stationary_plate_symmetric_force():
+    # a plate in the x-z plane centred in a symmetric channel: lift and side force vanish
+    from fsilbm3d_gb300.bodies import RigidPlate
+    fl = O.make_flow(uvwIn=(0.05, 0, 0), nu=0.02)
+    X, Y, Z = 40, 24, 24
+    b = O.Block(X, Y, Z, 1.0, (0, 0, 0), [101, 104, 101, 101, 101, 101], 1, fl)
+    b.initialise(0.0)
+    b.set_bc()
+    plate = RigidPlate(n_chord=6, n_span=6, chord=6.0, span=6.0, le=(12.0, 11.5, 11.5))
+    xyz, vel, area = plate.markers(0.0)
+    for _ in range(10):
+        body = O.Body(xyz, vel, area)
+        b.step([body], Uref=0.05, ntol=5, dtol=1e-6)
+    F_ = body.eforce.reshape(-1, 3).sum(axis=0)
+    assert F_[0] > 0  # v_Eforce is the force on the body: drag along the flow
+    assert abs(F_[1]) < 1e-10 * abs(F_[0]) + 1e-14
+    assert abs(F_[2]) < 1e-10 * abs(F_[0]) + 1e-14
