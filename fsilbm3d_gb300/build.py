@@ -22,7 +22,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
 UNITS = {
     "k_f64_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "k_fast.cu": [],
-    "fsi_abi.cu": [],
+    # host arithmetic (tau, MRT matrices) without contraction, as the reference
+    "fsi_abi.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "bc_impl.cuh"]
 

@@ -17,9 +17,13 @@ class Case:
                               volumeForceIn=volumeForceIn, volumeForceAmp=volumeForceAmp,
                               volumeForceFreq=volumeForceFreq, volumeForcePhi=volumeForcePhi, nu=nu)
         self.ob = O.Block(X, Y, Z, dh, origin, bnd, model, self.fl)
+        # the host builds M_COLLID/M_FORCE (FluidDomain.f90:466-522) and hands
+        # them to the device, as the Fortran host does through the ABI
+        mc = np.array(self.ob.b.mc[:]).reshape(19, 19, order="F") if model == 3 else None
+        mf = np.array(self.ob.b.mf[:]).reshape(19, 19, order="F") if model == 3 else None
         self.gb = F.Block(X, Y, Z, dh=dh, origin=origin, bndConds=bnd, iCollidModel=model, nu=nu,
                           precision=precision, denIn=denIn, uvwIn=uvwIn, shearRateIn=shearRateIn,
-                          velocityKind=velocityKind)
+                          velocityKind=velocityKind, m_collid=mc, m_force=mf)
         self.dh = dh
         self.denIn = denIn
         self.time = 0.0

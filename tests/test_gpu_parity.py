@@ -106,11 +106,11 @@ def test_ib_plate_bitwise(gpu_lib, model, nplates):
 def test_ib_converges_to_dtol(gpu_lib):
     dims = (36, 24, 20)
     c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.0, 0.0), nu=0.02,
-             plates=[plate_in(dims, n=5)], ntol=200, dtol=1e-3, Uref=0.05)
+             plates=[plate_in(dims, n=5)], ntol=200, dtol=0.2, Uref=0.05)
     c.init_equilibrium()
     r = c.step()
     assert r["it_o"] == r["it_g"] and 1 < r["it_g"] < 200
-    assert r["res_g"] <= 1e-3
+    assert r["res_g"] <= 0.2
 
 
 def test_graph_run_matches_steps(gpu_lib):
