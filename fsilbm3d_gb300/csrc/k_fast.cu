@@ -67,6 +67,11 @@ __device__ __forceinline__ long long cidx(int z, int y, int x, int Z, int Y) {
     return (long long)z + (long long)Z * ((long long)y + (long long)Y * (long long)x);
 }
 
+// 1/rho: IEEE in FP64; the hardware approximation (about 1 ulp) in FP32,
+// where the stored form's rounding dominates
+__device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
+
 // +v, -v or the additive identity -0 for lattice component e
 template <typename C> __device__ __forceinline__ C sel(int e, C v) { return e > 0 ? v : (e < 0 ? -v : C(-0.0)); }
 
@@ -94,7 +99,7 @@ __device__ __forceinline__ void macro_fast(const typename ST<P>::C g[Q], const t
     }
     if (ST<P>::OFF) { drho = s; rho = C(1) + s; }
     else { rho = s; drho = s - C(1); }
-    const C inv = C(1) / rho;
+    const C inv = rcp(rho);
     const C h = C(0.5) * dh;
     u0 = (jx + h * vf[0]) * inv;
     u1 = (jy + h * vf[1]) * inv;
@@ -181,29 +186,77 @@ __device__ __forceinline__ void collide_mrt(typename ST<P>::C g[Q], typename ST<
     }
 }
 
-template <int P, int MODEL>
-__global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST<P>::C> mm) {
+// SRT/BGK without forcing, Omega folded into per-weight-class constants:
+// per pair (i, opp) the post-collision values are
+//   g_i' = (1-Om) g_i + S + A,  g_o' = (1-Om) g_o + S - A,
+//   S = a_c + b_c (e.u)^2,  A = c_c (e.u),
+// with a_c = Om w (rho (1 - 1.5 u^2)) [stored f] or Om w (drho - 1.5 rho u^2)
+// [stored offsets], b_c = 4.5 Om w rho, c_c = 3 Om w rho.
+template <int P>
+__device__ __forceinline__ void collide_srt_free(typename ST<P>::C g[Q], typename ST<P>::C rho,
+                                                 typename ST<P>::C drho, typename ST<P>::C u0,
+                                                 typename ST<P>::C u1, typename ST<P>::C u2, typename ST<P>::C om) {
+    using C = typename ST<P>::C;
+    constexpr bool OFF = ST<P>::OFF;
+    const C k15 = C(1.5) * (u0 * u0 + u1 * u1 + u2 * u2);
+    const C omc = C(1) - om;
+    const C base = OFF ? (drho - rho * k15) : rho * (C(1) - k15);
+    const C orho = om * rho;
+    // weight classes: 0 -> 1/3, 1 -> 1/18, 2 -> 1/36
+    const C ac0 = (om * C(wt_(0))) * base;
+    const C ac1 = (om * C(wt_(1))) * base, bc1 = C(4.5 * wt_(1)) * orho, cc1 = C(3.0 * wt_(1)) * orho;
+    const C ac2 = (om * C(wt_(7))) * base, bc2 = C(4.5 * wt_(7)) * orho, cc2 = C(3.0 * wt_(7)) * orho;
+    g[0] = omc * g[0] + ac0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int i = pr_(k), o = opp_(i);
+        const bool cls1 = (i <= 6);
+        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C Sm = (cls1 ? bc1 : bc2) * (eu * eu) + (cls1 ? ac1 : ac2);
+        const C Am = (cls1 ? cc1 : cc2) * eu;
+        const C gi = g[i], go = g[o];
+        g[i] = omc * gi + (Sm + Am);
+        g[o] = omc * go + (Sm - Am);
+    }
+}
+
+// per-population element offsets, uniform across the grid: ld[i] = i*N
+// (population stride) and st[i] = i*N + e_i.(1, Z, Z*Y) (the streaming
+// displacement of an interior cell); the periodic wrap at the block faces is
+// a per-thread correction added to the pointer
+template <typename IT> struct Offs { IT ld[Q]; IT st[Q]; };
+
+template <typename IT>
+__device__ __forceinline__ IT wrap_corr(int e, IT cp, IT cm) { return e > 0 ? cp : (e < 0 ? cm : IT(0)); }
+
+// per-launch scalars in the arithmetic type, converted on the host: GB300
+// issues FP64 at a small fraction of the FP32 rate, so the FP32 kernels must
+// not convert double parameters per thread
+template <typename C> struct Scal { C om, dh, dh3, vf[3]; int forced; };
+
+template <int P, int MODEL, bool HOOKS, typename IT>
+__global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST<P>::C> mm, Offs<IT> of,
+                                                   Scal<typename ST<P>::C> sc) {
     using T = ST<P>;
     using S = typename T::S;
     using C = typename T::C;
-    int z = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
-    int x = blockIdx.z;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = blockIdx.z;
     if (z >= a.Z || y >= a.Y) return;
     const int X = a.X, Y = a.Y, Z = a.Z;
     const long long N = a.N;
-    const long long c = cidx(z, y, x, Z, Y);
-    const S *__restrict__ src = (const S *)a.src;
-    S *__restrict__ dst = (S *)a.dst;
+    const IT c = (IT)z + (IT)Z * ((IT)y + (IT)Y * (IT)x);
+    const S *__restrict__ sp = (const S *)a.src + c;
 
     C g[Q];
 #pragma unroll
-    for (int i = 0; i < Q; i++) g[i] = T::dec(src[c + N * i]);
+    for (int i = 0; i < Q; i++) g[i] = T::dec(__ldcs(sp + of.ld[i]));
 
-    C rho, drho, u0, u1, u2, F0, F1, F2;
-    bool forced;
+    C rho, drho, u0, u1, u2, F0 = C(0), F1 = C(0), F2 = C(0);
+    bool forced = false;
     const Win &w = a.win;
-    if (x >= w.x0 && x <= w.x1 && y >= w.y0 && y <= w.y1 && z >= w.z0 && z <= w.z1) {
+    if (HOOKS && x >= w.x0 && x <= w.x1 && y >= w.y0 && y <= w.y1 && z >= w.z0 && z <= w.z1) {
         long long wc = (long long)(z - w.z0) + (long long)w.WZ * ((long long)(y - w.y0) + (long long)w.WY * (x - w.x0));
         const double d = w.den[wc];
         if (T::OFF) { drho = (C)(d - 1.0); rho = C(1) + drho; }
@@ -212,48 +265,50 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
         F0 = (C)w.force[wc]; F1 = (C)w.force[wc + w.n]; F2 = (C)w.force[wc + 2 * w.n];
         forced = true;
     } else {
-        const C vf[3] = {(C)a.vf[0], (C)a.vf[1], (C)a.vf[2]};
-        macro_fast<P>(g, vf, (C)a.dh, rho, drho, u0, u1, u2);
-        F0 = vf[0]; F1 = vf[1]; F2 = vf[2];
-        forced = (a.vf[0] != 0.0) || (a.vf[1] != 0.0) || (a.vf[2] != 0.0);
+        macro_fast<P>(g, sc.vf, sc.dh, rho, drho, u0, u1, u2);
+        F0 = sc.vf[0]; F1 = sc.vf[1]; F2 = sc.vf[2];
+        forced = sc.forced != 0;
     }
-    if ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
-        (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2)) {
+    if (HOOKS && ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
+                  (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2))) {
         a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
         a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
     }
-    const C om = (C)a.omega, dh3 = C(3) * (C)a.dh;
+    const C om = sc.om, dh3 = sc.dh3;
     if (MODEL == 1) {
         if (forced) collide_srt<P, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, om, dh3);
-        else collide_srt<P, false>(g, rho, drho, u0, u1, u2, F0, F1, F2, om, dh3);
+        else collide_srt_free<P>(g, rho, drho, u0, u1, u2, om);
     } else {
         collide_mrt<P>(g, rho, drho, u0, u1, u2, F0, F1, F2, forced, dh3, mm);
     }
 
-    // halfwayBCset_ (FluidDomain.f90:567-614): post-collision faces as FP64 f
+    if (HOOKS) {
+        // halfwayBCset_ (FluidDomain.f90:567-614): post-collision faces as FP64 f
 #define FSI_HW(K, COND, OFS)                                                       \
-    if (a.hw[K] && (COND)) {                                                       \
-        double *h = a.hw[K] + (long long)Q * (OFS);                                \
-        _Pragma("unroll") for (int i = 0; i < Q; i++)                              \
-            h[i] = T::OFF ? (double)g[i] + wt_(i) : (double)g[i];                  \
-    }
-    FSI_HW(0, x == 0, z + (long long)Z * y)
-    FSI_HW(1, x == X - 1, z + (long long)Z * y)
-    FSI_HW(2, y == 0, z + (long long)Z * x)
-    FSI_HW(3, y == Y - 1, z + (long long)Z * x)
-    FSI_HW(4, z == 0, y + (long long)Y * x)
-    FSI_HW(5, z == Z - 1, y + (long long)Y * x)
+        if (a.hw[K] && (COND)) {                                                   \
+            double *h = a.hw[K] + (long long)Q * (OFS);                            \
+            _Pragma("unroll") for (int i = 0; i < Q; i++)                          \
+                h[i] = T::OFF ? (double)g[i] + wt_(i) : (double)g[i];              \
+        }
+        FSI_HW(0, x == 0, z + (long long)Z * y)
+        FSI_HW(1, x == X - 1, z + (long long)Z * y)
+        FSI_HW(2, y == 0, z + (long long)Z * x)
+        FSI_HW(3, y == Y - 1, z + (long long)Z * x)
+        FSI_HW(4, z == 0, y + (long long)Y * x)
+        FSI_HW(5, z == Z - 1, y + (long long)Y * x)
 #undef FSI_HW
+    }
 
-    const int zp = (z + 1 == Z) ? 0 : z + 1, zm = (z == 0) ? Z - 1 : z - 1;
-    const int yp = (y + 1 == Y) ? 0 : y + 1, ym = (y == 0) ? Y - 1 : y - 1;
-    const int xp = (x + 1 == X) ? 0 : x + 1, xm = (x == 0) ? X - 1 : x - 1;
+    // push: destination = c + st[i] + wrap correction (periodic in all axes)
+    const IT ZY = (IT)Z * (IT)Y, NN = (IT)N;
+    const IT czp = (z == Z - 1) ? -(IT)Z : 0, czm = (z == 0) ? (IT)Z : 0;
+    const IT cyp = (y == Y - 1) ? -ZY : 0, cym = (y == 0) ? ZY : 0;
+    const IT cxp = (x == X - 1) ? -NN : 0, cxm = (x == 0) ? NN : 0;
+    S *__restrict__ dp = (S *)a.dst + c;
 #pragma unroll
     for (int i = 0; i < Q; i++) {
-        const int zd = ez_(i) > 0 ? zp : (ez_(i) < 0 ? zm : z);
-        const int yd = ey_(i) > 0 ? yp : (ey_(i) < 0 ? ym : y);
-        const int xd = ex_(i) > 0 ? xp : (ex_(i) < 0 ? xm : x);
-        dst[cidx(zd, yd, xd, Z, Y) + N * i] = T::enc(g[i]);
+        const IT corr = wrap_corr(ez_(i), czp, czm) + wrap_corr(ey_(i), cyp, cym) + wrap_corr(ex_(i), cxp, cxm);
+        __stcs((dp + corr) + of.st[i], T::enc(g[i]));
     }
 }
 
@@ -318,18 +373,43 @@ __global__ void k_from_store(const void *__restrict__ fs, double *f, long long N
     f[i] = T::OFF ? v + wt_(q) : v;
 }
 
+template <int P, int MODEL, bool HOOKS, typename IT>
+cudaError_t step_launch(const StepArgs &a, const MatsT<typename ST<P>::C> &m, cudaStream_t st) {
+    Offs<IT> of{};
+    const long long ZY = (long long)a.Z * a.Y;
+    for (int i = 0; i < Q; i++) {
+        of.ld[i] = (IT)((long long)i * a.N);
+        of.st[i] = (IT)((long long)i * a.N + ez_(i) + (long long)a.Z * ey_(i) + ZY * ex_(i));
+    }
+    int bz = a.Z >= 128 ? 128 : ((a.Z + 31) / 32) * 32;
+    int by = TPB / bz;
+    if (by < 1) by = 1;
+    dim3 blk(bz, by), grd((a.Z + bz - 1) / bz, (a.Y + by - 1) / by, a.X);
+    using C = typename ST<P>::C;
+    Scal<C> sc{};
+    sc.om = (C)a.omega;
+    sc.dh = (C)a.dh;
+    sc.dh3 = (C)3 * (C)a.dh;
+    for (int k = 0; k < 3; k++) sc.vf[k] = (C)a.vf[k];
+    sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
+    k_step_fast<P, MODEL, HOOKS, IT><<<grd, blk, 0, st>>>(a, m, of, sc);
+    return cudaGetLastError();
+}
+
 template <int P, int MODEL>
 cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     using C = typename ST<P>::C;
     MatsT<C> m{};
     if (MODEL == 3)
         for (int i = 0; i < 361; i++) { m.mc[i] = (C)mm->mc[i]; m.mf[i] = (C)mm->mf[i]; }
-    int bz = a.Z >= 128 ? 128 : ((a.Z + 31) / 32) * 32;
-    int by = TPB / bz;
-    if (by < 1) by = 1;
-    dim3 blk(bz, by), grd((a.Z + bz - 1) / bz, (a.Y + by - 1) / by, a.X);
-    k_step_fast<P, MODEL><<<grd, blk, 0, st>>>(a, m);
-    return cudaGetLastError();
+    // the hook-free variant serves blocks without IB window, half-way faces
+    // and non-equilibrium extrapolation faces
+    bool hooks = a.win.x1 >= a.win.x0;
+    for (int k = 0; k < 6; k++) hooks = hooks || a.hw[k] != nullptr || a.l2[k] != 0;
+    // 32-bit element indices while all 19 populations fit
+    const bool small = (long long)Q * a.N < (1LL << 31) - 1;
+    if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
+    return hooks ? step_launch<P, MODEL, true, long long>(a, m, st) : step_launch<P, MODEL, false, long long>(a, m, st);
 }
 
 template <int P>
