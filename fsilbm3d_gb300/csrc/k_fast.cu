@@ -16,6 +16,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "bc_impl.cuh"
 #include "fsi_kernels.h"
 #include "../../include/fsi_gpu.h"
@@ -312,6 +314,198 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
     }
 }
 
+// ---------------------------------------------------------------------------
+// Paired-cell form of the step for the offset storage forms (FP32, FP16,
+// BF16) on blocks without IB window, half-way faces or 102 faces: each thread
+// owns the two z-adjacent cells (z0, z0+1), z0 even. Loads and stores move
+// both cells in one 32-bit (FP16/BF16) or 64-bit (FP32) access and all
+// arithmetic runs on packed FP32x2 (fma.rn.f32x2, sm_100 and later), so one
+// instruction serves both cells. A CTA holds whole z-rows; the +-z streaming
+// shift goes through shared memory, the +-y/+-x shift moves whole rows.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return __fmul2_rn(a, f2(-1.0f)); }
+__device__ __forceinline__ float2 sel2(int e, float2 v) { return e > 0 ? v : neg2(v); }
+
+template <int P> struct V2;
+template <> struct V2<FSI_PREC_F32> {
+    using S2 = float2; using S = float;
+    static __device__ __forceinline__ float2 dec(S2 s) { return s; }
+    static __device__ __forceinline__ S2 enc(float2 c) { return c; }
+    static __device__ __forceinline__ S lo(S2 s) { return s.x; }
+    static __device__ __forceinline__ S hi(S2 s) { return s.y; }
+    static __device__ __forceinline__ S2 pack(S a, S b) { return make_float2(a, b); }
+};
+template <> struct V2<FSI_PREC_F16> {
+    using S2 = __half2; using S = __half;
+    static __device__ __forceinline__ float2 dec(S2 s) { return __half22float2(s); }
+    static __device__ __forceinline__ S2 enc(float2 c) { return __float22half2_rn(c); }
+    static __device__ __forceinline__ S lo(S2 s) { return __low2half(s); }
+    static __device__ __forceinline__ S hi(S2 s) { return __high2half(s); }
+    static __device__ __forceinline__ S2 pack(S a, S b) { return __halves2half2(a, b); }
+};
+template <> struct V2<FSI_PREC_BF16> {
+    using S2 = __nv_bfloat162; using S = __nv_bfloat16;
+    static __device__ __forceinline__ float2 dec(S2 s) { return __bfloat1622float2(s); }
+    static __device__ __forceinline__ S2 enc(float2 c) { return __float22bfloat162_rn(c); }
+    static __device__ __forceinline__ S lo(S2 s) { return __low2bfloat16(s); }
+    static __device__ __forceinline__ S hi(S2 s) { return __high2bfloat16(s); }
+    static __device__ __forceinline__ S2 pack(S a, S b) { return __halves2bfloat162(a, b); }
+};
+
+// index of z-moving population i among the ten with ez != 0
+__host__ __device__ constexpr int zslot_(int i) {
+    return i == 5 ? 0 : i == 6 ? 1 : i == 11 ? 2 : i == 12 ? 3 : i == 13 ? 4 : i == 14 ? 5
+         : i == 15 ? 6 : i == 16 ? 7 : i == 17 ? 8 : i == 18 ? 9 : -1;
+}
+
+template <int P, bool FORCED>
+__global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc) {
+    using V = V2<P>;
+    using S2 = typename V::S2;
+    using S = typename V::S;
+    extern __shared__ unsigned char smraw[];
+    const int Z = a.Z, Y = a.Y, X = a.X;
+    const int tz = threadIdx.x, ty = threadIdx.y, R = blockDim.y;
+    const int z0 = 2 * tz;
+    const int y = blockIdx.y * R + ty, x = blockIdx.z;
+    const bool active = (y < Y);
+    S *sm = (S *)smraw;  // [10][R][Z]
+    const int c = z0 + Z * ((active ? y : 0) + Y * x);
+    const int N = (int)a.N;
+
+    float2 g[Q];
+    if (active) {
+        const S *sp = (const S *)a.src + c;
+#pragma unroll
+        for (int i = 0; i < Q; i++) g[i] = V::dec(__ldcs((const S2 *)(sp + of.ld[i])));
+    } else {
+#pragma unroll
+        for (int i = 0; i < Q; i++) g[i] = f2(0.0f);
+    }
+
+    // macro (offsets: rho = 1 + sum g)
+    float2 s = g[0], jx = f2(0.f), jy = f2(0.f), jz = f2(0.f);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int i = pr_(k), o = opp_(i);
+        const float2 sk = add2(g[i], g[o]), dk = sub2(g[i], g[o]);
+        s = add2(s, sk);
+        if (ex_(i)) jx = ex_(i) > 0 ? add2(jx, dk) : sub2(jx, dk);
+        if (ey_(i)) jy = ey_(i) > 0 ? add2(jy, dk) : sub2(jy, dk);
+        if (ez_(i)) jz = ez_(i) > 0 ? add2(jz, dk) : sub2(jz, dk);
+    }
+    const float2 drho = s, rho = add2(f2(1.0f), s);
+    const float2 inv = make_float2(__fdividef(1.0f, rho.x), __fdividef(1.0f, rho.y));
+    const float h = 0.5f * sc.dh;
+    float2 u0, u1, u2;
+    if (FORCED) {
+        u0 = mul2(add2(jx, f2(h * sc.vf[0])), inv);
+        u1 = mul2(add2(jy, f2(h * sc.vf[1])), inv);
+        u2 = mul2(add2(jz, f2(h * sc.vf[2])), inv);
+    } else {
+        u0 = mul2(jx, inv); u1 = mul2(jy, inv); u2 = mul2(jz, inv);
+    }
+
+    // SRT (FluidDomain.f90:1218-1227), Omega folded as in collide_srt_free
+    const float om = sc.om;
+    const float2 k15 = mul2(f2(1.5f), fma2(u0, u0, fma2(u1, u1, mul2(u2, u2))));
+    const float2 omc = f2(1.0f - om);
+    const float2 base = sub2(drho, mul2(rho, k15));
+    const float2 orho = mul2(f2(om), rho);
+    const float w0 = (float)wt_(0), w1 = (float)wt_(1), w2 = (float)wt_(7);
+    const float2 ac0 = mul2(f2(om * w0), base);
+    const float2 ac1 = mul2(f2(om * w1), base), bc1 = mul2(f2(4.5f * w1), orho), cc1 = mul2(f2(3.0f * w1), orho);
+    const float2 ac2 = mul2(f2(om * w2), base), bc2 = mul2(f2(4.5f * w2), orho), cc2 = mul2(f2(3.0f * w2), orho);
+    float2 uF = f2(0.f), cf = f2(0.f);
+    if (FORCED) {
+        uF = fma2(u0, f2(sc.vf[0]), fma2(u1, f2(sc.vf[1]), mul2(u2, f2(sc.vf[2]))));
+        cf = f2((1.0f - 0.5f * om) * sc.dh3);
+    }
+    g[0] = fma2(omc, g[0], ac0);
+    if (FORCED) g[0] = sub2(g[0], mul2(mul2(cf, f2(w0)), uF));
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int i = pr_(k), o = opp_(i);
+        const bool cls1 = (i <= 6);
+        float2 eu = f2(0.f);
+        bool first = true;
+        if (ex_(i)) { eu = first ? sel2(ex_(i), u0) : (ex_(i) > 0 ? add2(eu, u0) : sub2(eu, u0)); first = false; }
+        if (ey_(i)) { eu = first ? sel2(ey_(i), u1) : (ey_(i) > 0 ? add2(eu, u1) : sub2(eu, u1)); first = false; }
+        if (ez_(i)) { eu = first ? sel2(ez_(i), u2) : (ez_(i) > 0 ? add2(eu, u2) : sub2(eu, u2)); first = false; }
+        const float2 Sm = fma2(cls1 ? bc1 : bc2, mul2(eu, eu), cls1 ? ac1 : ac2);
+        const float2 Am = mul2(cls1 ? cc1 : cc2, eu);
+        float2 ni = fma2(omc, g[i], add2(Sm, Am));
+        float2 no = fma2(omc, g[o], sub2(Sm, Am));
+        if (FORCED) {
+            const float eF0 = ex_(i) * sc.vf[0] + ey_(i) * sc.vf[1] + ez_(i) * sc.vf[2];
+            const float2 cw = mul2(cf, f2(cls1 ? w1 : w2));
+            const float2 Fs = mul2(cw, sub2(mul2(f2(3.0f * eF0), eu), uF)), Fa = mul2(cw, f2(eF0));
+            ni = add2(ni, add2(Fs, Fa));
+            no = add2(no, sub2(Fs, Fa));
+        }
+        g[i] = ni;
+        g[o] = no;
+    }
+
+    // stage the ten z-moving populations of this row in shared memory
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < Q; i++)
+            if (ez_(i) != 0) *(S2 *)(sm + (zslot_(i) * R + ty) * Z + z0) = V::enc(g[i]);
+    }
+    __syncthreads();
+    if (!active) return;
+
+    // push; the destination row is (y+ey, x+ex) with periodic wrap
+    const int ZY = Z * Y;
+    const int cyp = (y == Y - 1) ? -ZY : 0, cym = (y == 0) ? ZY : 0;
+    const int cxp = (x == X - 1) ? -N : 0, cxm = (x == 0) ? N : 0;
+    S *dp = (S *)a.dst + c;
+    const int zl = (z0 == 0) ? Z - 1 : z0 - 1, zr = (z0 + 2 == Z) ? 0 : z0 + 2;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const int corr = (ey_(i) > 0 ? cyp : (ey_(i) < 0 ? cym : 0)) + (ex_(i) > 0 ? cxp : (ex_(i) < 0 ? cxm : 0));
+        S2 v;
+        if (ez_(i) == 0) {
+            v = V::enc(g[i]);
+        } else {
+            const S *row = sm + (zslot_(i) * R + ty) * Z;
+            // ez = +1: cells z0, z0+1 receive z0-1, z0; ez = -1: they receive z0+1, z0+2
+            v = ez_(i) > 0 ? V::pack(row[zl], row[z0]) : V::pack(row[z0 + 1], row[zr]);
+        }
+        __stcs((S2 *)(dp + corr + of.st[i]), v);
+    }
+}
+
+template <int P>
+cudaError_t pair_launch(const StepArgs &a, cudaStream_t st) {
+    Offs<int> of{};
+    const long long ZY = (long long)a.Z * a.Y;
+    for (int i = 0; i < Q; i++) {
+        of.ld[i] = (int)((long long)i * a.N);
+        // no z term: the z shift happens in shared memory
+        of.st[i] = (int)((long long)i * a.N + (long long)a.Z * ey_(i) + ZY * ex_(i));
+    }
+    Scal<float> sc{};
+    sc.om = (float)a.omega;
+    sc.dh = (float)a.dh;
+    sc.dh3 = 3.0f * (float)a.dh;
+    for (int k = 0; k < 3; k++) sc.vf[k] = (float)a.vf[k];
+    sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
+    const int tpr = a.Z / 2;
+    const int R = std::max(1, 256 / tpr);
+    dim3 blk(tpr, R), grd(1, (a.Y + R - 1) / R, a.X);
+    size_t smem = (size_t)10 * R * a.Z * sizeof(typename V2<P>::S);
+    if (sc.forced) k_step_pair<P, true><<<grd, blk, smem, st>>>(a, of, sc);
+    else k_step_pair<P, false><<<grd, blk, smem, st>>>(a, of, sc);
+    return cudaGetLastError();
+}
+
 template <int P>
 __global__ void k_macro_fast(const void *__restrict__ fs, double *den, double *u, int Y, int Z, long long N, double dh,
                              double vf0, double vf1, double vf2) {
@@ -408,6 +602,8 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     for (int k = 0; k < 6; k++) hooks = hooks || a.hw[k] != nullptr || a.l2[k] != 0;
     // 32-bit element indices while all 19 populations fit
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
+    if (P != FSI_PREC_F64_FAST && MODEL == 1 && !hooks && small && a.Z % 2 == 0 && a.Z <= 512)
+        return pair_launch<P == FSI_PREC_F64_FAST ? FSI_PREC_F32 : P>(a, st);
     if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
     return hooks ? step_launch<P, MODEL, true, long long>(a, m, st) : step_launch<P, MODEL, false, long long>(a, m, st);
 }

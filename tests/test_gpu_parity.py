@@ -154,6 +154,20 @@ def test_mixed_velocity_error(gpu_lib, prec, tol):
     assert _rel(uuu, uo) < tol
 
 
+@pytest.mark.parametrize("dims", [(14, 9, 22), (14, 9, 21), (7, 5, 64)])
+@pytest.mark.parametrize("prec,tol", [(F.PREC_F32, 2e-5), (F.PREC_F16, 5e-3), (F.PREC_BF16, 5e-2)])
+def test_mixed_forced_periodic(gpu_lib, dims, prec, tol):
+    # even z extent: paired-cell kernel; odd: one cell per thread
+    c = Case(dims, model=1, nu=0.02, precision=prec, volumeForceIn=(3e-5, -1e-5, 2e-5))
+    c.init_tgv(0.04)
+    for s in range(12):
+        c.step()
+    c.ob.b.volumeForce[:] = list(c.vf(c.time))
+    c.ob.macro()
+    den, uuu = c.gb.calculate_macro_quantities(c.vf(c.time))
+    assert _rel(uuu, c.ob.u.reshape(uuu.shape)) < tol
+
+
 @pytest.mark.parametrize("prec", [F.PREC_F64_FAST, F.PREC_F32, F.PREC_F16])
 def test_mixed_ib_force(gpu_lib, prec):
     dims = (40, 24, 20)
