@@ -30,7 +30,7 @@ GRID = (256, 256, 256)
 TAU = 0.6
 U0 = 0.05
 IB_GRID = (160, 96, 96)
-PROFILE_FILE = os.path.join(ROOT, "profiles", "k_step_fast_f16_tgv256.md")
+PROFILE_FILE = os.path.join(ROOT, "profiles", "k_step_pair_f16_tgv256.md")
 METRIC = "D3Q19 MLUPS, TGV 256^3, 1 GB300 (FP16-offset storage, FP32 collide)"
 
 
@@ -346,7 +346,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk, "unit": "GB/s",
                      "frac": round(achieved / pk, 4), "peak_kind": pk_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": N * B,
-                     "kernel": "k_step_fast<FSI_PREC_F16,SRT>"},
+                     "kernel": "k_step_pair<FSI_PREC_F16,SRT>"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": a.steps,
