@@ -149,6 +149,8 @@ struct fsi_pair {
     double *buf[6][2] = {};
     double *buft[6][2] = {};
     double *scr_f = nullptr, *scr_t = nullptr;
+    long long scr_cells = 0;
+    int *d_err = nullptr;  // first out-of-range access of a face kernel: code, index lo, hi
 };
 
 namespace {
@@ -718,6 +720,9 @@ int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme)
         if (e == cudaSuccess) e = cudaMalloc((void **)&p->scr_f, sizeof(double) * 19 * maxS);
         if (e == cudaSuccess) e = cudaMalloc((void **)&p->scr_t, sizeof(double) * maxS);
     }
+    p->scr_cells = (long long)maxS;
+    if (e == cudaSuccess) e = cudaMalloc((void **)&p->d_err, sizeof(int) * 4);
+    if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int) * 4);
     if (e != cudaSuccess) {
         fsi_pair_destroy(p);
         return fail(FSI_E_CUDA, "pair allocation: %s", cudaGetErrorString(e));
@@ -735,9 +740,29 @@ int fsi_pair_destroy(fsi_pair_t p) {
         }
     if (p->scr_f) cudaFree(p->scr_f);
     if (p->scr_t) cudaFree(p->scr_t);
+    if (p->d_err) cudaFree(p->d_err);
     delete p;
     return FSI_OK;
 }
+
+}  // extern "C"
+
+namespace {
+// reads and clears the pair's error word after its stream has drained
+int pair_check(fsi_pair *p) {
+    int h[3] = {0, 0, 0};
+    CK(cudaMemcpy(h, p->d_err, sizeof(int) * 3, cudaMemcpyDeviceToHost));
+    if (h[0] == 0) return FSI_OK;
+    CK(cudaMemset(p->d_err, 0, sizeof(int) * 4));
+    long long idx = (long long)(unsigned)h[1] | ((long long)h[2] << 32);
+    static const char *what[] = {"", "interpolation source", "interpolation target", "son face cell",
+                                 "father face cell", "son cell", "father cell"};
+    return fail(FSI_E_RANGE, "block refinement: %s index %lld out of range", what[h[0] >= 1 && h[0] <= 6 ? h[0] : 0],
+                idx);
+}
+}  // namespace
+
+extern "C" {
 
 int fsi_pair_extract(fsi_pair_t p, int time_level) {
     if (!p || (time_level != 1 && time_level != 2)) return fail(FSI_E_ARG, "invalid argument");
@@ -745,7 +770,7 @@ int fsi_pair_extract(fsi_pair_t p, int time_level) {
     for (int k = 0; k < 6; k++) {
         if (p->so->d.bndConds[k] != BC_FLUID) continue;
         CK(launch_pair_extract((const double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, p->p, k, p->buf[k][time_level - 1],
-                               p->buft[k][time_level - 1], fa->st));
+                               p->buft[k][time_level - 1], p->d_err, fa->st));
         if (time_level == 2) {
             int ax = k >> 1;
             long long A = ax == 2 ? p->p.yDimF : p->p.zDimF, B = ax == 0 ? p->p.yDimF : p->p.xDimF;
@@ -754,7 +779,7 @@ int fsi_pair_extract(fsi_pair_t p, int time_level) {
         }
     }
     CK(cudaStreamSynchronize(fa->st));
-    return FSI_OK;
+    return pair_check(p);
 }
 
 int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]) {
@@ -765,10 +790,10 @@ int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]) {
         if (p->p.sds[k] == 0) continue;
         int lvl = (n_timeStep == 0) ? 0 : 1;
         CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
-                           p->scheme, p->scr_f, p->scr_t, vf, fa->d.dh, so->st));
+                           p->scheme, p->scr_f, p->scr_t, p->scr_cells, vf, fa->d.dh, p->d_err, so->st));
     }
     CK(cudaStreamSynchronize(so->st));
-    return FSI_OK;
+    return pair_check(p);
 }
 
 int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
@@ -779,10 +804,11 @@ int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
         int want = (k % 2 == 0) ? 1 : -1;
         if (p->p.sds[k] != want) continue;
         CK(launch_pair_s2f((double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, (const double *)so->fa, so->X, so->Y, so->Z,
-                           so->tau, p->p, k, vf, so->d.dh, fa->st));
+                           so->tau, p->p, k, vf, so->d.dh, p->d_err, fa->st));
     }
     CK(cudaStreamSynchronize(fa->st));
-    return FSI_OK;
+    return pair_check(p);
 }
 
 }  // extern "C"
+

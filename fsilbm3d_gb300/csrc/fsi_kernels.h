@@ -45,16 +45,16 @@ struct PairGeom {
     int xDimS, xDimF, yDimS, yDimF, zDimS, zDimF;
 };
 cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f,
-                                const PairGeom &p, int face, double *buf, double *buft,
+                                const PairGeom &p, int face, double *buf, double *buft, int *err,
                                 cudaStream_t st);
 cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaStream_t st);
 cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const PairGeom &p,
                             int face, const double *buf, const double *buft, int scheme,
-                            double *scratch_f, double *scratch_t, const double vf[3], double dh,
-                            cudaStream_t st);
+                            double *scratch_f, double *scratch_t, long long scratch_cells,
+                            const double vf[3], double dh, int *err, cudaStream_t st);
 cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *fs,
                             int SX, int SY, int SZ, double tau_s, const PairGeom &p, int face,
-                            const double vf[3], double dh, cudaStream_t st);
+                            const double vf[3], double dh, int *err, cudaStream_t st);
 
 // ---- fast kernels (k_fast.cu): FP64 regrouped, FP32/FP16/BF16 storage ----
 cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st);

@@ -465,11 +465,20 @@ __global__ void k_ib_spread(const float *__restrict__ ew, const int *__restrict_
 }
 
 // ------------------------------------------------------- block refinement
+// The face kernels check every global index against its buffer; the first
+// out-of-range access is recorded in err (code, index low, index high) and
+// skipped, and the host turns it into FSI_E_RANGE.
+__device__ __forceinline__ void rec_err(int *err, int code, long long idx) {
+    if (atomicCAS(err, 0, code) == 0) {
+        err[1] = (int)(idx & 0xffffffffLL);
+        err[2] = (int)(idx >> 32);
+    }
+}
 
 // extract_interpolate_layer for one son face (LBMBlockComm.f90:354-369):
 // buf(e, a, b) = father fIn on the face plane; buft = father tau
 __global__ void k_pair_extract(const double *__restrict__ ff, int FY, int FZ, long long NF, double tau_f,
-                               PairGeom p, int face, double *buf, double *buft, int A, int B) {
+                               PairGeom p, int face, double *buf, double *buft, int A, int B, int *err) {
     int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (a >= A || b >= B) return;
     int ax = face >> 1, xF, yF, zF;
@@ -478,6 +487,7 @@ __global__ void k_pair_extract(const double *__restrict__ ff, int FY, int FZ, lo
     else { zF = p.f[face]; xF = b + p.f[0]; yF = a + p.f[2]; }
     long long c = cidx(zF - 1, yF - 1, xF - 1, FZ, FY);
     long long o = (long long)a + (long long)A * b;
+    if (c < 0 || c >= NF) { rec_err(err, 4, c); return; }
     for (int e = 0; e < Q; e++) buf[e + Q * o] = ff[c + NF * e];
     buft[o] = tau_f;
 }
@@ -503,11 +513,26 @@ __device__ __forceinline__ void grid_transform(double fin[Q], double coeff, cons
 // interpolate_fIn / interpolate_tau (LBMBlockComm.f90:808-956), one thread
 // per population q (nq threads), the reference's loop sequence per thread.
 // fF(nq,bF,aF) -> fS(nq,bS,aS).
-__global__ void k_pair_interp(int nq, int bF, const double *__restrict__ fF, int bS, int aS, double *fS, int scheme) {
+struct Checked {
+    double *p;
+    long long n;
+    int *err;
+    int code;
+    __device__ double &at(long long i) {
+        if (i < 0 || i >= n) { rec_err(err, code, i); return dummy; }
+        return p[i];
+    }
+    double dummy;
+};
+
+__global__ void k_pair_interp(int nq, int bF, const double *__restrict__ fFp, long long nF, int bS, int aS,
+                              double *fSp, long long nS, int scheme, int *err) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
-#define FF(b_, a_) fF[q + (long long)nq * (((b_) - 1) + (long long)bF * ((a_) - 1))]
-#define FS(b_, a_) fS[q + (long long)nq * (((b_) - 1) + (long long)bS * ((a_) - 1))]
+    Checked cF{const_cast<double *>(fFp), nF, err, 1, 0.0};
+    Checked cS{fSp, nS, err, 2, 0.0};
+#define FF(b_, a_) cF.at(q + (long long)nq * (((b_) - 1) + (long long)bF * ((a_) - 1)))
+#define FS(b_, a_) cS.at(q + (long long)nq * (((b_) - 1) + (long long)bS * ((a_) - 1)))
     int r1 = 0, r2 = 0, bSt = bS, aSt = aS;
     if (bS % 2 == 0) { bSt = bS - 1; r2 = 1; }
     if (aS % 2 == 0) { aSt = aS - 1; r1 = 1; }
@@ -563,7 +588,7 @@ __global__ void k_pair_interp(int nq, int bF, const double *__restrict__ fF, int
 // interpolation_father_to_son apply step (LBMBlockComm.f90:685-693)
 __global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, double tau_s, PairGeom p, int face,
                                  const double *tf, const double *tt, int AS, int BS, double vf0, double vf1,
-                                 double vf2, double dh) {
+                                 double vf2, double dh, int *err) {
     int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (a >= AS || b >= BS) return;
     int ax = face >> 1, xS, yS, zS;
@@ -572,6 +597,7 @@ __global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, doubl
     else { zS = p.s[face]; xS = b + 1; yS = a + 1; }
     long long c = cidx(zS - 1, yS - 1, xS - 1, SZ, SY);
     long long o = (long long)a + (long long)AS * b;
+    if (c < 0 || c >= NS) { rec_err(err, 3, c); return; }
     double coeff = (tau_s / tt[o]) / 2.0;
     double fin[Q], vf[3] = {vf0, vf1, vf2};
     for (int e = 0; e < Q; e++) fin[e] = tf[Q * o + e];
@@ -582,7 +608,7 @@ __global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, doubl
 // deliver_son_to_father for one face (LBMBlockComm.f90:555-570 and siblings)
 __global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_f, const double *__restrict__ fs,
                            int SY, int SZ, long long NS, double tau_s, PairGeom p, int face, int n1, int n2,
-                           double vf0, double vf1, double vf2, double dh) {
+                           double vf0, double vf1, double vf2, double dh, int *err) {
     int i1 = blockIdx.x * blockDim.x + threadIdx.x, i2 = blockIdx.y;
     if (i1 >= n2 || i2 >= n1) return;
     int ax = face >> 1;
@@ -594,6 +620,8 @@ __global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_
     S[o2] = v2; F[o2] = (v2 - p.si[2 * o2]) / 2 + p.fi[2 * o2];
     long long cs = cidx(S[2] - 1, S[1] - 1, S[0] - 1, SZ, SY);
     long long cf = cidx(F[2] - 1, F[1] - 1, F[0] - 1, FZ, FY);
+    if (cs < 0 || cs >= NS) { rec_err(err, 5, cs); return; }
+    if (cf < 0 || cf >= NF) { rec_err(err, 6, cf); return; }
     double coeff = (tau_f / tau_s) * 2.0;
     double t[Q], vf[3] = {vf0, vf1, vf2};
     for (int e = 0; e < Q; e++) t[e] = fs[cs + NS * e];
@@ -721,13 +749,13 @@ cudaError_t launch_ib_spread(const float *ew, const int *start, const int *list,
 }
 
 cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f, const PairGeom &p, int face,
-                                double *buf, double *buft, cudaStream_t st) {
+                                double *buf, double *buft, int *err, cudaStream_t st) {
     int ax = face >> 1, A, B;
     if (ax == 0) { A = p.zDimF; B = p.yDimF; }
     else if (ax == 1) { A = p.zDimF; B = p.xDimF; }
     else { A = p.yDimF; B = p.xDimF; }
     k_pair_extract<<<dim3((A + 63) / 64, B), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, p, face, buf,
-                                                          buft, A, B);
+                                                          buft, A, B, err);
     return cudaGetLastError();
 }
 
@@ -738,21 +766,23 @@ cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaS
 
 cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const PairGeom &p, int face,
                             const double *buf, const double *buft, int scheme, double *scratch_f, double *scratch_t,
-                            const double vf[3], double dh, cudaStream_t st) {
+                            long long scratch_cells, const double vf[3], double dh, int *err, cudaStream_t st) {
     int ax = face >> 1, AF, BF, AS, BS;
     if (ax == 0) { AF = p.zDimF; BF = p.yDimF; AS = p.zDimS; BS = p.yDimS; }
     else if (ax == 1) { AF = p.zDimF; BF = p.xDimF; AS = p.zDimS; BS = p.xDimS; }
     else { AF = p.yDimF; BF = p.xDimF; AS = p.yDimS; BS = p.xDimS; }
-    (void)BF;
-    k_pair_interp<<<1, 32, 0, st>>>(Q, AF, buf, AS, BS, scratch_f, scheme);
-    k_pair_interp<<<1, 32, 0, st>>>(1, AF, buft, AS, BS, scratch_t, 1);
+    const long long nF = (long long)AF * BF;
+    if ((long long)AS * BS > scratch_cells) return cudaErrorInvalidValue;
+    k_pair_interp<<<1, 32, 0, st>>>(Q, AF, buf, Q * nF, AS, BS, scratch_f, Q * scratch_cells, scheme, err);
+    k_pair_interp<<<1, 32, 0, st>>>(1, AF, buft, nF, AS, BS, scratch_t, scratch_cells, 1, err);
     k_pair_f2s_apply<<<dim3((AS + 63) / 64, BS), 64, 0, st>>>(fs, SY, SZ, (long long)SX * SY * SZ, tau_s, p, face,
-                                                              scratch_f, scratch_t, AS, BS, vf[0], vf[1], vf[2], dh);
+                                                              scratch_f, scratch_t, AS, BS, vf[0], vf[1], vf[2], dh,
+                                                              err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *fs, int SX, int SY,
-                            int SZ, double tau_s, const PairGeom &p, int face, const double vf[3], double dh,
+                            int SZ, double tau_s, const PairGeom &p, int face, const double vf[3], double dh, int *err,
                             cudaStream_t st) {
     int ax = face >> 1;
     int o1 = (ax == 0) ? 1 : 0, o2 = (ax == 2) ? 1 : 2;
@@ -762,7 +792,7 @@ cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, co
     if (n1 <= 0 || n2 <= 0) return cudaSuccess;
     k_pair_s2f<<<dim3((n2 + 63) / 64, n1), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, fs, SY, SZ,
                                                          (long long)SX * SY * SZ, tau_s, p, face, n1, n2, vf[0], vf[1],
-                                                         vf[2], dh);
+                                                         vf[2], dh, err);
     return cudaGetLastError();
 }
 

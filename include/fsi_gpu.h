@@ -151,6 +151,7 @@ int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]);
 /* deliver_son_to_father (LBMBlockComm.f90:546-653); vf = son volume force */
 int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]);
 
+
 #ifdef __cplusplus
 }
 #endif

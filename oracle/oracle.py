@@ -101,6 +101,10 @@ def lib():
         L.or_field_stat.argtypes = [BP, C.c_double, DP, DP]
         L.or_build_pair.argtypes = [BP, BP, C.POINTER(OrPair)]
         L.or_grid_transform.argtypes = [DP, C.c_double, DP, C.c_double]
+        BUF = (DP * 2) * 6
+        L.or_extract_layer.argtypes = [BP, BP, C.POINTER(OrPair), C.c_int, BUF, BUF]
+        L.or_interp_f2s.argtypes = [BP, BP, C.POINTER(OrPair), C.c_int, BUF, BUF, C.c_int]
+        L.or_deliver_s2f.argtypes = [BP, BP, C.POINTER(OrPair)]
         _lib = L
     return _lib
 
@@ -210,6 +214,58 @@ class Body:
         s.ei = self.ei.ctypes.data_as(C.POINTER(C.c_int16))
         s.ew = self.ew.ctypes.data_as(C.POINTER(C.c_float))
         self.s = s
+
+
+class Pair:
+    """A father/son pair with its extracted face layers (CommPair and the
+    fIn_F*/tau_F* buffers, LBMBlockComm.f90:11-18, 213-264)."""
+
+    def __init__(self, father, son, scheme=1):
+        self.fa, self.so, self.scheme = father, son, scheme
+        self.p = OrPair()
+        lib().or_build_pair(C.byref(father.b), C.byref(son.b), C.byref(self.p))
+        p = self.p
+        self.keep = []
+        self.bf = ((DP * 2) * 6)()
+        self.bt = ((DP * 2) * 6)()
+        for k in range(6):
+            ax = k // 2
+            A, B = [(p.zDimF, p.yDimF), (p.zDimF, p.xDimF), (p.yDimF, p.xDimF)][ax]
+            for t in range(2):
+                f = np.zeros(19 * A * B)
+                tt = np.zeros(A * B)
+                self.keep += [f, tt]
+                self.bf[k][t] = _dp(f)
+                self.bt[k][t] = _dp(tt)
+
+    def extract(self, level):
+        lib().or_extract_layer(C.byref(self.fa.b), C.byref(self.so.b), C.byref(self.p), level, self.bf, self.bt)
+
+    def father_to_son(self, n_timeStep):
+        lib().or_interp_f2s(C.byref(self.so.b), C.byref(self.fa.b), C.byref(self.p), n_timeStep, self.bf, self.bt,
+                            self.scheme)
+
+    def son_to_father(self):
+        lib().or_deliver_s2f(C.byref(self.fa.b), C.byref(self.so.b), C.byref(self.p))
+
+
+def block_stage_pre(b):
+    """update_volume_force_ .. add_volume_force_ without bodies"""
+    L = lib()
+    L.or_update_volume_force(C.byref(b.b), C.byref(b.flow))
+    L.or_macro(C.byref(b.b))
+    L.or_reset_force(C.byref(b.b))
+    L.or_add_force(C.byref(b.b))
+
+
+def block_stage_post(b):
+    """collision_ .. set_boundary_conditions_"""
+    L = lib()
+    L.or_collide(C.byref(b.b))
+    L.or_halfway_set(C.byref(b.b))
+    L.or_stream(C.byref(b.b), _dp(b.tmp))
+    if L.or_set_bc(C.byref(b.b), C.byref(b.flow)) != 0:
+        raise RuntimeError("oracle: unknown boundary condition")
 
 
 def feq(density, vel):

@@ -156,3 +156,15 @@ def test_ib_stationary_plate_symmetric_force():
     assert F_[0] > 0  # v_Eforce is the force on the body: drag along the flow
     assert abs(F_[1]) < 1e-10 * abs(F_[0]) + 1e-14
     assert abs(F_[2]) < 1e-10 * abs(F_[0]) + 1e-14
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+def test_refined_uniform_flow_stays_uniform(scheme):
+    from refine import TwoLevel
+    tl = TwoLevel(gpu=False, scheme=scheme)
+    f0 = tl.ofa.fview().copy()
+    s0 = tl.oso.fview().copy()
+    for _ in range(3):
+        tl.step()
+    assert np.max(np.abs(tl.ofa.fview() - f0)) < 1e-15
+    assert np.max(np.abs(tl.oso.fview() - s0)) < 1e-15
