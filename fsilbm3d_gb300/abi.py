@@ -53,8 +53,10 @@ SYMBOLS = [
     "fsi_block_upload_f", "fsi_block_download_f", "fsi_block_initialise", "fsi_block_set_boundary_conditions",
     "fsi_block_macro", "fsi_block_step", "fsi_block_run", "fsi_ib_set_bodies", "fsi_ib_solve",
     "fsi_ib_get_stencil", "fsi_ib_get_window", "fsi_pair_create", "fsi_pair_destroy", "fsi_pair_extract",
-    "fsi_pair_father_to_son", "fsi_pair_son_to_father",
+    "fsi_pair_father_to_son", "fsi_pair_son_to_father", "fsi_pair_father_to_son_static",
 ]
+# son face cells the allocation-free father-to-son variant can hold
+STATIC_FACE_CELLS = 65536
 
 
 def library_path():
@@ -95,6 +97,7 @@ def load_library():
     L.fsi_pair_extract.argtypes = [VP, C.c_int]
     L.fsi_pair_father_to_son.argtypes = [VP, C.c_int, DP]
     L.fsi_pair_son_to_father.argtypes = [VP, DP]
+    L.fsi_pair_father_to_son_static.argtypes = [VP, C.c_int, DP]
     for s in SYMBOLS:
         getattr(L, s).restype = C.c_int
     _lib = L
@@ -301,6 +304,12 @@ class Pair:
         """interpolation_father_to_son (LBMBlockComm.f90:655-806)"""
         vf = _vec3(volumeForce)
         _check(load_library().fsi_pair_father_to_son(self.h, int(n_timeStep), _dp(vf)))
+
+    def father_to_son_static(self, n_timeStep, volumeForce=(0.0, 0.0, 0.0)):
+        """father_to_son without any device allocation: for hosts that may not
+        allocate GPU memory inside their time loop (fsi_pair_father_to_son_static)"""
+        vf = _vec3(volumeForce)
+        _check(load_library().fsi_pair_father_to_son_static(self.h, int(n_timeStep), _dp(vf)))
 
     def son_to_father(self, volumeForce=(0.0, 0.0, 0.0)):
         """deliver_son_to_father (LBMBlockComm.f90:546-653)"""

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 
 #include "../../include/fsi_gpu.h"
 #include "fsi_kernels.h"
@@ -812,3 +813,56 @@ int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
 
 }  // extern "C"
 
+// ------------------------------------------------- allocation-free variant
+// Scratch of fsi_pair_father_to_son_static: the interpolated son face
+// (19 populations per face cell) followed by its interpolated tau, for at
+// most FSI_STATIC_FACE_CELLS face cells. Each device that loads the library
+// holds this array until the process exits.
+static __device__ __align__(256) double g_pair_face_scratch[20LL * FSI_STATIC_FACE_CELLS];
+
+namespace {
+std::mutex g_scratch_mu;
+double *g_scratch_ptr[256] = {};  // device address of the array, per device
+
+// looked up once per device, with that device current
+int static_scratch(double **out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(FSI_E_ARG, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        double *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_pair_face_scratch);
+        if (e != cudaSuccess) return fail(FSI_E_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return FSI_OK;
+}
+}  // namespace
+
+extern "C" int fsi_pair_father_to_son_static(fsi_pair_t p, int n_timeStep, const double vf[3]) {
+    if (!p || !vf) return fail(FSI_E_ARG, "invalid argument");
+    fsi_block *so = p->so, *fa = p->fa;
+    for (int k = 0; k < 6; k++) {
+        if (p->p.sds[k] == 0) continue;
+        int ax = k >> 1;
+        long long AS = ax == 2 ? p->p.yDimS : p->p.zDimS, BS = ax == 0 ? p->p.yDimS : p->p.xDimS;
+        if (AS * BS > FSI_STATIC_FACE_CELLS)
+            return fail(FSI_E_ARG, "son face of %lld cells exceeds the static scratch of %d face cells", AS * BS,
+                        FSI_STATIC_FACE_CELLS);
+    }
+    double *scr = nullptr;
+    int rc = static_scratch(&scr);
+    if (rc) return rc;
+    double *scr_f = scr, *scr_t = scr + 19LL * FSI_STATIC_FACE_CELLS;
+    CK(cudaStreamSynchronize(fa->st));
+    for (int k = 0; k < 6; k++) {
+        if (p->p.sds[k] == 0) continue;
+        int lvl = (n_timeStep == 0) ? 0 : 1;
+        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
+                           p->scheme, scr_f, scr_t, FSI_STATIC_FACE_CELLS, vf, fa->d.dh, p->d_err, so->st));
+    }
+    CK(cudaStreamSynchronize(so->st));
+    return pair_check(p);
+}

@@ -151,6 +151,23 @@ int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]);
 /* deliver_son_to_father (LBMBlockComm.f90:546-653); vf = son volume force */
 int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]);
 
+/* No counterpart in the reference. fsi_pair_father_to_son for callers that
+ * cannot allocate device memory once their time loop runs -- a host that
+ * budgets all GPU memory at start-up, or one that may not call cudaMalloc
+ * from its stepping code -- since fsi_pair_father_to_son interpolates the
+ * father's face into scratch planes that fsi_pair_create allocated. This
+ * variant allocates nothing: its scratch is one file-scope device array of
+ * FSI_STATIC_FACE_CELLS son face cells (20 doubles each, 10 MiB, held by
+ * every GPU that loads the library until the process exits). Faces larger
+ * than that return FSI_E_ARG. The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. All calls share the one array and each call leaves its
+ * last contents there (every element is written before it is read, so
+ * nothing needs clearing): calls that overlap on the GPU, from different
+ * threads or streams, race. Same arguments and results as
+ * fsi_pair_father_to_son. */
+#define FSI_STATIC_FACE_CELLS 65536
+int fsi_pair_father_to_son_static(fsi_pair_t p, int n_timeStep, const double vf[3]);
 
 #ifdef __cplusplus
 }
