@@ -11,7 +11,6 @@ no pitching: the triad stays the identity).
 Marker layout matches the reference: marker (element i, span station s) is
 global marker cnt = i*Nspan + s.
 """
-import math
 
 import numpy as np
 
@@ -67,20 +66,13 @@ class RigidPlate:
         XYZ, UVW = self.body_state(t)
         pos = self.x00 + XYZ  # MapReferencePosToCurrent with TTT = I
         beta = -self.alpha * 2.0 * self.denIn
-        xyz = np.empty((self.M, 3))
-        vel = np.empty((self.M, 3))
-        area = np.empty(self.M)
-        for i in range(self.n_chord):
-            mid = 0.5 * (pos[i] + pos[i + 1])
-            len1 = math.sqrt(float(np.sum((pos[i + 1] - pos[i]) ** 2)))
-            dl = self.spanlen / self.n_span
-            a = dl * len1 * beta
-            for s in range(self.n_span):
-                ls = dl * (0.5 + s) - self.Lspan
-                m = i * self.n_span + s
-                xyz[m] = mid + self.dirc * ls
-                vel[m] = UVW
-                area[m] = a
+        mid = 0.5 * (pos[:-1] + pos[1:])                            # element centres
+        len1 = np.sqrt(np.sum((pos[1:] - pos[:-1]) ** 2, axis=1))   # element lengths
+        dl = self.spanlen / self.n_span
+        ls = dl * (0.5 + np.arange(self.n_span)) - self.Lspan       # span stations
+        xyz = (mid[:, None, :] + self.dirc[None, None, :] * ls[None, :, None]).reshape(self.M, 3)
+        vel = np.broadcast_to(UVW, (self.M, 3)).copy()
+        area = np.repeat(dl * len1 * beta, self.n_span)
         return xyz, vel, area
 
 

@@ -25,7 +25,7 @@ UNITS = {
     # host arithmetic (tau, MRT matrices) without contraction, as the reference
     "fsi_abi.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "bc_impl.cuh"]
+HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "bc_impl.cuh", "ib_impl.cuh"]
 
 
 def _nvcc():

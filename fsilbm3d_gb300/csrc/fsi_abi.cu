@@ -130,6 +130,11 @@ struct fsi_block {
     float *d_ew = nullptr;
     double *h_tol = nullptr;  // pinned
     int *h_err = nullptr;     // pinned
+    // cooperative IB solve of the fast forms
+    int coop_grid = 0;
+    int *d_status = nullptr;  // 4 ints: flags, iterations, barrier count, generation
+    double *d_res = nullptr, *d_tolacc = nullptr;
+    int tolacc_cap = 0;
     // IB window
     IbGeom geom{};
     long long Nw = 0, Nw_cap = 0;
@@ -241,7 +246,7 @@ void free_block(fsi_block *h) {
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
-                    h->cnt, h->start, h->fillc, h->list};
+                    h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -590,6 +595,66 @@ int compute_window(fsi_block *h, const double *xyz) {
     return FSI_OK;
 }
 
+// The fast forms: one cooperative launch does the window macro, the stencil,
+// the whole penalty loop with its residual test and the spreading; the host
+// reads back the Lagrangian force, the iteration count and the residual.
+int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol,
+                  double *eforce, int *iters, double *residual) {
+    if (!h->coop_grid) {
+        h->coop_grid = ib_coop_grid(h->prec);
+        if (h->coop_grid <= 0) return fail(FSI_E_CUDA, "no co-resident grid for the IB kernel");
+    }
+    if (!h->d_status) {
+        CK(cudaMalloc((void **)&h->d_status, sizeof(int) * 4));
+        CK(cudaMalloc((void **)&h->d_res, sizeof(double)));
+    }
+    if (ntol > h->tolacc_cap) {
+        if (h->d_tolacc) cudaFree(h->d_tolacc);
+        h->tolacc_cap = std::max(ntol, 64);
+        CK(cudaMalloc((void **)&h->d_tolacc, sizeof(double) * h->tolacc_cap));
+    }
+    CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 4, h->st));
+    const double ih = 1.0 / h->d.dh;
+    IbCoop a{};
+    a.g = h->geom;
+    a.N = h->N;
+    a.Nw = h->Nw;
+    a.f = h->fa;
+    for (int k = 0; k < 3; k++) a.vf[k] = vf[k];
+    a.nb = h->nb;
+    a.Mtot = h->Mtot;
+    a.offs = h->d_offs;
+    a.xyz = h->d_xyz; a.vel = h->d_vel; a.area = h->d_area;
+    a.ei = h->d_ei; a.ew = h->d_ew;
+    a.eforce = h->d_eforce; a.fet = h->d_fet;
+    a.wden = h->wden; a.wu = h->wu; a.wforce = h->wforce;
+    a.ntol = ntol;
+    a.dtol = dtol;
+    a.dsumU = (double)h->Mtot * Uref;
+    a.invh3p = ((0.5 * dt) * ((ih * ih) * ih)) / denIn;  // Solidbody.f90:996
+    a.invh3s = (ih * ih) * ih;                          // Solidbody.f90:936
+    a.tol_acc = h->d_tolacc;
+    a.status = h->d_status;
+    a.res = h->d_res;
+    CK(launch_ib_coop(a, h->prec, h->coop_grid, h->st));
+    CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_err, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_tol + 1, h->d_status + 1, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const int st = *h->h_err;
+    if (st & 1) return fail(FSI_E_RANGE, "index out of block bounds in IB stencil");
+    if (st & 2) return fail(FSI_E_RANGE, "IB stencil outside the IB window");
+    if (st & 4) return fail(FSI_E_NAN, "Nan found in PenaltyForce");
+    if (st & 8) return fail(FSI_E_TIMEOUT, "IB grid barrier timed out");
+    int it = 0;
+    memcpy(&it, (const void *)(h->h_tol + 1), sizeof(int));
+    if (iters) *iters = it;
+    if (residual) *residual = h->h_tol[0];
+    h->win_valid = true;
+    return FSI_OK;
+}
+
 }  // namespace
 
 int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
@@ -607,6 +672,7 @@ int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const doub
     CK(cudaMemcpyAsync(h->d_xyz, xyz, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync(h->d_vel, vel, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync(h->d_area, area, sizeof(double) * Mt, cudaMemcpyHostToDevice, h->st));
+    if (h->prec != FSI_PREC_F64) return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, eforce, iters, residual);
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
     CK(cudaMemsetAsync(h->d_eforce, 0, sizeof(double) * 3 * Mt, h->st));
     // calculate_macro_quantities_ + ResetVolumeForce_ restricted to the window

@@ -39,6 +39,32 @@ cudaError_t launch_ib_spread(const float *ew, const int *start, const int *list,
                              const double *eforce, double invh3, const double vf[3],
                              double *wforce, cudaStream_t st);
 
+// One persistent cooperative launch for the whole IB solve of the fast forms
+// (k_fast.cu): window macro, stencil, the penalty loop with its residual test
+// on the device, spreading. status[0]: 1 stencil outside the block, 2 outside
+// the window, 4 non-finite residual, 8 a grid barrier timed out;
+// status[1]: iterations; status[2..3]: barrier count and generation.
+struct IbCoop {
+    IbGeom g;
+    long long N, Nw;
+    const void *f;
+    double vf[3];
+    int nb, Mtot;
+    const int *offs;
+    const double *xyz, *vel, *area;
+    int16_t *ei;
+    float *ew;
+    double *eforce, *fet;
+    double *wden, *wu, *wforce;
+    int ntol;
+    double dtol, dsumU, invh3p, invh3s;
+    double *tol_acc;  // ntol sums
+    int *status;
+    double *res;
+};
+cudaError_t launch_ib_coop(const IbCoop &a, int prec, int grid, cudaStream_t st);
+int ib_coop_grid(int prec);  // co-resident CTAs (256 threads) on this device, 0 on error
+
 // ---- block refinement (k_f64_exact.cu) ----
 struct PairGeom {
     int sds[6], s[6], f[6], si[6], fi[6];

@@ -10,6 +10,7 @@
 // block-refinement face exchange.
 #include "fsi_kernels.h"
 #include "bc_impl.cuh"
+#include "ib_impl.cuh"
 
 #include <math.h>
 
@@ -220,84 +221,18 @@ __global__ void k_win_macro(const double *__restrict__ f, double *wden, double *
     wu[wc] = u0; wu[wc + Nw] = u1; wu[wc + 2 * Nw] = u2;
 }
 
-// Phi, Solidbody.f90:822-833
-__device__ __forceinline__ double phi4(double x) {
-    double r = fabs(x);
-    if (r < 1.0) return ((3.0 - 2.0 * r) + sqrt(1.0 + (4.0 * r) * (1.0 - r))) * 0.125;
-    if (r < 2.0) return ((5.0 - 2.0 * r) - sqrt(-7.0 + (4.0 * r) * (3.0 - r))) * 0.125;
-    return 0.0;
-}
-
-// trimedindex, Solidbody.f90:834-866 (1-based); returns false if out of range
-__device__ __forceinline__ bool trimed(int i, int dim, int out[4], int lo, int hi) {
-    bool ok = true;
-#pragma unroll
-    for (int k = -1; k <= 2; k++) {
-        int v = i + k;
-        if (v < 1) {
-            if (lo == BC_PERIODIC) v = v + dim;
-            else if ((lo == BC_SYMMETRIC || lo == BC_WALL) && v == 0) v = 2;
-            else if (lo == BC_WALL_HW && v == 0) v = 1;
-            else { ok = false; v = 1; }
-        } else if (v > dim) {
-            if (hi == BC_PERIODIC) v = v - dim;
-            else if ((hi == BC_SYMMETRIC || hi == BC_WALL) && v == dim + 1) v = dim - 1;
-            else if (hi == BC_WALL_HW && v == dim + 1) v = dim;
-            else { ok = false; v = dim; }
-        }
-        out[k + 1] = v;
-    }
-    return ok;
-}
-
 // UpdateElmtInterp_, Solidbody.f90:760-807. One thread per marker; the
 // stencil origin comes from the first marker of the marker's body.
+// Out-of-window indices come back clamped into the window so that no later
+// kernel reads outside it; the host reports the error and stops.
 __global__ void k_ib_stencil(const double *__restrict__ xyz, const int *__restrict__ offs, int nb, int Mtot,
                              IbGeom g, int16_t *ei, float *ew, int *err) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= Mtot) return;
     int b = 0;
     while (b + 1 < nb && m >= offs[b + 1]) b++;
-    const double *p0 = xyz + 3LL * offs[b];
-    const double invdh = 1.0 / g.dh;
-    int i0 = (int)floor((p0[0] - g.xmin) * invdh);
-    double x0 = g.xmin + (double)i0 * g.dh;
-    i0 = i0 + 1;
-    int j0 = (int)floor((p0[1] - g.ymin) * invdh);
-    double y0 = g.ymin + (double)j0 * g.dh;
-    j0 = j0 + 1;
-    int k0 = (int)floor((p0[2] - g.zmin) * invdh);
-    double z0 = g.zmin + (double)k0 * g.dh;
-    k0 = k0 + 1;
-    const double *p = xyz + 3LL * m;
-    double ox = (p[0] - x0) * invdh, oy = (p[1] - y0) * invdh, oz = (p[2] - z0) * invdh;
-    int i = (int)floor(ox), j = (int)floor(oy), k = (int)floor(oz);
-    double detx = ox - (double)i, dety = oy - (double)j, detz = oz - (double)k;
-    i += i0; j += j0; k += k0;
-    int ix[4], jy[4], kz[4];
-    bool ok = trimed(i, g.X, ix, g.bc[0], g.bc[1]);
-    ok = trimed(j, g.Y, jy, g.bc[2], g.bc[3]) && ok;
-    ok = trimed(k, g.Z, kz, g.bc[4], g.bc[5]) && ok;
-    bool inwin = true;
-#pragma unroll
-    for (int t = 0; t < 4; t++) {
-        inwin = inwin && (ix[t] - 1 >= g.wx0) && (ix[t] - 1 <= g.wx1) && (jy[t] - 1 >= g.wy0) &&
-                (jy[t] - 1 <= g.wy1) && (kz[t] - 1 >= g.wz0) && (kz[t] - 1 <= g.wz1);
-    }
-    if (!ok) atomicOr(err, 1);
-    if (!inwin) atomicOr(err, 2);
-    int16_t *e = ei + 12LL * m;
-    float *w = ew + 12LL * m;
-#pragma unroll
-    for (int t = 0; t < 4; t++) {
-        // out-of-window indices are clamped into the window so that no later
-        // kernel reads outside it; the host reports the error and stops
-        int xi = inwin ? ix[t] : g.wx0 + 1, yi = inwin ? jy[t] : g.wy0 + 1, zi = inwin ? kz[t] : g.wz0 + 1;
-        e[t] = (int16_t)xi; e[4 + t] = (int16_t)yi; e[8 + t] = (int16_t)zi;
-        w[t] = (float)phi4((double)(t - 1) - detx);
-        w[4 + t] = (float)phi4((double)(t - 1) - dety);
-        w[8 + t] = (float)phi4((double)(t - 1) - detz);
-    }
+    const int st = ib_stencil_one(xyz + 3LL * offs[b], xyz + 3LL * m, g, ei + 12LL * m, ew + 12LL * m);
+    if (st) atomicOr(err, st);
 }
 
 // window cell of stencil entry e = marker*64 + (x*16 + y*4 + z)

@@ -20,6 +20,7 @@
 
 #include "bc_impl.cuh"
 #include "fsi_kernels.h"
+#include "ib_impl.cuh"
 #include "../../include/fsi_gpu.h"
 
 namespace fsi {
@@ -547,6 +548,170 @@ __global__ void k_win_macro_fast(const void *__restrict__ fs, double *wden, doub
     wu[wc] = u0; wu[wc + Nw] = u1; wu[wc + 2 * Nw] = u2;
 }
 
+// ---------------------------------------------------------------------------
+// Immersed boundary for the fast forms: the whole of calculate_interaction_force
+// (Solidbody.f90:869-918) in one persistent cooperative launch. Phases are
+// separated by a grid barrier; a warp serves one marker (two stencil points per
+// lane, shuffle reduction); the velocity correction and the spreading scatter
+// with FP64 atomics, so sums are not in the reference's order (the exact form
+// keeps that order). Data written inside the launch are read through L2
+// (__ldcg): L1 is not coherent across SMs.
+// ---------------------------------------------------------------------------
+
+// grid barrier with an iteration limit: on timeout the status gets bit 8 and
+// every CTA returns
+__device__ __forceinline__ bool gbar(int *status, unsigned nblk) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned *cnt = (unsigned *)(status + 2);
+        volatile unsigned *gen = (volatile unsigned *)(status + 3);
+        const unsigned g0 = *gen;
+        __threadfence();
+        if (atomicAdd(cnt, 1u) == nblk - 1) {
+            *cnt = 0;
+            __threadfence();
+            atomicAdd((unsigned *)(status + 3), 1u);
+        } else {
+            long long it = 0;
+            while (*gen == g0) {
+                if (++it > (1LL << 24)) { atomicOr(status, 8); break; }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return (*(volatile int *)status & 8) == 0;
+}
+
+__device__ __forceinline__ long long ib_wcell(const IbGeom &g, const int16_t *s, int p) {
+    return (long long)(s[8 + (p & 3)] - 1 - g.wz0) +
+           (long long)g.WZ * ((long long)(s[4 + ((p >> 2) & 3)] - 1 - g.wy0) + (long long)g.WY * (s[p >> 4] - 1 - g.wx0));
+}
+
+__device__ __forceinline__ double ib_weight(const float *w, int p) {
+    return ((double)w[p >> 4] * (double)w[4 + ((p >> 2) & 3)]) * (double)w[8 + (p & 3)];
+}
+
+template <int P>
+__global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
+    using T = ST<P>;
+    using C = typename T::C;
+    const unsigned nblk = gridDim.x;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nth = (long long)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    const long long gw = tid >> 5, nw = nth >> 5;
+    const IbGeom &g = a.g;
+    const long long Nw = a.Nw;
+
+    // calculate_macro_quantities_ and the force reset + add_volume_force_ on the window
+    const C vf[3] = {(C)a.vf[0], (C)a.vf[1], (C)a.vf[2]};
+    for (long long wc = tid; wc < Nw; wc += nth) {
+        const int wz = (int)(wc % g.WZ);
+        const long long t = wc / g.WZ;
+        const int wy = (int)(t % g.WY), wx = (int)(t / g.WY);
+        const long long c = cidx(wz + g.wz0, wy + g.wy0, wx + g.wx0, g.Z, g.Y);
+        const typename T::S *src = (const typename T::S *)a.f;
+        C gl[Q];
+#pragma unroll
+        for (int i = 0; i < Q; i++) gl[i] = T::dec(src[c + a.N * i]);
+        C rho, drho, u0, u1, u2;
+        macro_fast<P>(gl, vf, (C)g.dh, rho, drho, u0, u1, u2);
+        a.wden[wc] = T::OFF ? 1.0 + (double)drho : (double)rho;
+        a.wu[wc] = u0; a.wu[wc + Nw] = u1; a.wu[wc + 2 * Nw] = u2;
+        a.wforce[wc] = a.vf[0]; a.wforce[wc + Nw] = a.vf[1]; a.wforce[wc + 2 * Nw] = a.vf[2];
+    }
+    // UpdateElmtInterp_ and v_Eforce = 0 (Solidbody.f90:886-889)
+    for (long long m = tid; m < a.Mtot; m += nth) {
+        int b = 0;
+        while (b + 1 < a.nb && m >= a.offs[b + 1]) b++;
+        const int st = ib_stencil_one(a.xyz + 3LL * a.offs[b], a.xyz + 3 * m, g, a.ei + 12 * m, a.ew + 12 * m);
+        if (st) atomicOr(a.status, st);
+        a.eforce[3 * m] = 0.0; a.eforce[3 * m + 1] = 0.0; a.eforce[3 * m + 2] = 0.0;
+    }
+    for (long long i = tid; i < a.ntol; i += nth) a.tol_acc[i] = 0.0;
+    if (!gbar(a.status, nblk)) return;
+    if (*(volatile int *)a.status & 3) return;
+
+    // the PenaltyForce_ loop, Solidbody.f90:893-906 (bodies one after another)
+    int it = 0;
+    double dmax = 1e10;
+    while (it < a.ntol && dmax > a.dtol) {
+        for (int b = 0; b < a.nb; b++) {
+            const int m0 = a.offs[b], m1 = a.offs[b + 1];
+            for (long long m = m0 + gw; m < m1; m += nw) {
+                const int16_t *s = a.ei + 12 * m;
+                const float *w = a.ew + 12 * m;
+                double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+                for (int p = lane; p < 64; p += 32) {
+                    const long long wc = ib_wcell(g, s, p);
+                    const double wt = ib_weight(w, p);
+                    v0 += __ldcg(a.wu + wc) * wt;
+                    v1 += __ldcg(a.wu + wc + Nw) * wt;
+                    v2 += __ldcg(a.wu + wc + 2 * Nw) * wt;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+                    v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+                    v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+                }
+                if (lane == 0) {
+                    const double d0 = a.vel[3 * m] - v0, d1 = a.vel[3 * m + 1] - v1, d2 = a.vel[3 * m + 2] - v2;
+                    const double ar = a.area[m];
+                    const double F0 = d0 * ar, F1 = d1 * ar, F2 = d2 * ar;
+                    a.eforce[3 * m] = __ldcg(a.eforce + 3 * m) + F0;
+                    a.eforce[3 * m + 1] = __ldcg(a.eforce + 3 * m + 1) + F1;
+                    a.eforce[3 * m + 2] = __ldcg(a.eforce + 3 * m + 2) + F2;
+                    a.fet[3 * m] = F0 * a.invh3p; a.fet[3 * m + 1] = F1 * a.invh3p; a.fet[3 * m + 2] = F2 * a.invh3p;
+                    atomicAdd(a.tol_acc + it, (fabs(d0) + fabs(d1)) + fabs(d2));
+                }
+            }
+            if (!gbar(a.status, nblk)) return;
+            // the velocity correction of the support (Solidbody.f90:1034-1048)
+            for (long long m = m0 + gw; m < m1; m += nw) {
+                const int16_t *s = a.ei + 12 * m;
+                const float *w = a.ew + 12 * m;
+                const double f0 = __ldcg(a.fet + 3 * m), f1 = __ldcg(a.fet + 3 * m + 1), f2 = __ldcg(a.fet + 3 * m + 2);
+                for (int p = lane; p < 64; p += 32) {
+                    const long long wc = ib_wcell(g, s, p);
+                    const double wt = ib_weight(w, p);
+                    atomicAdd(a.wu + wc, -(f0 * wt));
+                    atomicAdd(a.wu + wc + Nw, -(f1 * wt));
+                    atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
+                }
+            }
+            if (!gbar(a.status, nblk)) return;
+        }
+        const double tol = __ldcg(a.tol_acc + it);
+        if (!isfinite(tol)) {
+            if (tid == 0) atomicOr(a.status, 4);
+            return;
+        }
+        dmax = tol / a.dsumU;
+        it = it + 1;
+    }
+    // FluidVolumeForce_ spreading (Solidbody.f90:968-977) onto vf
+    for (long long m = gw; m < a.Mtot; m += nw) {
+        const int16_t *s = a.ei + 12 * m;
+        const float *w = a.ew + 12 * m;
+        const double f0 = __ldcg(a.eforce + 3 * m) * a.invh3s, f1 = __ldcg(a.eforce + 3 * m + 1) * a.invh3s,
+                     f2 = __ldcg(a.eforce + 3 * m + 2) * a.invh3s;
+        for (int p = lane; p < 64; p += 32) {
+            const long long wc = ib_wcell(g, s, p);
+            const double wt = ib_weight(w, p);
+            atomicAdd(a.wforce + wc, -(f0 * wt));
+            atomicAdd(a.wforce + wc + Nw, -(f1 * wt));
+            atomicAdd(a.wforce + wc + 2 * Nw, -(f2 * wt));
+        }
+    }
+    if (tid == 0) {
+        a.status[1] = it;
+        *a.res = dmax;
+    }
+}
+
 template <int P>
 __global__ void k_to_store(const double *__restrict__ f, void *fs, long long N) {
     using T = ST<P>;
@@ -663,6 +828,26 @@ cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, 
     long long N = (long long)X * Y * Z;
     FSI_DISPATCH(prec, k_macro_fast<PP><<<g, bz, 0, st>>>(fs, den, u, Y, Z, N, dh, vf[0], vf[1], vf[2]);
                  return cudaGetLastError())
+}
+
+cudaError_t launch_ib_coop(const IbCoop &a, int prec, int grid, cudaStream_t st) {
+    void *args[] = {(void *)&a};
+    FSI_DISPATCH(prec, return cudaLaunchCooperativeKernel((void *)k_ib_coop<PP>, grid, 256, args, 0, st))
+}
+
+int ib_coop_grid(int prec) {
+    int dev = 0, sms = 0, nb = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (prec) {
+    case FSI_PREC_F64_FAST: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_F64_FAST>, 256, 0); break;
+    case FSI_PREC_F32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_F32>, 256, 0); break;
+    case FSI_PREC_F16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_F16>, 256, 0); break;
+    case FSI_PREC_BF16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_BF16>, 256, 0); break;
+    default: break;
+    }
+    return e == cudaSuccess ? nb * sms : 0;
 }
 
 cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double *wu, const IbGeom &g, long long N,

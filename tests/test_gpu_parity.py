@@ -183,6 +183,59 @@ def test_mixed_ib_force(gpu_lib, prec):
     assert np.max(np.abs(Fg - Fo)) <= tol * np.max(np.abs(Fo))
 
 
+@pytest.mark.parametrize("prec", [F.PREC_F64_FAST, F.PREC_F16])
+def test_fast_ib_converges_like_oracle(gpu_lib, prec):
+    # the cooperative single-launch IB solve: same stopping rule on the device
+    dims = (36, 24, 20)
+    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.0, 0.0), nu=0.02,
+             plates=[plate_in(dims, n=5)], ntol=200, dtol=0.2, Uref=0.05, precision=prec)
+    c.init_equilibrium()
+    r = c.step()
+    assert abs(r["it_o"] - r["it_g"]) <= (0 if prec == F.PREC_F64_FAST else 1)
+    assert r["res_g"] <= 0.2
+    rel = np.max(np.abs(r["ef_g"] - r["ef_o"])) / np.max(np.abs(r["ef_o"]))
+    assert rel < (1e-12 if prec == F.PREC_F64_FAST else 2e-2)
+
+
+@pytest.mark.parametrize("prec", [F.PREC_F64_FAST, F.PREC_F32, F.PREC_BF16])
+def test_fast_ib_two_plates_many_steps(gpu_lib, prec):
+    dims = (40, 24, 20)
+    plates = [plate_in(dims, n=5, heave=1.5, freq=0.02),
+              plate_in(dims, n=4, heave=-1.0, freq=0.03, center=(26.4, 11.7, 9.6))]
+    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.0, 0.0), nu=0.02, plates=plates, ntol=4,
+             dtol=1e-12, Uref=0.05, precision=prec)
+    c.init_equilibrium()
+    for s in range(8):
+        r = c.step()
+        assert r["it_g"] == r["it_o"] == 4
+    Fo, Fg = r["ef_o"].sum(axis=0), r["ef_g"].sum(axis=0)
+    tol = {F.PREC_F64_FAST: 1e-10, F.PREC_F32: 1e-4, F.PREC_BF16: 5e-2}[prec]
+    assert np.max(np.abs(Fg - Fo)) <= tol * np.max(np.abs(Fo))
+
+
+def test_fast_ib_errors_are_status_codes(gpu_lib):
+    b = F.Block(16, 16, 16, bndConds=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0, 0), precision=F.PREC_F16)
+    b.initialise(0.0)
+    b.ib_set_bodies([4])
+    xyz = np.array([[8.2, 8.1, 8.3], [8.7, 8.1, 8.3], [9.2, 8.1, 8.3], [9.7, 8.1, 8.3]])
+    vel = np.zeros((4, 3))
+    area = -2.0 * np.ones(4)
+    ef, it, res = b.ib_solve(xyz, vel, area, ntol=3, dtol=0.0, Uref=0.05)
+    assert it == 3 and np.all(np.isfinite(ef))
+    bad = vel.copy()
+    bad[2, 1] = np.inf
+    with pytest.raises(F.FsiError) as e:
+        b.ib_solve(xyz, bad, area, ntol=2, dtol=0.0, Uref=0.05)
+    assert e.value.code == -3
+    far = xyz.copy()
+    far[0, 0] = 0.2
+    with pytest.raises(F.FsiError) as e:
+        b.ib_solve(far, vel, area, ntol=2, dtol=0.0, Uref=0.05)
+    assert e.value.code == -6
+    b.step(blktime=1.0)
+    assert np.all(np.isfinite(b.download_f()))
+
+
 # --------------------------------------------------------------- error paths
 
 def test_errors_are_status_codes(gpu_lib):
