@@ -54,7 +54,11 @@ SYMBOLS = [
     "fsi_block_macro", "fsi_block_step", "fsi_block_run", "fsi_ib_set_bodies", "fsi_ib_solve",
     "fsi_ib_get_stencil", "fsi_ib_get_window", "fsi_pair_create", "fsi_pair_destroy", "fsi_pair_extract",
     "fsi_pair_father_to_son", "fsi_pair_son_to_father", "fsi_pair_father_to_son_static",
+    "fsi_mlp_create", "fsi_mlp_destroy", "fsi_mlp_set_params", "fsi_mlp_get_params", "fsi_mlp_set_norm",
+    "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm",
 ]
+# the warm-start perceptron (FSI_MLP_* in the header)
+MLP_IN, MLP_OUT, MLP_NPARAM, MLP_NNORM = 12, 3, 5187, 30
 # son face cells the allocation-free father-to-son variant can hold
 STATIC_FACE_CELLS = 65536
 
@@ -98,6 +102,17 @@ def load_library():
     L.fsi_pair_father_to_son.argtypes = [VP, C.c_int, DP]
     L.fsi_pair_son_to_father.argtypes = [VP, DP]
     L.fsi_pair_father_to_son_static.argtypes = [VP, C.c_int, DP]
+    FP = C.POINTER(C.c_float)
+    L.fsi_mlp_create.argtypes = [C.POINTER(VP), C.c_ulonglong]
+    L.fsi_mlp_destroy.argtypes = [VP]
+    L.fsi_mlp_set_params.argtypes = [VP, FP, C.c_int]
+    L.fsi_mlp_get_params.argtypes = [VP, FP, C.c_int]
+    L.fsi_mlp_set_norm.argtypes = [VP, FP]
+    L.fsi_mlp_forward.argtypes = [VP, FP, C.c_int, FP]
+    L.fsi_mlp_grad.argtypes = [VP, FP, FP, C.c_int, FP, FP]
+    L.fsi_mlp_train.argtypes = [VP, FP, FP, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, FP]
+    L.fsi_ib_solve_warm.argtypes = [VP, DP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int,
+                                    C.c_double, VP, FP, DP, IP, DP]
     for s in SYMBOLS:
         getattr(L, s).restype = C.c_int
     _lib = L
@@ -116,6 +131,14 @@ def _check(rc):
 
 def _dp(a):
     return a.ctypes.data_as(DP)
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _f32(a, cols):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, cols))
 
 
 def _vec3(v):
@@ -263,6 +286,36 @@ class Block:
                                            _dp(eforce), C.byref(it), C.byref(res)))
         return eforce.reshape(-1, 3), it.value, res.value
 
+    def ib_solve_warm(self, xyz, vel, area, aux=None, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0,
+                      ntol=3, dtol=1e-5, warm=None, features=False):
+        """ib_solve with the learned warm start (fast forms only).
+        aux (Mtot,6): acceleration, normal per marker (None: zeros); warm: an
+        Mlp or None; features=True also returns the (Mtot,12) feature array.
+        Returns (eforce, iterations, residual[, features])."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        area = np.ascontiguousarray(area, dtype=np.float64).reshape(-1)
+        if area.size != self.Mtot or xyz.size != 3 * self.Mtot or vel.size != 3 * self.Mtot:
+            raise ValueError("marker arrays do not match the bodies set with ib_set_bodies")
+        auxp = DP()
+        if aux is not None:
+            aux = np.ascontiguousarray(aux, dtype=np.float64).reshape(-1)
+            if aux.size != 6 * self.Mtot:
+                raise ValueError("aux must hold 6 values per marker")
+            auxp = _dp(aux)
+        eforce = np.empty(3 * self.Mtot)
+        feat = np.empty((self.Mtot, MLP_IN), dtype=np.float32) if features else None
+        vf = _vec3(volumeForce)
+        it = C.c_int()
+        res = C.c_double()
+        _check(load_library().fsi_ib_solve_warm(self.h, _dp(xyz), _dp(vel), _dp(area), auxp, _dp(vf), denIn,
+                                                self.dh if dt is None else dt, Uref, int(ntol), dtol,
+                                                warm.h if warm is not None else None,
+                                                _fp(feat) if features else C.POINTER(C.c_float)(),
+                                                _dp(eforce), C.byref(it), C.byref(res)))
+        out = (eforce.reshape(-1, 3), it.value, res.value)
+        return out + (feat,) if features else out
+
     def ib_stencil(self):
         ei = np.empty(12 * self.Mtot, dtype=np.int16)
         ew = np.empty(12 * self.Mtot, dtype=np.float32)
@@ -315,3 +368,75 @@ class Pair:
         """deliver_son_to_father (LBMBlockComm.f90:546-653)"""
         vf = _vec3(volumeForce)
         _check(load_library().fsi_pair_son_to_father(self.h, _dp(vf)))
+
+
+class Mlp:
+    """The warm-start perceptron (12 -> 64 -> 64 -> 3, tanh, FP32) on the
+    current device: inference, full-batch gradient and Adam training run in
+    the library's CUDA kernels."""
+
+    def __init__(self, seed=0):
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.fsi_mlp_create(C.byref(h), C.c_ulonglong(seed)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().fsi_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self):
+        P = np.empty(MLP_NPARAM, dtype=np.float32)
+        _check(load_library().fsi_mlp_get_params(self.h, _fp(P), MLP_NPARAM))
+        return P
+
+    @params.setter
+    def params(self, P):
+        P = np.ascontiguousarray(P, dtype=np.float32).reshape(-1)
+        _check(load_library().fsi_mlp_set_params(self.h, _fp(P), int(P.size)))
+
+    def set_norm(self, mean_in, std_in, mean_out, std_out):
+        nrm = np.concatenate([np.ravel(mean_in), np.ravel(std_in), np.ravel(mean_out), np.ravel(std_out)])
+        nrm = np.ascontiguousarray(nrm, dtype=np.float32)
+        if nrm.size != MLP_NNORM:
+            raise ValueError("expected %d statistics" % MLP_NNORM)
+        _check(load_library().fsi_mlp_set_norm(self.h, _fp(nrm)))
+
+    def fit_norm(self, X, Y, floor=1e-6):
+        """statistics from a training set (deviations floored at floor)"""
+        X = np.asarray(X, dtype=np.float64).reshape(-1, MLP_IN)
+        Y = np.asarray(Y, dtype=np.float64).reshape(-1, MLP_OUT)
+        self.set_norm(X.mean(0), np.maximum(X.std(0), floor), Y.mean(0), np.maximum(Y.std(0), floor))
+
+    def forward(self, X):
+        X = _f32(X, MLP_IN)
+        Y = np.empty((X.shape[0], MLP_OUT), dtype=np.float32)
+        _check(load_library().fsi_mlp_forward(self.h, _fp(X), int(X.shape[0]), _fp(Y)))
+        return Y
+
+    def grad(self, X, Y):
+        X, Y = _f32(X, MLP_IN), _f32(Y, MLP_OUT)
+        if X.shape[0] != Y.shape[0]:
+            raise ValueError("X and Y hold different sample counts")
+        g = np.empty(MLP_NPARAM, dtype=np.float32)
+        loss = C.c_float()
+        _check(load_library().fsi_mlp_grad(self.h, _fp(X), _fp(Y), int(X.shape[0]), _fp(g), C.byref(loss)))
+        return g, loss.value
+
+    def train(self, X, Y, epochs=100, batch=256, lr=1e-3, seed=0):
+        """Adam over shuffled mini-batches; returns the per-epoch mean loss"""
+        X, Y = _f32(X, MLP_IN), _f32(Y, MLP_OUT)
+        if X.shape[0] != Y.shape[0]:
+            raise ValueError("X and Y hold different sample counts")
+        hist = np.empty(int(epochs), dtype=np.float32)
+        _check(load_library().fsi_mlp_train(self.h, _fp(X), _fp(Y), int(X.shape[0]), int(epochs), int(batch),
+                                            C.c_float(lr), C.c_ulonglong(seed), _fp(hist)))
+        return hist

@@ -1,8 +1,9 @@
 """Build libfsi_gpu.so (sm_103a) in-tree with nvcc.
 
-Three translation units, compiled in parallel:
+Four translation units, compiled in parallel:
   k_f64_exact.cu  -fmad=false  FP64 kernels in the reference's operation order
   k_fast.cu                    FP64 regrouped and FP32/FP16/BF16 storage forms
+  k_mlp.cu                     warm-start perceptron: inference, gradient, Adam
   fsi_abi.cu                   host implementation of include/fsi_gpu.h
 """
 import os
@@ -22,10 +23,11 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
 UNITS = {
     "k_f64_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "k_fast.cu": [],
+    "k_mlp.cu": [],
     # host arithmetic (tau, MRT matrices) without contraction, as the reference
     "fsi_abi.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "bc_impl.cuh", "ib_impl.cuh"]
+HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "bc_impl.cuh", "ib_impl.cuh", "mlp_impl.cuh"]
 
 
 def _nvcc():

@@ -16,8 +16,12 @@
 
 #include "../../include/fsi_gpu.h"
 #include "fsi_kernels.h"
+#include "mlp_impl.cuh"
 
 using namespace fsi;
+
+static_assert(FSI_MLP_IN == MLP_IN && FSI_MLP_OUT == MLP_OUT, "perceptron shape");
+static_assert(FSI_MLP_NPARAM == MLP_NP && FSI_MLP_NNORM == MLP_NNORM, "perceptron sizes");
 
 namespace {
 
@@ -135,6 +139,10 @@ struct fsi_block {
     int *d_status = nullptr;  // 4 ints: flags, iterations, barrier count, generation
     double *d_res = nullptr, *d_tolacc = nullptr;
     int tolacc_cap = 0;
+    // warm start: per-marker auxiliary inputs and logged features
+    double *d_aux = nullptr;
+    float *d_feat = nullptr;
+    int warm_cap = 0;
     // IB window
     IbGeom geom{};
     long long Nw = 0, Nw_cap = 0;
@@ -157,6 +165,21 @@ struct fsi_pair {
     double *scr_f = nullptr, *scr_t = nullptr;
     long long scr_cells = 0;
     int *d_err = nullptr;  // first out-of-range access of a face kernel: code, index lo, hi
+};
+
+// The warm-start perceptron: parameters, input/output statistics, Adam state
+// and the training set, all resident on the device of its creation.
+struct fsi_mlp {
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    float *P = nullptr, *nrm = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr, *loss = nullptr;
+    float *X = nullptr, *Y = nullptr;
+    int *perm = nullptr, *hperm = nullptr;  // two epochs' sample orders, device and pinned host
+    cudaEvent_t ev[2] = {nullptr, nullptr};  // each order slot's last use
+    long long cap = 0;  // samples the training buffers hold
+    int loss_cap = 0;
+    int t = 0;          // Adam steps taken
+    bool norm_set = false;
 };
 
 namespace {
@@ -246,7 +269,8 @@ void free_block(fsi_block *h) {
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
-                    h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc};
+                    h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
+                    h->d_feat};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -515,9 +539,13 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     h->Mtot = h->offs[nbodies];
     if ((long long)h->Mtot * 64 > 0x7fffffffLL) return fail(FSI_E_ARG, "too many markers");
     for (int k = 0; k < 6; k++) h->ibbc[k] = bc ? bc[k] : h->d.bndConds[k];
-    void *ptrs[] = {h->d_offs, h->d_xyz, h->d_vel, h->d_area, h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew};
+    void *ptrs[] = {h->d_offs, h->d_xyz, h->d_vel, h->d_area, h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew,
+                    h->d_aux, h->d_feat};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    h->d_aux = nullptr;
+    h->d_feat = nullptr;
+    h->warm_cap = 0;
     int Mt = std::max(1, h->Mtot);
     CK(cudaMalloc((void **)&h->d_offs, sizeof(int) * (nbodies + 1)));
     CK(cudaMalloc((void **)&h->d_xyz, sizeof(double) * 3 * Mt));
@@ -598,8 +626,14 @@ int compute_window(fsi_block *h, const double *xyz) {
 // The fast forms: one cooperative launch does the window macro, the stencil,
 // the whole penalty loop with its residual test and the spreading; the host
 // reads back the Lagrangian force, the iteration count and the residual.
+struct Warm {
+    const fsi_mlp *mlp = nullptr;  // network of the warm start, or null
+    bool aux = false;              // d_aux holds this call's auxiliary inputs
+    float *features = nullptr;     // host (12,Mtot) out, or null
+};
+
 int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol,
-                  double *eforce, int *iters, double *residual) {
+                  const Warm &wm, double *eforce, int *iters, double *residual) {
     if (!h->coop_grid) {
         h->coop_grid = ib_coop_grid(h->prec);
         if (h->coop_grid <= 0) return fail(FSI_E_CUDA, "no co-resident grid for the IB kernel");
@@ -636,8 +670,15 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     a.tol_acc = h->d_tolacc;
     a.status = h->d_status;
     a.res = h->d_res;
+    a.mlp = wm.mlp ? wm.mlp->P : nullptr;
+    a.mlp_nrm = wm.mlp ? wm.mlp->nrm : nullptr;
+    a.aux = wm.aux ? h->d_aux : nullptr;
+    a.feat = wm.features ? h->d_feat : nullptr;
+    a.Uref = Uref;
     CK(launch_ib_coop(a, h->prec, h->coop_grid, h->st));
     CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
+    if (wm.features)
+        CK(cudaMemcpyAsync(wm.features, h->d_feat, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(h->h_err, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(h->h_tol + 1, h->d_status + 1, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -655,6 +696,17 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     return FSI_OK;
 }
 
+// the window and the marker arrays of one solve
+int ib_upload(fsi_block *h, const double *xyz, const double *vel, const double *area) {
+    int rc = compute_window(h, xyz);
+    if (rc) return rc;
+    const int Mt = h->Mtot;
+    CK(cudaMemcpyAsync(h->d_xyz, xyz, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_vel, vel, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_area, area, sizeof(double) * Mt, cudaMemcpyHostToDevice, h->st));
+    return FSI_OK;
+}
+
 }  // namespace
 
 int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
@@ -666,13 +718,10 @@ int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const doub
     if (residual) *residual = 0.0;
     if (h->nb == 0 || h->Mtot == 0) return FSI_OK;
     if (!xyz || !vel || !area || !eforce) return fail(FSI_E_ARG, "null marker array");
-    int rc = compute_window(h, xyz);
+    int rc = ib_upload(h, xyz, vel, area);
     if (rc) return rc;
     const int Mt = h->Mtot;
-    CK(cudaMemcpyAsync(h->d_xyz, xyz, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->d_vel, vel, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->d_area, area, sizeof(double) * Mt, cudaMemcpyHostToDevice, h->st));
-    if (h->prec != FSI_PREC_F64) return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, eforce, iters, residual);
+    if (h->prec != FSI_PREC_F64) return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, Warm{}, eforce, iters, residual);
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
     CK(cudaMemsetAsync(h->d_eforce, 0, sizeof(double) * 3 * Mt, h->st));
     // calculate_macro_quantities_ + ResetVolumeForce_ restricted to the window
@@ -720,6 +769,44 @@ int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const doub
     if (residual) *residual = dmax;
     h->win_valid = true;
     return FSI_OK;
+}
+
+int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double *aux,
+                      const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol, fsi_mlp_t warm,
+                      float *features, double *eforce, int *iters, double *residual) {
+    if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    if (h->prec == FSI_PREC_F64)
+        return fail(FSI_E_ARG, "the warm start needs a fast form; FSI_PREC_F64 keeps the reference's iteration");
+    if (warm && !warm->norm_set) return fail(FSI_E_STATE, "network statistics not set (fsi_mlp_set_norm)");
+    if (!(Uref > 0.0)) return fail(FSI_E_ARG, "Uref must be positive");
+    if (warm) {
+        int dev = -1;
+        CK(cudaGetDevice(&dev));
+        if (dev != warm->dev) return fail(FSI_E_ARG, "network lives on device %d, block on %d", warm->dev, dev);
+    }
+    h->win_valid = false;
+    if (iters) *iters = 0;
+    if (residual) *residual = 0.0;
+    if (h->nb == 0 || h->Mtot == 0) return FSI_OK;
+    if (!xyz || !vel || !area || !eforce) return fail(FSI_E_ARG, "null marker array");
+    int rc = ib_upload(h, xyz, vel, area);
+    if (rc) return rc;
+    if (h->warm_cap < h->Mtot) {
+        if (h->d_aux) cudaFree(h->d_aux);
+        if (h->d_feat) cudaFree(h->d_feat);
+        h->d_aux = nullptr;
+        h->d_feat = nullptr;
+        h->warm_cap = 0;
+        CK(cudaMalloc((void **)&h->d_aux, sizeof(double) * 6 * h->Mtot));
+        CK(cudaMalloc((void **)&h->d_feat, sizeof(float) * 12 * h->Mtot));
+        h->warm_cap = h->Mtot;
+    }
+    if (aux) CK(cudaMemcpyAsync(h->d_aux, aux, sizeof(double) * 6 * h->Mtot, cudaMemcpyHostToDevice, h->st));
+    Warm wm;
+    wm.mlp = warm;
+    wm.aux = aux != nullptr;
+    wm.features = features;
+    return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
 }
 
 int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew) {
@@ -875,6 +962,218 @@ int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
     }
     CK(cudaStreamSynchronize(fa->st));
     return pair_check(p);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- warm start
+
+namespace {
+
+uint64_t splitmix64(uint64_t &x) {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+double unit_uniform(uint64_t &x) { return (double)(splitmix64(x) >> 11) * (1.0 / 9007199254740992.0); }
+
+void free_mlp(fsi_mlp *m) {
+    if (!m) return;
+    void *ptrs[] = {m->P, m->nrm, m->grad, m->m, m->v, m->loss, m->X, m->Y, m->perm};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (m->hperm) cudaFreeHost(m->hperm);
+    for (int k = 0; k < 2; k++)
+        if (m->ev[k]) cudaEventDestroy(m->ev[k]);
+    if (m->st) cudaStreamDestroy(m->st);
+    delete m;
+}
+
+int mlp_reserve(fsi_mlp *m, long long n) {
+    if (n <= m->cap) return FSI_OK;
+    CK(cudaStreamSynchronize(m->st));
+    void *ptrs[] = {m->X, m->Y, m->perm};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (m->hperm) cudaFreeHost(m->hperm);
+    m->X = m->Y = nullptr;
+    m->perm = m->hperm = nullptr;
+    m->cap = 0;
+    CK(cudaMalloc((void **)&m->X, sizeof(float) * FSI_MLP_IN * n));
+    CK(cudaMalloc((void **)&m->Y, sizeof(float) * FSI_MLP_OUT * n));
+    CK(cudaMalloc((void **)&m->perm, sizeof(int) * 2 * n));
+    CK(cudaMallocHost((void **)&m->hperm, sizeof(int) * 2 * n));
+    m->cap = n;
+    return FSI_OK;
+}
+
+int mlp_reset_adam(fsi_mlp *m) {
+    CK(cudaMemsetAsync(m->grad, 0, sizeof(float) * FSI_MLP_NPARAM, m->st));
+    CK(cudaMemsetAsync(m->m, 0, sizeof(float) * FSI_MLP_NPARAM, m->st));
+    CK(cudaMemsetAsync(m->v, 0, sizeof(float) * FSI_MLP_NPARAM, m->st));
+    m->t = 0;
+    return FSI_OK;
+}
+
+int mlp_create(fsi_mlp *m, unsigned long long seed) {
+    CK(cudaGetDevice(&m->dev));
+    CK(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; k++) CK(cudaEventCreateWithFlags(&m->ev[k], cudaEventDisableTiming));
+    float **bufs[] = {&m->P, &m->grad, &m->m, &m->v};
+    for (float **b : bufs) CK(cudaMalloc((void **)b, sizeof(float) * FSI_MLP_NPARAM));
+    CK(cudaMalloc((void **)&m->nrm, sizeof(float) * FSI_MLP_NNORM));
+    m->loss_cap = 64;
+    CK(cudaMalloc((void **)&m->loss, sizeof(float) * m->loss_cap));
+    // Glorot-uniform weights, zero biases
+    std::vector<float> P(FSI_MLP_NPARAM, 0.0f);
+    uint64_t r = seed;
+    const int fan[3][2] = {{FSI_MLP_IN, MLP_H}, {MLP_H, MLP_H}, {MLP_H, FSI_MLP_OUT}};
+    const int w0[3] = {MLP_W1, MLP_W2, MLP_W3};
+    for (int l = 0; l < 3; l++) {
+        const double lim = std::sqrt(6.0 / (fan[l][0] + fan[l][1]));
+        for (int i = 0; i < fan[l][0] * fan[l][1]; i++) P[w0[l] + i] = (float)((2.0 * unit_uniform(r) - 1.0) * lim);
+    }
+    CK(cudaMemcpy(m->P, P.data(), sizeof(float) * FSI_MLP_NPARAM, cudaMemcpyHostToDevice));
+    std::vector<float> nrm(FSI_MLP_NNORM, 0.0f);
+    for (int k = 0; k < FSI_MLP_IN; k++) nrm[FSI_MLP_IN + k] = 1.0f;
+    for (int c = 0; c < FSI_MLP_OUT; c++) nrm[2 * FSI_MLP_IN + FSI_MLP_OUT + c] = 1.0f;
+    CK(cudaMemcpy(m->nrm, nrm.data(), sizeof(float) * FSI_MLP_NNORM, cudaMemcpyHostToDevice));
+    if (int rc = mlp_reset_adam(m)) return rc;
+    CK(cudaStreamSynchronize(m->st));
+    return FSI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsi_mlp_create(fsi_mlp_t *out, unsigned long long seed) {
+    if (!out) return fail(FSI_E_ARG, "null argument");
+    *out = nullptr;
+    fsi_mlp *m = new fsi_mlp;
+    if (int rc = mlp_create(m, seed)) {
+        free_mlp(m);
+        return rc;
+    }
+    *out = m;
+    return FSI_OK;
+}
+
+int fsi_mlp_destroy(fsi_mlp_t m) {
+    if (!m) return FSI_OK;
+    cudaStreamSynchronize(m->st);
+    free_mlp(m);
+    return FSI_OK;
+}
+
+int fsi_mlp_set_params(fsi_mlp_t m, const float *params, int n) {
+    if (!m || !params) return fail(FSI_E_ARG, "null argument");
+    if (n != FSI_MLP_NPARAM) return fail(FSI_E_ARG, "expected %d parameters, got %d", FSI_MLP_NPARAM, n);
+    CK(cudaMemcpyAsync(m->P, params, sizeof(float) * n, cudaMemcpyHostToDevice, m->st));
+    if (int rc = mlp_reset_adam(m)) return rc;
+    CK(cudaStreamSynchronize(m->st));
+    return FSI_OK;
+}
+
+int fsi_mlp_get_params(fsi_mlp_t m, float *params, int n) {
+    if (!m || !params) return fail(FSI_E_ARG, "null argument");
+    if (n != FSI_MLP_NPARAM) return fail(FSI_E_ARG, "expected %d parameters, got %d", FSI_MLP_NPARAM, n);
+    CK(cudaMemcpyAsync(params, m->P, sizeof(float) * n, cudaMemcpyDeviceToHost, m->st));
+    CK(cudaStreamSynchronize(m->st));
+    return FSI_OK;
+}
+
+int fsi_mlp_set_norm(fsi_mlp_t m, const float *norm) {
+    if (!m || !norm) return fail(FSI_E_ARG, "null argument");
+    for (int k = 0; k < FSI_MLP_NNORM; k++)
+        if (!std::isfinite(norm[k])) return fail(FSI_E_ARG, "non-finite statistic %d", k);
+    for (int k = 0; k < FSI_MLP_IN; k++)
+        if (!(norm[FSI_MLP_IN + k] > 0.0f)) return fail(FSI_E_ARG, "input deviation %d must be positive", k);
+    for (int c = 0; c < FSI_MLP_OUT; c++)
+        if (!(norm[2 * FSI_MLP_IN + FSI_MLP_OUT + c] > 0.0f))
+            return fail(FSI_E_ARG, "output deviation %d must be positive", c);
+    CK(cudaMemcpyAsync(m->nrm, norm, sizeof(float) * FSI_MLP_NNORM, cudaMemcpyHostToDevice, m->st));
+    CK(cudaStreamSynchronize(m->st));
+    m->norm_set = true;
+    return FSI_OK;
+}
+
+int fsi_mlp_forward(fsi_mlp_t m, const float *x, int n, float *y) {
+    if (!m || n < 0 || (n > 0 && (!x || !y))) return fail(FSI_E_ARG, "invalid argument");
+    if (!m->norm_set) return fail(FSI_E_STATE, "network statistics not set (fsi_mlp_set_norm)");
+    if (n == 0) return FSI_OK;
+    if (int rc = mlp_reserve(m, n)) return rc;
+    CK(cudaMemcpyAsync(m->X, x, sizeof(float) * FSI_MLP_IN * n, cudaMemcpyHostToDevice, m->st));
+    CK(launch_mlp_forward(m->P, m->nrm, m->X, m->Y, n, m->st));
+    CK(cudaMemcpyAsync(y, m->Y, sizeof(float) * FSI_MLP_OUT * n, cudaMemcpyDeviceToHost, m->st));
+    CK(cudaStreamSynchronize(m->st));
+    return FSI_OK;
+}
+
+int fsi_mlp_grad(fsi_mlp_t m, const float *x, const float *y, int n, float *grad, float *loss) {
+    if (!m || n <= 0 || !x || !y || !grad) return fail(FSI_E_ARG, "invalid argument");
+    if (!m->norm_set) return fail(FSI_E_STATE, "network statistics not set (fsi_mlp_set_norm)");
+    if (int rc = mlp_reserve(m, n)) return rc;
+    CK(cudaMemcpyAsync(m->X, x, sizeof(float) * FSI_MLP_IN * n, cudaMemcpyHostToDevice, m->st));
+    CK(cudaMemcpyAsync(m->Y, y, sizeof(float) * FSI_MLP_OUT * n, cudaMemcpyHostToDevice, m->st));
+    CK(cudaMemsetAsync(m->grad, 0, sizeof(float) * FSI_MLP_NPARAM, m->st));
+    CK(cudaMemsetAsync(m->loss, 0, sizeof(float), m->st));
+    CK(launch_mlp_grad(m->P, m->nrm, m->X, m->Y, nullptr, 0, n, n, m->grad, m->loss, m->st));
+    CK(cudaMemcpyAsync(grad, m->grad, sizeof(float) * FSI_MLP_NPARAM, cudaMemcpyDeviceToHost, m->st));
+    float l = 0.0f;
+    CK(cudaMemcpyAsync(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->st));
+    CK(cudaMemsetAsync(m->grad, 0, sizeof(float) * FSI_MLP_NPARAM, m->st));
+    CK(cudaStreamSynchronize(m->st));
+    if (loss) *loss = l;
+    return FSI_OK;
+}
+
+int fsi_mlp_train(fsi_mlp_t m, const float *x, const float *y, int n, int epochs, int batch, float lr,
+                  unsigned long long seed, float *loss_per_epoch) {
+    if (!m || n <= 0 || !x || !y || epochs <= 0 || batch <= 0 || !(lr > 0.0f))
+        return fail(FSI_E_ARG, "invalid argument");
+    if (!m->norm_set) return fail(FSI_E_STATE, "network statistics not set (fsi_mlp_set_norm)");
+    if (int rc = mlp_reserve(m, n)) return rc;
+    if (epochs > m->loss_cap) {
+        CK(cudaStreamSynchronize(m->st));
+        cudaFree(m->loss);
+        m->loss = nullptr;
+        m->loss_cap = 0;
+        CK(cudaMalloc((void **)&m->loss, sizeof(float) * epochs));
+        m->loss_cap = epochs;
+    }
+    batch = std::min(batch, n);
+    const int nbatch = (n + batch - 1) / batch;
+    CK(cudaMemcpyAsync(m->X, x, sizeof(float) * FSI_MLP_IN * n, cudaMemcpyHostToDevice, m->st));
+    CK(cudaMemcpyAsync(m->Y, y, sizeof(float) * FSI_MLP_OUT * n, cudaMemcpyHostToDevice, m->st));
+    CK(cudaMemsetAsync(m->loss, 0, sizeof(float) * epochs, m->st));
+    CK(cudaMemsetAsync(m->grad, 0, sizeof(float) * FSI_MLP_NPARAM, m->st));
+    for (int k = 0; k < 2; k++) CK(cudaEventRecord(m->ev[k], m->st));
+    // Sample orders alternate between two slots: the host refills a slot only
+    // after the copy of its previous use has run (the slot's event).
+    uint64_t r = seed;
+    for (int e = 0; e < epochs; e++) {
+        const int k = e & 1;
+        int *hp = m->hperm + (long long)k * m->cap, *dp = m->perm + (long long)k * m->cap;
+        CK(cudaEventSynchronize(m->ev[k]));
+        for (int i = 0; i < n; i++) hp[i] = i;
+        for (int i = n - 1; i > 0; i--) std::swap(hp[i], hp[(int)(splitmix64(r) % (uint64_t)(i + 1))]);
+        CK(cudaMemcpyAsync(dp, hp, sizeof(int) * n, cudaMemcpyHostToDevice, m->st));
+        for (int b = 0; b < nbatch; b++) {
+            const int b0 = b * batch, nb = std::min(batch, n - b0);
+            CK(launch_mlp_grad(m->P, m->nrm, m->X, m->Y, dp, b0, nb, nb, m->grad, m->loss + e, m->st));
+            CK(launch_mlp_adam(m->P, m->grad, m->m, m->v, lr, ++m->t, m->st));
+        }
+        CK(cudaEventRecord(m->ev[k], m->st));
+    }
+    std::vector<float> hl(epochs);
+    CK(cudaMemcpyAsync(hl.data(), m->loss, sizeof(float) * epochs, cudaMemcpyDeviceToHost, m->st));
+    CK(cudaStreamSynchronize(m->st));
+    if (loss_per_epoch)
+        for (int e = 0; e < epochs; e++) loss_per_epoch[e] = hl[e] / (float)nbatch;
+    return FSI_OK;
 }
 
 }  // extern "C"

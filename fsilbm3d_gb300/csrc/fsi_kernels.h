@@ -61,6 +61,11 @@ struct IbCoop {
     double *tol_acc;  // ntol sums
     int *status;
     double *res;
+    // learned warm start (all null: the reference's loop alone)
+    const float *mlp, *mlp_nrm;  // perceptron parameters and statistics, or null
+    const double *aux;           // (6,Mtot): acceleration, normal; or null
+    float *feat;                 // (12,Mtot) features out, or null
+    double Uref;
 };
 cudaError_t launch_ib_coop(const IbCoop &a, int prec, int grid, cudaStream_t st);
 int ib_coop_grid(int prec);  // co-resident CTAs (256 threads) on this device, 0 on error
@@ -91,5 +96,11 @@ cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, 
                               const double vf[3], cudaStream_t st);
 cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double *wu, const IbGeom &g, long long N,
                                   const double vf[3], cudaStream_t st);
+
+// ---- warm-start perceptron (k_mlp.cu) ----
+cudaError_t launch_mlp_forward(const float *P, const float *nrm, const float *X, float *Y, int n, cudaStream_t st);
+cudaError_t launch_mlp_grad(const float *P, const float *nrm, const float *X, const float *Y, const int *perm,
+                            long long b0, int nb, int batch_total, float *grad, float *loss, cudaStream_t st);
+cudaError_t launch_mlp_adam(float *P, float *grad, float *m, float *v, float lr, int step, cudaStream_t st);
 
 }  // namespace fsi

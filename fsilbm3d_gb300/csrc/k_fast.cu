@@ -21,6 +21,7 @@
 #include "bc_impl.cuh"
 #include "fsi_kernels.h"
 #include "ib_impl.cuh"
+#include "mlp_impl.cuh"
 #include "../../include/fsi_gpu.h"
 
 namespace fsi {
@@ -633,6 +634,77 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
     for (long long i = tid; i < a.ntol; i += nth) a.tol_acc[i] = 0.0;
     if (!gbar(a.status, nblk)) return;
     if (*(volatile int *)a.status & 3) return;
+
+    // learned warm start (no counterpart in the reference): features of every
+    // marker from the uncorrected window velocity; with a network, its
+    // predicted force becomes the first correction, applied to all bodies at
+    // once, and the penalty loop below continues from it
+    if (a.mlp || a.feat) {
+        const float iU = (float)(1.0 / a.Uref);
+        for (long long m = gw; m < a.Mtot; m += nw) {
+            const int16_t *s = a.ei + 12 * m;
+            const float *w = a.ew + 12 * m;
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+            for (int p = lane; p < 64; p += 32) {
+                const long long wc = ib_wcell(g, s, p);
+                const double wt = ib_weight(w, p);
+                v0 += __ldcg(a.wu + wc) * wt;
+                v1 += __ldcg(a.wu + wc + Nw) * wt;
+                v2 += __ldcg(a.wu + wc + 2 * Nw) * wt;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+                v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+                v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+            }
+            float x[MLP_IN];
+            x[0] = (float)(a.vel[3 * m] - v0) * iU;
+            x[1] = (float)(a.vel[3 * m + 1] - v1) * iU;
+            x[2] = (float)(a.vel[3 * m + 2] - v2) * iU;
+#pragma unroll
+            for (int k = 0; k < 3; k++) x[3 + k] = (float)a.vel[3 * m + k] * iU;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                x[6 + k] = a.aux ? (float)a.aux[6 * m + k] * iU : 0.0f;
+                x[9 + k] = a.aux ? (float)a.aux[6 * m + 3 + k] : 0.0f;
+            }
+            if (a.feat) {
+#pragma unroll
+                for (int k = 0; k < MLP_IN; k++)
+                    if (lane == k) a.feat[MLP_IN * m + k] = x[k];
+            }
+            if (a.mlp) {
+                float y[MLP_OUT];
+                mlp_forward_warp(a.mlp, a.mlp_nrm, x, lane, y);
+                if (lane == 0) {
+                    const double sc = a.area[m] * a.Uref;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        const double F = (double)y[k] * sc;
+                        a.eforce[3 * m + k] = F;
+                        a.fet[3 * m + k] = F * a.invh3p;
+                    }
+                }
+            }
+        }
+        if (a.mlp) {
+            if (!gbar(a.status, nblk)) return;
+            for (long long m = gw; m < a.Mtot; m += nw) {
+                const int16_t *s = a.ei + 12 * m;
+                const float *w = a.ew + 12 * m;
+                const double f0 = __ldcg(a.fet + 3 * m), f1 = __ldcg(a.fet + 3 * m + 1), f2 = __ldcg(a.fet + 3 * m + 2);
+                for (int p = lane; p < 64; p += 32) {
+                    const long long wc = ib_wcell(g, s, p);
+                    const double wt = ib_weight(w, p);
+                    atomicAdd(a.wu + wc, -(f0 * wt));
+                    atomicAdd(a.wu + wc + Nw, -(f1 * wt));
+                    atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
+                }
+            }
+            if (!gbar(a.status, nblk)) return;
+        }
+    }
 
     // the PenaltyForce_ loop, Solidbody.f90:893-906 (bodies one after another)
     int it = 0;

@@ -137,6 +137,59 @@ int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew);
 /* the IB window of the last fsi_ib_solve (0-based inclusive x0,x1,y0,y1,z0,z1) */
 int fsi_ib_get_window(fsi_block_t h, int box[6]);
 
+/* Learned warm start of the penalty loop. No counterpart in the reference:
+ * its loop (Solidbody.f90:893-906) starts every time step from v_Eforce = 0.
+ * A 12 -> 64 -> 64 -> 3 perceptron (tanh hidden layers, FP32) maps the
+ * features of one marker to its converged Lagrangian force; the prediction
+ * is applied as a first velocity correction and the unchanged loop then runs
+ * to the same ntol/dtol test, so the warm start changes how many iterations
+ * are needed, not the stopping rule.
+ *
+ * Features of marker m, in this order (velocities divided by Uref):
+ *   0-2  U_body - u_interp of the uncorrected field
+ *   3-5  U_body
+ *   6-8  body acceleration (aux), divided by Uref
+ *   9-11 surface normal (aux)
+ * Target: the converged v_Eforce of the marker divided by (area * Uref).
+ * Inputs are standardised with (x - mean)/std and outputs de-standardised,
+ * from FSI_MLP_NNORM statistics: mean_in[12], std_in[12], mean_out[3],
+ * std_out[3]. Parameters, one FP32 array of FSI_MLP_NPARAM: W1[64][12],
+ * b1[64], W2[64][64], b2[64], W3[3][64], b3[3] (row = output unit). */
+#define FSI_MLP_IN     12
+#define FSI_MLP_OUT    3
+#define FSI_MLP_NPARAM 5187
+#define FSI_MLP_NNORM  30
+typedef struct fsi_mlp *fsi_mlp_t;
+/* Glorot-uniform weights from seed, zero biases, identity statistics, on the
+ * current device */
+int fsi_mlp_create(fsi_mlp_t *out, unsigned long long seed);
+int fsi_mlp_destroy(fsi_mlp_t m);
+/* n must be FSI_MLP_NPARAM; set_params also clears the Adam moments */
+int fsi_mlp_set_params(fsi_mlp_t m, const float *params, int n);
+int fsi_mlp_get_params(fsi_mlp_t m, float *params, int n);
+/* the FSI_MLP_NNORM statistics; deviations must be positive */
+int fsi_mlp_set_norm(fsi_mlp_t m, const float *norm);
+/* y (3,n) = network(x (12,n)), de-standardised */
+int fsi_mlp_forward(fsi_mlp_t m, const float *x, int n, float *y);
+/* gradient (FSI_MLP_NPARAM) and value of the loss
+ * L = sum over the n samples and 3 outputs of (yn - tn)^2 / (3n),
+ * yn and tn the standardised prediction and target */
+int fsi_mlp_grad(fsi_mlp_t m, const float *x, const float *y, int n, float *grad, float *loss);
+/* epochs of Adam (beta 0.9/0.999, eps 1e-8) over shuffled mini-batches of
+ * batch samples; loss_per_epoch (epochs, may be NULL) receives the mean
+ * mini-batch loss of each epoch. The Adam moments persist across calls. */
+int fsi_mlp_train(fsi_mlp_t m, const float *x, const float *y, int n, int epochs, int batch, float lr,
+                  unsigned long long seed, float *loss_per_epoch);
+/* fsi_ib_solve for the fast forms (FSI_PREC_F64 returns FSI_E_ARG) with
+ * aux (6,Mtot) = acceleration, normal per marker (NULL: zeros); warm (NULL:
+ * the reference's loop from zero force); features (12,Mtot) out (NULL: not
+ * written) -- with warm NULL and ntol large, the features and the returned
+ * eforce are a training pair. */
+int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const double *area,
+                      const double *aux, const double vf[3], double denIn, double dt, double Uref,
+                      int ntol, double dtol, fsi_mlp_t warm, float *features, double *eforce,
+                      int *iters, double *residual);
+
 /* Block refinement, LBMBlockComm.f90:340-979. A pair links a father and a
  * son block; the son's faces with code 0 (BCfluid) receive father data. */
 typedef struct fsi_pair *fsi_pair_t;
