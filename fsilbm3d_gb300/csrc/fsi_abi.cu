@@ -64,27 +64,8 @@ size_t elem_size(int prec) {
 void build_mrt(double omega, double *mc, double *mf) {
     const int Q_ = 19;
     double M[19][19], Mi[19][19], D[19], T[19][19];
-    for (int i = 0; i < Q_; i++) {
-        double ex = ex_(i), ey = ey_(i), ez = ez_(i);
-        double e2 = ex * ex + ey * ey + ez * ez;
-        M[0][i] = 1.0;
-        M[1][i] = 19.0 * e2 - 30.0;
-        M[2][i] = (21.0 * e2 * e2 - 53.0 * e2 + 24.0) / 2.0;
-        M[3][i] = ex; M[5][i] = ey; M[7][i] = ez;
-        M[4][i] = (5.0 * e2 - 9.0) * ex;
-        M[6][i] = (5.0 * e2 - 9.0) * ey;
-        M[8][i] = (5.0 * e2 - 9.0) * ez;
-        M[9][i] = 3.0 * ex * ex - e2;
-        M[10][i] = (3.0 * e2 - 5.0) * (3.0 * ex * ex - e2);
-        M[11][i] = ey * ey - ez * ez;
-        M[12][i] = (3.0 * e2 - 5.0) * (ey * ey - ez * ez);
-        M[13][i] = ex * ey;
-        M[14][i] = ey * ez;
-        M[15][i] = ez * ex;
-        M[16][i] = (ey * ey - ez * ez) * ex;
-        M[17][i] = (ez * ez - ex * ex) * ey;
-        M[18][i] = (ex * ex - ey * ey) * ez;
-    }
+    for (int k = 0; k < Q_; k++)
+        for (int i = 0; i < Q_; i++) M[k][i] = (double)mrow_(k, i);
     for (int r = 0; r < Q_; r++) {
         double s = 0.0;
         for (int k = 0; k < Q_; k++) s += M[r][k] * M[r][k];
@@ -103,6 +84,41 @@ void build_mrt(double omega, double *mc, double *mf) {
             mc[r + Q_ * c] = s;
             mf[r + Q_ * c] = (r == c ? 1.0 : 0.0) - 0.5 * s;
         }
+}
+
+// The moment form of a given M_COLLID/M_FORCE pair: S = M M_COLLID M^-1 must
+// be diagonal with zeros on the conserved moments, and M_FORCE = I - M_COLLID/2.
+void mrt_moment_form(MrtMats &m) {
+    const int Q_ = 19;
+    double M[19][19], D[19], T[19][19];
+    for (int k = 0; k < Q_; k++) {
+        D[k] = 0.0;
+        for (int i = 0; i < Q_; i++) {
+            M[k][i] = (double)mrow_(k, i);
+            D[k] += M[k][i] * M[k][i];
+        }
+    }
+    for (int k = 0; k < Q_; k++)
+        for (int c = 0; c < Q_; c++) {
+            double s = 0.0;
+            for (int i = 0; i < Q_; i++) s += M[k][i] * m.mc[i + Q_ * c];
+            T[k][c] = s;
+        }
+    bool ok = true;
+    for (int k = 0; k < Q_ && ok; k++)
+        for (int l = 0; l < Q_; l++) {
+            double s = 0.0;
+            for (int c = 0; c < Q_; c++) s += T[k][c] * M[l][c] / D[l];
+            if (k == l) m.sd[k] = s / D[k];
+            else if (std::fabs(s) > 1e-9) { ok = false; break; }
+        }
+    for (int k : {0, 3, 5, 7})
+        if (std::fabs(m.sd[k]) > 1e-12) ok = false;
+    for (int i = 0; i < Q_ * Q_ && ok; i++) {
+        const double id = (i % Q_ == i / Q_) ? 1.0 : 0.0;
+        if (std::fabs(m.mf[i] - (id - 0.5 * m.mc[i])) > 1e-12) ok = false;
+    }
+    m.diag = ok ? 1 : 0;
 }
 
 }  // namespace
@@ -352,6 +368,7 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     } else {
         build_mrt(h->omega, h->mm.mc, h->mm.mf);
     }
+    mrt_moment_form(h->mm);
     h->prec = d->precision;
     h->esz = elem_size(h->prec);
     size_t fbytes = h->esz * 19 * (size_t)h->N;
@@ -372,16 +389,20 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
             int A, B;
             face_dims(h, k, A, B);
             chk(cudaMalloc((void **)&h->hw[k], sizeof(double) * 19 * (size_t)A * B));
-            if (e == cudaSuccess) chk(cudaMemset(h->hw[k], 0, sizeof(double) * 19 * (size_t)A * B));
+            if (e == cudaSuccess) chk(cudaMemsetAsync(h->hw[k], 0, sizeof(double) * 19 * (size_t)A * B, h->st));
         }
     }
     chk(cudaHostAlloc((void **)&h->h_tol, sizeof(double) * 64, cudaHostAllocDefault));
     chk(cudaHostAlloc((void **)&h->h_err, sizeof(int), cudaHostAllocDefault));
     chk(cudaMalloc((void **)&h->d_err, sizeof(int)));
-    if (e == cudaSuccess) chk(cudaMemset(h->den, 0, sizeof(double) * h->N));
-    if (e == cudaSuccess) chk(cudaMemset(h->u, 0, sizeof(double) * 3 * h->N));
-    if (e == cudaSuccess) chk(cudaMemset(h->fa, 0, fbytes));
-    if (e == cudaSuccess) chk(cudaMemset(h->fb, 0, fbytes));
+    // every device operation of a block goes to its own (non-blocking)
+    // stream: work on the legacy default stream would not be ordered with it
+    if (e == cudaSuccess) chk(cudaMemsetAsync(h->den, 0, sizeof(double) * h->N, h->st));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(h->u, 0, sizeof(double) * 3 * h->N, h->st));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(h->fa, 0, fbytes, h->st));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(h->fb, 0, fbytes, h->st));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
+    if (e == cudaSuccess) chk(cudaStreamSynchronize(h->st));
     if (e != cudaSuccess) {
         free_block(h);
         return fail(FSI_E_CUDA, "block allocation: %s", cudaGetErrorString(e));
@@ -557,7 +578,8 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     CK(cudaMalloc((void **)&h->d_tol, sizeof(double) * 64));
     CK(cudaMalloc((void **)&h->d_ei, sizeof(int16_t) * 12 * Mt));
     CK(cudaMalloc((void **)&h->d_ew, sizeof(float) * 12 * Mt));
-    CK(cudaMemcpy(h->d_offs, h->offs.data(), sizeof(int) * (nbodies + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(h->d_offs, h->offs.data(), sizeof(int) * (nbodies + 1), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return FSI_OK;
 }
 
@@ -812,8 +834,9 @@ int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const
 int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew) {
     if (!h) return fail(FSI_E_ARG, "null handle");
     if (h->Mtot == 0) return FSI_OK;
-    if (ei) CK(cudaMemcpy(ei, h->d_ei, sizeof(int16_t) * 12 * h->Mtot, cudaMemcpyDeviceToHost));
-    if (ew) CK(cudaMemcpy(ew, h->d_ew, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost));
+    if (ei) CK(cudaMemcpyAsync(ei, h->d_ei, sizeof(int16_t) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
+    if (ew) CK(cudaMemcpyAsync(ew, h->d_ew, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return FSI_OK;
 }
 
@@ -876,7 +899,8 @@ int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme)
     }
     p->scr_cells = (long long)maxS;
     if (e == cudaSuccess) e = cudaMalloc((void **)&p->d_err, sizeof(int) * 4);
-    if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int) * 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->d_err, 0, sizeof(int) * 4, fa->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(fa->st);
     if (e != cudaSuccess) {
         fsi_pair_destroy(p);
         return fail(FSI_E_CUDA, "pair allocation: %s", cudaGetErrorString(e));
@@ -905,9 +929,12 @@ namespace {
 // reads and clears the pair's error word after its stream has drained
 int pair_check(fsi_pair *p) {
     int h[3] = {0, 0, 0};
-    CK(cudaMemcpy(h, p->d_err, sizeof(int) * 3, cudaMemcpyDeviceToHost));
+    cudaStream_t st = p->fa->st;
+    CK(cudaMemcpyAsync(h, p->d_err, sizeof(int) * 3, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     if (h[0] == 0) return FSI_OK;
-    CK(cudaMemset(p->d_err, 0, sizeof(int) * 4));
+    CK(cudaMemsetAsync(p->d_err, 0, sizeof(int) * 4, st));
+    CK(cudaStreamSynchronize(st));
     long long idx = (long long)(unsigned)h[1] | ((long long)h[2] << 32);
     static const char *what[] = {"", "interpolation source", "interpolation target", "son face cell",
                                  "father face cell", "son cell", "father cell"};
@@ -1035,11 +1062,11 @@ int mlp_create(fsi_mlp *m, unsigned long long seed) {
         const double lim = std::sqrt(6.0 / (fan[l][0] + fan[l][1]));
         for (int i = 0; i < fan[l][0] * fan[l][1]; i++) P[w0[l] + i] = (float)((2.0 * unit_uniform(r) - 1.0) * lim);
     }
-    CK(cudaMemcpy(m->P, P.data(), sizeof(float) * FSI_MLP_NPARAM, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(m->P, P.data(), sizeof(float) * FSI_MLP_NPARAM, cudaMemcpyHostToDevice, m->st));
     std::vector<float> nrm(FSI_MLP_NNORM, 0.0f);
     for (int k = 0; k < FSI_MLP_IN; k++) nrm[FSI_MLP_IN + k] = 1.0f;
     for (int c = 0; c < FSI_MLP_OUT; c++) nrm[2 * FSI_MLP_IN + FSI_MLP_OUT + c] = 1.0f;
-    CK(cudaMemcpy(m->nrm, nrm.data(), sizeof(float) * FSI_MLP_NNORM, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(m->nrm, nrm.data(), sizeof(float) * FSI_MLP_NNORM, cudaMemcpyHostToDevice, m->st));
     if (int rc = mlp_reset_adam(m)) return rc;
     CK(cudaStreamSynchronize(m->st));
     return FSI_OK;

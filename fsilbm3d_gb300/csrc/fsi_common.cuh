@@ -47,6 +47,29 @@ __host__ __device__ constexpr int inc_(int k, int j) {
 // (the incoming set of the opposite face, in the same order)
 __host__ __device__ constexpr int mir_(int k, int j) { return inc_(k ^ 1, j); }
 
+// The moment basis of calculate_MRT_params (FluidDomain.f90:466-522): row k
+// of M at velocity i. Every entry is an integer.
+__host__ __device__ constexpr int mrow_(int k, int i) {
+    const int x = ex_(i), y = ey_(i), z = ez_(i);
+    const int e2 = x * x + y * y + z * z;
+    return k == 0 ? 1
+         : k == 1 ? 19 * e2 - 30
+         : k == 2 ? (21 * e2 * e2 - 53 * e2 + 24) / 2
+         : k == 3 ? x : k == 4 ? (5 * e2 - 9) * x
+         : k == 5 ? y : k == 6 ? (5 * e2 - 9) * y
+         : k == 7 ? z : k == 8 ? (5 * e2 - 9) * z
+         : k == 9 ? 3 * x * x - e2
+         : k == 10 ? (3 * e2 - 5) * (3 * x * x - e2)
+         : k == 11 ? y * y - z * z
+         : k == 12 ? (3 * e2 - 5) * (y * y - z * z)
+         : k == 13 ? x * y : k == 14 ? y * z : k == 15 ? z * x
+         : k == 16 ? (y * y - z * z) * x
+         : k == 17 ? (z * z - x * x) * y
+         : (x * x - y * y) * z;
+}
+// rows odd in e: opposite velocities carry opposite entries
+__host__ __device__ constexpr bool modd_(int k) { return (k >= 3 && k <= 8) || k >= 16; }
+
 // boundary codes, ConstParams.f90:31-34
 enum : int {
     BC_EQ = 101, BC_NEQ = 102, BC_EXT1 = 103, BC_EXT2 = 104,
@@ -78,6 +101,11 @@ struct Win {
 struct MrtMats {
     double mc[361];       // M_COLLID, column-major
     double mf[361];       // M_FORCE
+    // M_COLLID = M^-1 S M with S diagonal, zero on the conserved moments
+    // 0, 3, 5, 7, and M_FORCE = I - M_COLLID/2: then sd[k] = S_k / |row k|^2
+    // and the moment-space kernels apply the collision; else diag = 0
+    int diag;
+    double sd[19];
 };
 
 struct StepArgs {

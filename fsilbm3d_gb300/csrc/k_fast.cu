@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
 
 // ---------------------------------------------------------------------------
 // Paired-cell form of the step for the offset storage forms (FP32, FP16,
-// BF16) on blocks without IB window, half-way faces or 102 faces: each thread
+// BF16), SRT or MRT, with or without the IB window and face hooks: each thread
 // owns the two z-adjacent cells (z0, z0+1), z0 even. Loads and stores move
 // both cells in one 32-bit (FP16/BF16) or 64-bit (FP32) access and all
 // arithmetic runs on packed FP32x2 (fma.rn.f32x2, sm_100 and later), so one
@@ -331,7 +331,6 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 neg2(float2 a) { return __fmul2_rn(a, f2(-1.0f)); }
-__device__ __forceinline__ float2 sel2(int e, float2 v) { return e > 0 ? v : neg2(v); }
 
 template <int P> struct V2;
 template <> struct V2<FSI_PREC_F32> {
@@ -365,8 +364,43 @@ __host__ __device__ constexpr int zslot_(int i) {
          : i == 15 ? 6 : i == 16 ? 7 : i == 17 ? 8 : i == 18 ? 9 : -1;
 }
 
-template <int P, bool FORCED>
-__global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc) {
+// moment-space MRT: S_k / |row k|^2 for every moment (zero on conserved ones)
+struct MrtS { float sd[Q]; };
+
+// accumulator of integer-weighted terms; the weights are compile-time
+// constants after unrolling, so zero terms vanish and +-1 become add/sub
+struct Acc2 {
+    float2 v;
+    bool set;
+};
+__device__ __forceinline__ void acc_add(Acc2 &a, int c, float2 x) {
+    if (c == 0) return;
+    if (!a.set) {
+        a.v = c == 1 ? x : (c == -1 ? neg2(x) : mul2(f2((float)c), x));
+        a.set = true;
+    } else {
+        a.v = c == 1 ? add2(a.v, x) : (c == -1 ? sub2(a.v, x) : fma2(f2((float)c), x, a.v));
+    }
+}
+__device__ __forceinline__ float2 acc_val(const Acc2 &a) { return a.set ? a.v : f2(0.0f); }
+
+__device__ __forceinline__ float2 edot(int i, float2 v0, float2 v1, float2 v2) {
+    Acc2 a{f2(0.0f), false};
+    acc_add(a, ex_(i), v0);
+    acc_add(a, ey_(i), v1);
+    acc_add(a, ez_(i), v2);
+    return acc_val(a);
+}
+
+__device__ __forceinline__ void setl(float2 &v, int l, float s) {
+    if (l == 0) v.x = s;
+    else v.y = s;
+}
+__device__ __forceinline__ float getl(float2 v, int l) { return l == 0 ? v.x : v.y; }
+
+template <int P, int MODEL, bool FORCED, bool HOOKS>
+__global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
+    static_assert(!HOOKS || FORCED, "window cells carry their own force");
     using V = V2<P>;
     using S2 = typename V::S2;
     using S = typename V::S;
@@ -401,57 +435,182 @@ __global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Sca
         if (ey_(i)) jy = ey_(i) > 0 ? add2(jy, dk) : sub2(jy, dk);
         if (ez_(i)) jz = ez_(i) > 0 ? add2(jz, dk) : sub2(jz, dk);
     }
-    const float2 drho = s, rho = add2(f2(1.0f), s);
+    float2 drho = s, rho = add2(f2(1.0f), s);
     const float2 inv = make_float2(__fdividef(1.0f, rho.x), __fdividef(1.0f, rho.y));
     const float h = 0.5f * sc.dh;
-    float2 u0, u1, u2;
+    float2 u0, u1, u2, F0 = f2(0.f), F1 = f2(0.f), F2 = f2(0.f);
     if (FORCED) {
-        u0 = mul2(add2(jx, f2(h * sc.vf[0])), inv);
-        u1 = mul2(add2(jy, f2(h * sc.vf[1])), inv);
-        u2 = mul2(add2(jz, f2(h * sc.vf[2])), inv);
+        F0 = f2(sc.vf[0]); F1 = f2(sc.vf[1]); F2 = f2(sc.vf[2]);
+        u0 = mul2(fma2(f2(h), F0, jx), inv);
+        u1 = mul2(fma2(f2(h), F1, jy), inv);
+        u2 = mul2(fma2(f2(h), F2, jz), inv);
     } else {
         u0 = mul2(jx, inv); u1 = mul2(jy, inv); u2 = mul2(jz, inv);
     }
+    if (HOOKS && active) {
+        // cells of the IB window take den/u/force from the IB stage
+        const Win &w = a.win;
+        if (x >= w.x0 && x <= w.x1 && y >= w.y0 && y <= w.y1) {
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                const int z = z0 + l;
+                if (z >= w.z0 && z <= w.z1) {
+                    const long long wc =
+                        (long long)(z - w.z0) + (long long)w.WZ * ((long long)(y - w.y0) + (long long)w.WY * (x - w.x0));
+                    const float d = (float)(w.den[wc] - 1.0);
+                    setl(drho, l, d);
+                    setl(rho, l, 1.0f + d);
+                    setl(u0, l, (float)w.u[wc]);
+                    setl(u1, l, (float)w.u[wc + w.n]);
+                    setl(u2, l, (float)w.u[wc + 2 * w.n]);
+                    setl(F0, l, (float)w.force[wc]);
+                    setl(F1, l, (float)w.force[wc + w.n]);
+                    setl(F2, l, (float)w.force[wc + 2 * w.n]);
+                }
+            }
+        }
+        // den/u on the layer-2 planes of 102 faces
+        const bool pxy = (a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2);
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            const int z = z0 + l;
+            if (pxy || (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2)) {
+                const long long cc = (long long)c + l;
+                a.den[cc] = 1.0 + (double)getl(drho, l);
+                a.u[cc] = getl(u0, l);
+                a.u[cc + a.N] = getl(u1, l);
+                a.u[cc + 2 * a.N] = getl(u2, l);
+            }
+        }
+    }
 
-    // SRT (FluidDomain.f90:1218-1227), Omega folded as in collide_srt_free
     const float om = sc.om;
     const float2 k15 = mul2(f2(1.5f), fma2(u0, u0, fma2(u1, u1, mul2(u2, u2))));
-    const float2 omc = f2(1.0f - om);
-    const float2 base = sub2(drho, mul2(rho, k15));
-    const float2 orho = mul2(f2(om), rho);
+    float2 uF = f2(0.f);
+    if (FORCED) uF = fma2(u0, F0, fma2(u1, F1, mul2(u2, F2)));
     const float w0 = (float)wt_(0), w1 = (float)wt_(1), w2 = (float)wt_(7);
-    const float2 ac0 = mul2(f2(om * w0), base);
-    const float2 ac1 = mul2(f2(om * w1), base), bc1 = mul2(f2(4.5f * w1), orho), cc1 = mul2(f2(3.0f * w1), orho);
-    const float2 ac2 = mul2(f2(om * w2), base), bc2 = mul2(f2(4.5f * w2), orho), cc2 = mul2(f2(3.0f * w2), orho);
-    float2 uF = f2(0.f), cf = f2(0.f);
-    if (FORCED) {
-        uF = fma2(u0, f2(sc.vf[0]), fma2(u1, f2(sc.vf[1]), mul2(u2, f2(sc.vf[2]))));
-        cf = f2((1.0f - 0.5f * om) * sc.dh3);
-    }
-    g[0] = fma2(omc, g[0], ac0);
-    if (FORCED) g[0] = sub2(g[0], mul2(mul2(cf, f2(w0)), uF));
+    if (MODEL == 1) {
+        // SRT (FluidDomain.f90:1218-1227), Omega folded as in collide_srt_free
+        const float2 omc = f2(1.0f - om);
+        const float2 base = sub2(drho, mul2(rho, k15));
+        const float2 orho = mul2(f2(om), rho);
+        const float2 ac0 = mul2(f2(om * w0), base);
+        const float2 ac1 = mul2(f2(om * w1), base), bc1 = mul2(f2(4.5f * w1), orho), cc1 = mul2(f2(3.0f * w1), orho);
+        const float2 ac2 = mul2(f2(om * w2), base), bc2 = mul2(f2(4.5f * w2), orho), cc2 = mul2(f2(3.0f * w2), orho);
+        const float cf = (1.0f - 0.5f * om) * sc.dh3;
+        g[0] = fma2(omc, g[0], ac0);
+        if (FORCED) g[0] = sub2(g[0], mul2(f2(cf * w0), uF));
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
-        const int i = pr_(k), o = opp_(i);
-        const bool cls1 = (i <= 6);
-        float2 eu = f2(0.f);
-        bool first = true;
-        if (ex_(i)) { eu = first ? sel2(ex_(i), u0) : (ex_(i) > 0 ? add2(eu, u0) : sub2(eu, u0)); first = false; }
-        if (ey_(i)) { eu = first ? sel2(ey_(i), u1) : (ey_(i) > 0 ? add2(eu, u1) : sub2(eu, u1)); first = false; }
-        if (ez_(i)) { eu = first ? sel2(ez_(i), u2) : (ez_(i) > 0 ? add2(eu, u2) : sub2(eu, u2)); first = false; }
-        const float2 Sm = fma2(cls1 ? bc1 : bc2, mul2(eu, eu), cls1 ? ac1 : ac2);
-        const float2 Am = mul2(cls1 ? cc1 : cc2, eu);
-        float2 ni = fma2(omc, g[i], add2(Sm, Am));
-        float2 no = fma2(omc, g[o], sub2(Sm, Am));
-        if (FORCED) {
-            const float eF0 = ex_(i) * sc.vf[0] + ey_(i) * sc.vf[1] + ez_(i) * sc.vf[2];
-            const float2 cw = mul2(cf, f2(cls1 ? w1 : w2));
-            const float2 Fs = mul2(cw, sub2(mul2(f2(3.0f * eF0), eu), uF)), Fa = mul2(cw, f2(eF0));
-            ni = add2(ni, add2(Fs, Fa));
-            no = add2(no, sub2(Fs, Fa));
+        for (int k = 0; k < 9; k++) {
+            const int i = pr_(k), o = opp_(i);
+            const bool cls1 = (i <= 6);
+            const float2 eu = edot(i, u0, u1, u2);
+            const float2 Sm = fma2(cls1 ? bc1 : bc2, mul2(eu, eu), cls1 ? ac1 : ac2);
+            const float2 Am = mul2(cls1 ? cc1 : cc2, eu);
+            float2 ni = fma2(omc, g[i], add2(Sm, Am));
+            float2 no = fma2(omc, g[o], sub2(Sm, Am));
+            if (FORCED) {
+                const float2 eF = edot(i, F0, F1, F2);
+                const float cw = cf * (cls1 ? w1 : w2);
+                const float2 Fs = mul2(f2(cw), sub2(mul2(f2(3.0f), mul2(eF, eu)), uF)), Fa = mul2(f2(cw), eF);
+                ni = add2(ni, add2(Fs, Fa));
+                no = add2(no, sub2(Fs, Fa));
+            }
+            g[i] = ni;
+            g[o] = no;
         }
-        g[i] = ni;
-        g[o] = no;
+    } else {
+        // MRT (FluidDomain.f90:1236-1238) in moment space:
+        //   g += M^-1 S M (feq - g - Flb/2) + Flb,
+        // which is M_COLLID (feq - g) + M_FORCE Flb for M_FORCE = I - M_COLLID/2.
+        // Opposite velocities are handled as sums (even moments) and
+        // differences (odd moments) of r = feq - g - Flb/2.
+        const float dh3 = sc.dh3;
+        float2 rs[9], rd[9];
+        const float2 r0 = FORCED ? sub2(fma2(f2(w0), sub2(drho, mul2(rho, k15)), mul2(f2(0.5f * dh3 * w0), uF)), g[0])
+                                 : sub2(mul2(f2(w0), sub2(drho, mul2(rho, k15))), g[0]);
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int i = pr_(k), o = opp_(i);
+            const float w = (float)wt_(i);
+            const float2 eu = edot(i, u0, u1, u2);
+            const float2 wr = mul2(f2(w), rho);
+            // (feq_i + feq_o) and (feq_i - feq_o)
+            const float2 fsum = mul2(f2(2.0f), fma2(f2(w), drho, mul2(wr, fma2(f2(4.5f), mul2(eu, eu), neg2(k15)))));
+            const float2 fdif = mul2(mul2(f2(6.0f), wr), eu);
+            float2 sm = sub2(fsum, add2(g[i], g[o]));
+            float2 dm = sub2(fdif, sub2(g[i], g[o]));
+            if (FORCED) {
+                // (Flb_i + Flb_o)/2 and (Flb_i - Flb_o)/2
+                const float2 eF = edot(i, F0, F1, F2);
+                sm = sub2(sm, mul2(f2(dh3 * w), sub2(mul2(f2(3.0f), mul2(eu, eF)), uF)));
+                dm = sub2(dm, mul2(f2(dh3 * w), eF));
+            }
+            rs[k] = sm;
+            rd[k] = dm;
+        }
+        // relaxed moments t_k = S_k/|row k|^2 (M r)_k
+        float2 t[Q];
+#pragma unroll
+        for (int m = 0; m < Q; m++) {
+            if (m == 0 || m == 3 || m == 5 || m == 7) { t[m] = f2(0.f); continue; }
+            Acc2 acc{f2(0.f), false};
+            if (!modd_(m)) acc_add(acc, mrow_(m, 0), r0);
+#pragma unroll
+            for (int k = 0; k < 9; k++) acc_add(acc, mrow_(m, pr_(k)), modd_(m) ? rd[k] : rs[k]);
+            t[m] = mul2(f2(ms.sd[m]), acc_val(acc));
+        }
+        // back to populations: Delta_i = sum_k M[k][i] t_k, split by parity
+        {
+            Acc2 e{f2(0.f), false};
+#pragma unroll
+            for (int m = 0; m < Q; m++)
+                if (!modd_(m) && m != 0) acc_add(e, mrow_(m, 0), t[m]);
+            float2 d0 = acc_val(e);
+            if (FORCED) d0 = sub2(d0, mul2(f2(dh3 * w0), uF));
+            g[0] = add2(g[0], d0);
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int i = pr_(k), o = opp_(i);
+            Acc2 e{f2(0.f), false}, d{f2(0.f), false};
+#pragma unroll
+            for (int m = 1; m < Q; m++) {
+                if (m == 3 || m == 5 || m == 7) continue;
+                if (modd_(m)) acc_add(d, mrow_(m, i), t[m]);
+                else acc_add(e, mrow_(m, i), t[m]);
+            }
+            float2 ev = acc_val(e), dv = acc_val(d);
+            if (FORCED) {
+                const float w = (float)wt_(i);
+                const float2 eu = edot(i, u0, u1, u2);
+                const float2 eF = edot(i, F0, F1, F2);
+                ev = add2(ev, mul2(f2(dh3 * w), sub2(mul2(f2(3.0f), mul2(eu, eF)), uF)));
+                dv = add2(dv, mul2(f2(dh3 * w), eF));
+            }
+            g[i] = add2(g[i], add2(ev, dv));
+            g[o] = add2(g[o], sub2(ev, dv));
+        }
+    }
+
+    if (HOOKS && active) {
+        // halfwayBCset_ (FluidDomain.f90:567-614): post-collision faces as FP64 f
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            const int z = z0 + l;
+            double *hp[6] = {(a.hw[0] && x == 0) ? a.hw[0] + (long long)Q * (z + (long long)Z * y) : nullptr,
+                             (a.hw[1] && x == X - 1) ? a.hw[1] + (long long)Q * (z + (long long)Z * y) : nullptr,
+                             (a.hw[2] && y == 0) ? a.hw[2] + (long long)Q * (z + (long long)Z * x) : nullptr,
+                             (a.hw[3] && y == Y - 1) ? a.hw[3] + (long long)Q * (z + (long long)Z * x) : nullptr,
+                             (a.hw[4] && z == 0) ? a.hw[4] + (long long)Q * (y + (long long)Y * x) : nullptr,
+                             (a.hw[5] && z == Z - 1) ? a.hw[5] + (long long)Q * (y + (long long)Y * x) : nullptr};
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (hp[k]) {
+#pragma unroll
+                    for (int i = 0; i < Q; i++) hp[k][i] = (double)getl(g[i], l) + wt_(i);
+                }
+        }
     }
 
     // stage the ten z-moving populations of this row in shared memory
@@ -484,8 +643,8 @@ __global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Sca
     }
 }
 
-template <int P>
-cudaError_t pair_launch(const StepArgs &a, cudaStream_t st) {
+template <int P, int MODEL>
+cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaStream_t st) {
     Offs<int> of{};
     const long long ZY = (long long)a.Z * a.Y;
     for (int i = 0; i < Q; i++) {
@@ -499,12 +658,16 @@ cudaError_t pair_launch(const StepArgs &a, cudaStream_t st) {
     sc.dh3 = 3.0f * (float)a.dh;
     for (int k = 0; k < 3; k++) sc.vf[k] = (float)a.vf[k];
     sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
+    MrtS ms{};
+    if (MODEL == 3)
+        for (int k = 0; k < Q; k++) ms.sd[k] = (float)mm->sd[k];
     const int tpr = a.Z / 2;
     const int R = std::max(1, 256 / tpr);
     dim3 blk(tpr, R), grd(1, (a.Y + R - 1) / R, a.X);
     size_t smem = (size_t)10 * R * a.Z * sizeof(typename V2<P>::S);
-    if (sc.forced) k_step_pair<P, true><<<grd, blk, smem, st>>>(a, of, sc);
-    else k_step_pair<P, false><<<grd, blk, smem, st>>>(a, of, sc);
+    if (hooks) k_step_pair<P, MODEL, true, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    else if (sc.forced) k_step_pair<P, MODEL, true, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    else k_step_pair<P, MODEL, false, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
     return cudaGetLastError();
 }
 
@@ -839,8 +1002,8 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     for (int k = 0; k < 6; k++) hooks = hooks || a.hw[k] != nullptr || a.l2[k] != 0;
     // 32-bit element indices while all 19 populations fit
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
-    if (P != FSI_PREC_F64_FAST && MODEL == 1 && !hooks && small && a.Z % 2 == 0 && a.Z <= 512)
-        return pair_launch<P == FSI_PREC_F64_FAST ? FSI_PREC_F32 : P>(a, st);
+    if (P != FSI_PREC_F64_FAST && (MODEL == 1 || mm->diag) && small && a.Z % 2 == 0 && a.Z <= 512)
+        return pair_launch<P == FSI_PREC_F64_FAST ? FSI_PREC_F32 : P, MODEL>(a, mm, hooks, st);
     if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
     return hooks ? step_launch<P, MODEL, true, long long>(a, m, st) : step_launch<P, MODEL, false, long long>(a, m, st);
 }

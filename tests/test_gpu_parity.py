@@ -49,6 +49,7 @@ BC_CASES = {
     "forced_channel": dict(bnd=(301, 301, 203, 203, 302, 302), volumeForceIn=(2e-5, 0.0, 1e-6),
                            volumeForceAmp=1e-5, volumeForceFreq=0.1, volumeForcePhi=15.0),
     "zfaces": dict(bnd=(301, 301, 302, 302, 102, 104), uvwIn=(0.0, 0.0, 0.03)),
+    "zhalfway": dict(bnd=(101, 104, 301, 301, 203, 204), uvwIn=(0.04, 0.0, 0.0), shearRateIn=(0.0, 0.0, 0.002)),
 }
 
 
@@ -141,9 +142,10 @@ def test_f64_fast_within_1e12(gpu_lib):
     assert _rel(fg, fo) < 1e-12
 
 
+@pytest.mark.parametrize("model", [1, 3])
 @pytest.mark.parametrize("prec,tol", [(F.PREC_F32, 2e-5), (F.PREC_F16, 5e-3), (F.PREC_BF16, 5e-2)])
-def test_mixed_velocity_error(gpu_lib, prec, tol):
-    c = Case((24, 20, 16), model=1, nu=0.02, precision=prec)
+def test_mixed_velocity_error(gpu_lib, prec, tol, model):
+    c = Case((24, 20, 16), model=model, nu=0.02, precision=prec)
     c.init_tgv(0.05)
     for s in range(20):
         c.step()
@@ -154,11 +156,12 @@ def test_mixed_velocity_error(gpu_lib, prec, tol):
     assert _rel(uuu, uo) < tol
 
 
+@pytest.mark.parametrize("model", [1, 3])
 @pytest.mark.parametrize("dims", [(14, 9, 22), (14, 9, 21), (7, 5, 64)])
 @pytest.mark.parametrize("prec,tol", [(F.PREC_F32, 2e-5), (F.PREC_F16, 5e-3), (F.PREC_BF16, 5e-2)])
-def test_mixed_forced_periodic(gpu_lib, dims, prec, tol):
+def test_mixed_forced_periodic(gpu_lib, dims, prec, tol, model):
     # even z extent: paired-cell kernel; odd: one cell per thread
-    c = Case(dims, model=1, nu=0.02, precision=prec, volumeForceIn=(3e-5, -1e-5, 2e-5))
+    c = Case(dims, model=model, nu=0.02, precision=prec, volumeForceIn=(3e-5, -1e-5, 2e-5))
     c.init_tgv(0.04)
     for s in range(12):
         c.step()
@@ -168,10 +171,29 @@ def test_mixed_forced_periodic(gpu_lib, dims, prec, tol):
     assert _rel(uuu, c.ob.u.reshape(uuu.shape)) < tol
 
 
+@pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("zdim", [20, 19])
+@pytest.mark.parametrize("prec,tol", [(F.PREC_F32, 1e-4), (F.PREC_F16, 5e-3), (F.PREC_BF16, 5e-2)])
+@pytest.mark.parametrize("name", ["neq_walls", "halfway", "zfaces", "zhalfway", "inflow_ext2"])
+def test_mixed_boundaries(gpu_lib, name, prec, tol, zdim, model):
+    # face hooks (half-way copies, 102 layer-2 planes) in both step kernels:
+    # even z extent -> paired cells, odd -> one cell per thread
+    c = Case((14, 11, zdim), model=model, nu=0.01, precision=prec, **BC_CASES[name])
+    c.init_equilibrium()
+    for s in range(8):
+        c.step()
+    c.ob.macro()
+    den, uuu = c.gb.calculate_macro_quantities()
+    uo = c.ob.u.reshape(uuu.shape)
+    assert _rel(uuu, uo) < tol
+    assert np.max(np.abs(den - c.ob.den.reshape(den.shape))) < tol
+
+
+@pytest.mark.parametrize("model", [1, 3])
 @pytest.mark.parametrize("prec", [F.PREC_F64_FAST, F.PREC_F32, F.PREC_F16])
-def test_mixed_ib_force(gpu_lib, prec):
+def test_mixed_ib_force(gpu_lib, prec, model):
     dims = (40, 24, 20)
-    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.0, 0.0), nu=0.02,
+    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), model=model, uvwIn=(0.05, 0.0, 0.0), nu=0.02,
              plates=[plate_in(dims, n=5, heave=1.0, freq=0.02)], ntol=4, dtol=1e-12, Uref=0.05,
              precision=prec)
     c.init_equilibrium()
@@ -266,3 +288,18 @@ def test_errors_are_status_codes(gpu_lib):
     # the context is still usable after the reported errors
     b.step(blktime=1.0)
     assert np.all(np.isfinite(b.download_f()))
+
+
+# ------------------------------------------------ stream ordering at scale
+
+@pytest.mark.parametrize("prec", [F.PREC_F64, F.PREC_F16])
+def test_large_block_initialise_is_ordered(gpu_lib, prec):
+    # creation zeroes multi-GB buffers; initialise must land after that on
+    # every block, including one created right after another was freed
+    for rep in range(2):
+        b = F.Block(256, 256, 192, precision=prec, uvwIn=(0.05, 0.01, 0.0), bndConds=(101, 104, 101, 101, 101, 101))
+        b.initialise(0.0)
+        den, uuu = b.calculate_macro_quantities()
+        assert np.all(den == den[0, 0, 0]) and abs(den[0, 0, 0] - 1.0) < 1e-3
+        assert np.allclose(uuu[0], 0.05, rtol=0, atol=1e-3) and np.allclose(uuu[1], 0.01, rtol=0, atol=1e-3)
+        b.close()
