@@ -1,14 +1,24 @@
-"""Throughput benchmark of the D3Q19 (+IB) time step on GB300.
+"""Throughput benchmark of the D3Q19+IB time step on GB300.
 
-Workload (the periodic throughput case of the reference's hot path): a
-Taylor-Green vortex on a 256^3 periodic D3Q19 block, SRT collision,
-tau = 0.6, u0 = 0.05, no body. One step = one fused collide+stream pass over
-all 16.8M cells. The headline form stores distributions as FP16 offsets
-f - w_i and collides in FP32; the line also reports the FP64 forms (the
-plain reference-order form and the regrouped one), FP32 and BF16 storage,
-each with its velocity error against the plain FP64 form after the same
-steps, and an immersed-boundary case (160x96x96 block with a 17x17-marker
-rigid plate in heave, FP64 plain vs FP16 mixed, with the force error).
+Headline workload (mixed-precision FSI): one 384x256x256 D3Q19 block at
+dh = L/32, Re = U L / nu = 1000 with U = 0.05, MRT collision, uniform inflow
+(face code 101) on x-, zero-gradient outflow (104) on x+, inflow-velocity
+faces (101) on y and z, and a 1L x 1L plate of 33 x 33 Lagrangian markers
+in heave, A = 0.3 L, f* = f L / U = 0.2. The plate's kinematics are
+prescribed (rigid heave): the flexible plate of that case needs the
+reference's host-side structural solver, which stays outside the GPU path.
+One step = the IB stage (markers host -> device, the penalty loop to
+ntol = 5 / dtol = 1e-4 in one cooperative launch, the Lagrangian force
+device -> host) + the fused collide/stream kernel + the face kernels.
+Distributions are stored as FP16 offsets f - w_i, collision runs in FP32,
+the Lagrangian force in FP64.
+
+Beside it on the same workload: the FP64 plain path (reference operation
+order) with the force-coefficient error of the mixed path against it, and
+the CPU restatement of the reference step (OpenMP, host cores) on a bounded
+sample. Then the periodic Taylor-Green 256^3 throughput forms (FP64 plain,
+FP64 regrouped, FP32, FP16, BF16 storage; SRT and MRT) and the 160x96x96
+plate case at dh = L/16.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -26,28 +36,36 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-GRID = (256, 256, 256)
+FSI_GRID = (384, 256, 256)
+FSI_NODES = 33
+U = 0.05
+RE = 1000.0
+NTOL, DTOL = 5, 1e-4
+BND = (101, 104, 101, 101, 101, 101)
+TGV_GRID = (256, 256, 256)
 TAU = 0.6
 U0 = 0.05
-IB_GRID = (160, 96, 96)
-PROFILE_FILE = os.path.join(ROOT, "profiles", "k_step_pair_f16_tgv256.md")
-METRIC = "D3Q19 MLUPS, TGV 256^3, 1 GB300 (FP16-offset storage, FP32 collide)"
+IB160_GRID = (160, 96, 96)
+PROFILE_FILE = os.path.join(ROOT, "profiles", "k_step_pair_f16_mrt_fsi384.md")
+METRIC = "D3Q19+IB MLUPS, 1 GB300: mixed (FP16-offset storage, FP32 MRT collide) vs FP64 plain"
+WORKLOAD = ("mixed-precision FSI: 384x256x256 D3Q19 MRT block, dh=L/32, Re=1000, U=0.05, "
+            "1Lx1L plate 33x33 markers, prescribed heave A=0.3L f*=0.2")
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--steps", type=int, default=1000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--no-ib", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--grid", type=int, default=256, help="cube edge (profiling runs use a smaller one)")
-    p.add_argument("--forms", default="f64,f64_fast,f32,bf16", help="forms timed besides the fp16 headline")
+    p.add_argument("--no-extra", action="store_true", help="skip the TGV forms and the 160x96x96 case")
+    p.add_argument("--f64-steps", type=int, default=24, help="steps of the FP64 plain comparison")
+    p.add_argument("--grid", default="384x256x256", help="headline grid (profiling runs use a smaller one)")
     a = p.parse_args()
-    global GRID
-    GRID = (a.grid, a.grid, a.grid)
+    global FSI_GRID
+    FSI_GRID = tuple(int(v) for v in a.grid.split("x"))
     return a
 
 
@@ -99,10 +117,11 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(0.3)
         except Exception:
             self.proc = None
 
@@ -137,6 +156,102 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def read_traffic():
+    """per-launch DRAM traffic of the dominant kernel from the committed ncu summary"""
+    try:
+        for ln in open(PROFILE_FILE):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------ FSI workload
+
+def fsi_setup():
+    from fsilbm3d_gb300.bodies import RigidPlate
+    X, Y, Z = FSI_GRID
+    L = FSI_NODES - 1          # cells per plate length
+    dh = 1.0 / L
+    nu = U * 1.0 / RE
+    le = (min(3.0, 0.25 * X * dh), 0.5 * Y * dh, 0.5 * Z * dh)  # leading edge, mid-span
+    plate = RigidPlate(n_chord=FSI_NODES, n_span=FSI_NODES, chord=1.0, span=1.0, le=le,
+                       heave_ampl=(0.0, 0.3, 0.0), freq=0.2 * U / 1.0)
+    return dh, nu, plate
+
+
+def fsi_block(F, prec, dh, nu, plate, model=3):
+    X, Y, Z = FSI_GRID
+    b = F.Block(X, Y, Z, dh=dh, bndConds=BND, iCollidModel=model, nu=nu, precision=prec, uvwIn=(U, 0, 0))
+    b.initialise(0.0)
+    b.set_boundary_conditions(0.0)
+    b.ib_set_bodies([plate.M])
+    return b
+
+
+def fsi_steps(b, plate, dh, t, n, forces=None):
+    """n time steps in the reference's order: IB stage, then the fluid step"""
+    from fsilbm3d_gb300.bodies import force_coefficients
+    its = 0
+    for _ in range(n):
+        xyz, vel, area = plate.markers(t)
+        ef, it, res = b.ib_solve(xyz, vel, area, denIn=1.0, dt=dh, Uref=U, ntol=NTOL, dtol=DTOL)
+        t += dh
+        b.step(blktime=t)
+        its += it
+        if forces is not None:
+            forces.append(force_coefficients(ef, 1.0, U, plate.area))
+    return t, its
+
+
+def n_face_kernels():
+    return sum(1 for c in BND if c not in (0, 1, 301))
+
+
+def cpu_fsi_sample(threads, nsteps=None, seconds=12.0):
+    """The CPU restatement of the reference step (OpenMP) on the headline
+    workload, FP64, SRT->MRT as configured; a bounded number of steps."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    X, Y, Z = FSI_GRID
+    dh, nu, plate = fsi_setup()
+    fl = O.make_flow(uvwIn=(U, 0, 0), nu=nu)
+    ob = O.Block(X, Y, Z, dh, (0.0, 0.0, 0.0), BND, 3, fl, with_tau=False)
+    ob.initialise(0.0)
+    ob.set_bc()
+    t = 0.0
+
+    def one(t):
+        xyz, vel, area = plate.markers(t)
+        t += dh
+        ob.b.blktime = t
+        ob.step([O.Body(xyz, vel, area)], Uref=U, ntol=NTOL, dtol=DTOL)
+        return t
+
+    t = one(t)  # warm-up
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        t = one(t)
+        n += 1
+        el = time.perf_counter() - t0
+        if (nsteps is not None and n >= nsteps) or (nsteps is None and el >= seconds):
+            break
+    return X * Y * Z * n / el / 1e6, n, el
+
+
+# ---------------------------------------------------- periodic TGV forms
+
 def tgv_f64(grid):
     """TGV initial distributions (FP64 feq of the TGV field), built on the host."""
     from fsilbm3d_gb300.d3q19 import E, WT
@@ -157,98 +272,83 @@ def tgv_f64(grid):
     return f
 
 
-def read_traffic():
-    """per-launch DRAM traffic of the dominant kernel from the committed ncu summary"""
-    try:
-        for ln in open(PROFILE_FILE):
-            if ln.startswith("traffic_bytes_per_launch:"):
-                return float(ln.split(":")[1])
-    except OSError:
-        pass
-    return None
-
-
-def peaks():
-    try:
-        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        return float(d["hbm_gbs"]), "measured"
-    except Exception:
-        return 6800.0, "fallback"
-
-
-def run_form(F, prec, f0, steps, warmup, nu):
-    X, Y, Z = GRID
-    b = F.Block(X, Y, Z, nu=nu, precision=prec)
-    b.upload_f(f0)
-    b.run(warmup)
-    b.upload_f(f0)
-    ms = b.run(steps)
-    den, uuu = b.calculate_macro_quantities()
-    return b, ms, uuu
-
-
-def cpu_reference_sample(threads, nsteps=None, seconds=12.0):
-    """The CPU restatement of the reference step on the host cores (OpenMP)."""
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    X, Y, Z = GRID
-    fl = O.make_flow(nu=(TAU - 0.5) / 3.0)
-    b = O.Block(X, Y, Z, 1.0, (0, 0, 0), [301] * 6, 1, fl, with_tau=False)
-    b.init_tgv(U0)
-    b.step()  # warm-up
-    n = 0
-    t0 = time.perf_counter()
-    while True:
-        b.step()
-        n += 1
-        el = time.perf_counter() - t0
-        if (nsteps is not None and n >= nsteps) or (nsteps is None and el >= seconds):
-            break
-    mlups = X * Y * Z * n / el / 1e6
-    return mlups, n, el
-
-
-def ib_case(F, steps):
-    """160x96x96 block, 17x17 rigid plate in heave (dh = 1/16, Re = 200)."""
-    from fsilbm3d_gb300.bodies import RigidPlate, force_coefficients
-    X, Y, Z = IB_GRID
-    dh = 1.0 / 16.0
-    U = 0.05
-    nu = U * 1.0 / 200.0
-    plate = RigidPlate(n_chord=17, n_span=17, chord=1.0, span=1.0, le=(2.5, 3.0, 3.0),
-                       heave_ampl=(0.0, 0.5, 0.0), freq=0.25 * U / 1.0)
-    bnd = (101, 104, 101, 101, 101, 101)
+def tgv_forms(F, steps, pk):
+    X, Y, Z = TGV_GRID
+    N = X * Y * Z
+    nu = (TAU - 0.5) / 3.0
+    f0 = tgv_f64(TGV_GRID)
     out = {}
-    forces = {}
+    for model, mname in ((1, "srt"), (3, "mrt")):
+        ref_u = None
+        for name in ("f64", "f64_fast", "f32", "f16", "bf16"):
+            b = F.Block(X, Y, Z, nu=nu, precision=F.PRECISIONS[name], iCollidModel=model)
+            b.upload_f(f0)
+            b.run(3)
+            b.upload_f(f0)
+            n = steps if name != "f64" else max(4, steps // 4)
+            ms = b.run(n)
+            den, uuu = b.calculate_macro_quantities()
+            B = 2 * 19 * b.store_bytes
+            mlups = N * n / (ms * 1e-3) / 1e6
+            r = {"mlups": round(mlups, 1), "ms_per_step": ms / n, "steps": n,
+                 "algorithmic_gbs": round(mlups * B / 1e3, 1), "hbm_frac": round(mlups * B / 1e3 / pk, 4)}
+            if name == "f64":
+                ref_u, ref_n = uuu, n
+            elif n == ref_n:
+                r["u_max_rel_err_vs_f64"] = float(np.max(np.abs(uuu - ref_u)) / np.max(np.abs(ref_u)))
+            out["%s_%s" % (name, mname)] = r
+            b.close()
+        # the error of every form after the same steps as FP64 plain
+        for name in ("f64_fast", "f32", "f16", "bf16"):
+            key = "%s_%s" % (name, mname)
+            if "u_max_rel_err_vs_f64" in out[key]:
+                continue
+            b = F.Block(X, Y, Z, nu=nu, precision=F.PRECISIONS[name], iCollidModel=model)
+            b.upload_f(f0)
+            b.run(ref_n)
+            den, uuu = b.calculate_macro_quantities()
+            out[key]["u_max_rel_err_vs_f64"] = float(np.max(np.abs(uuu - ref_u)) / np.max(np.abs(ref_u)))
+            out[key]["err_after_steps"] = ref_n
+            b.close()
+    out["workload"] = "taylor-green vortex 256^3 periodic, tau=0.6, u0=0.05, inputs larger than L2"
+    return out
+
+
+def ib160_case(F, steps):
+    """160x96x96 block, 17x17-marker rigid plate in heave (dh = L/16, Re = 200)."""
+    from fsilbm3d_gb300.bodies import RigidPlate, force_coefficients
+    X, Y, Z = IB160_GRID
+    dh = 1.0 / 16.0
+    nu = U * 1.0 / 200.0
+    plate = RigidPlate(n_chord=17, n_span=17, chord=1.0, span=1.0, le=(2.5, 3.0, 2.5),
+                       heave_ampl=(0.0, 0.5, 0.0), freq=0.25 * U / 1.0)
+    out, forces = {}, {}
     for name, prec in (("f64", F.PREC_F64), ("f16", F.PREC_F16)):
-        b = F.Block(X, Y, Z, dh=dh, bndConds=bnd, iCollidModel=3, nu=nu, precision=prec, uvwIn=(U, 0, 0))
+        b = F.Block(X, Y, Z, dh=dh, bndConds=BND, iCollidModel=3, nu=nu, precision=prec, uvwIn=(U, 0, 0))
         b.initialise(0.0)
         b.set_boundary_conditions(0.0)
         b.ib_set_bodies([plate.M])
-        t = 0.0
-        its = []
-        hist = []
-        t0 = time.perf_counter()
+        t, hist = 0.0, []
+        b.timer_start()
         for s in range(steps):
+            xyz, vel, area = plate.markers(t)
+            ef, it, res = b.ib_solve(xyz, vel, area, denIn=1.0, dt=dh, Uref=U, ntol=NTOL, dtol=DTOL)
             t += dh
-            xyz, vel, area = plate.markers(t - dh)
-            ef, it, res = b.ib_solve(xyz, vel, area, denIn=1.0, dt=dh, Uref=U, ntol=5, dtol=1e-4)
             b.step(blktime=t)
-            its.append(it)
             hist.append(force_coefficients(ef, 1.0, U, plate.area))
-        el = time.perf_counter() - t0
+        ms = b.timer_stop()
         forces[name] = np.array(hist)
-        out[name] = {"mlups_e2e": X * Y * Z * steps / el / 1e6, "ms_per_step": el / steps * 1e3,
-                     "ib_iters_per_step": float(np.mean(its))}
+        out[name] = {"mlups": round(X * Y * Z * steps / (ms * 1e-3) / 1e6, 1), "ms_per_step": ms / steps}
         b.close()
     ref = forces["f64"]
-    err = np.max(np.abs(forces["f16"] - ref)) / max(np.max(np.abs(ref[:, :2])), 1e-30)
-    out["cl_cd_max_rel_err_f16_vs_f64"] = float(err)
+    err = np.max(np.abs(forces["f16"] - ref), axis=0) / np.maximum(np.max(np.abs(ref), axis=0), 1e-30)
+    out["cd_cl_max_rel_err_f16_vs_f64"] = [float(err[0]), float(err[1])]
     out["steps"] = steps
     out["workload"] = "160x96x96 MRT, dh=L/16, Re=200, 17x17-marker rigid plate heave A=0.5L f*=0.25"
     return out
 
+
+# ------------------------------------------------------------------ main
 
 def main():
     a = parse()
@@ -256,124 +356,142 @@ def main():
     if a.impl == "reference":
         return main_reference(a, rank, world, dist)
     import fsilbm3d_gb300 as F
-    if a.warmup < 3:
-        a.warmup = 3
-    X, Y, Z = GRID
+    a.warmup = max(a.warmup, 3)
+    X, Y, Z = FSI_GRID
     N = X * Y * Z
-    nu = (TAU - 0.5) / 3.0
-    f0 = tgv_f64(GRID)
     pk, pk_kind = peaks()
+    dh, nu, plate = fsi_setup()
 
-    # ---- the other forms, same steps, for the error against plain FP64
-    forms = {}
-    ref_u = None
-    for name in [x for x in a.forms.split(",") if x]:
-        prec = F.PRECISIONS[name]
-        b, ms, uuu = run_form(F, prec, f0, a.steps, a.warmup, nu)
-        B = 2 * 19 * b.store_bytes
-        mlups = N * a.steps / (ms * 1e-3) / 1e6
-        forms[name] = {"mlups": round(mlups, 1), "ms_per_step": ms / a.steps, "algorithmic_gbs": mlups * B / 1e3,
-                       "hbm_frac": mlups * B / 1e3 / pk}
-        if name == "f64":
-            ref_u = uuu
-        elif ref_u is not None:
-            forms[name]["u_max_rel_err_vs_f64"] = float(np.max(np.abs(uuu - ref_u)) / np.max(np.abs(ref_u)))
-        b.close()
-
-    # ---- headline: FP16-offset storage, timed K steps from a captured graph
-    b = F.Block(X, Y, Z, nu=nu, precision=F.PREC_F16)
-    b.upload_f(f0)
-    b.run(a.warmup)
-    b.upload_f(f0)
+    # ---- headline: mixed path, K steps timed on the block's stream
+    b = fsi_block(F, F.PREC_F16, dh, nu, plate)
+    t, _ = fsi_steps(b, plate, dh, 0.0, a.warmup)
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    barrier(dist)
-    b.run(0)  # device synchronised
     clocks.start()
-    ms = b.run(a.steps)
+    barrier(dist)
+    b.timer_start()
+    w0 = time.perf_counter()
+    t, its = fsi_steps(b, plate, dh, t, a.steps)
+    ms = b.timer_stop()
+    wall = time.perf_counter() - w0
     clk = clocks.stop()
     barrier(dist)
     ms = max_over_ranks(dist, ms)
-    den, uuu = b.calculate_macro_quantities()
-    mlups_rank = N * a.steps / (ms * 1e-3) / 1e6
     value = sum_over_ranks(dist, N * a.steps) / (ms * 1e-3) / 1e6
-    B = 2 * 19 * 2
-    achieved = N * B / (ms / a.steps * 1e-3) / 1e9
-    forms["f16"] = {"mlups": round(mlups_rank, 1), "ms_per_step": ms / a.steps, "algorithmic_gbs": achieved,
-                    "hbm_frac": achieved / pk}
-    if ref_u is not None:
-        forms["f16"]["u_max_rel_err_vs_f64"] = float(np.max(np.abs(uuu - ref_u)) / np.max(np.abs(ref_u)))
+    b.close()
 
-    # ---- end to end through the C-ABI with host buffers: pinned-host upload of
-    # the state, one ABI call per step, download of the state
+    # ---- the dominant kernel alone on the headline grid: the same step
+    # kernel on a periodic block (no face kernels), from a captured graph
+    kb = F.Block(X, Y, Z, dh=dh, iCollidModel=3, nu=nu, precision=F.PREC_F16, uvwIn=(U, 0, 0))
+    kb.initialise(0.0)
+    kb.run(4)
+    nk = max(20, min(a.steps, 200))
+    kms = kb.run(nk) / nk
+    kb.close()
+    B = 2 * 19 * 2
+    achieved = N * B / (kms * 1e-3) / 1e9
+
+    # ---- FP64 plain on the same workload, and the force error of the
+    # mixed path against it over the same steps from the same start
+    nf = max(4, a.f64_steps)
+    hist = {}
+    f64 = {}
+    for name, prec in (("f64", F.PREC_F64), ("f16", F.PREC_F16)):
+        bb = fsi_block(F, prec, dh, nu, plate)
+        hist[name] = []
+        bb.timer_start()
+        fsi_steps(bb, plate, dh, 0.0, nf, forces=hist[name])
+        tms = bb.timer_stop()
+        f64[name] = {"mlups": round(N * nf / (tms * 1e-3) / 1e6, 1), "ms_per_step": tms / nf}
+        bb.close()
+    c64, c16 = np.array(hist["f64"]), np.array(hist["f16"])
+    err = np.max(np.abs(c16 - c64), axis=0) / np.maximum(np.max(np.abs(c64), axis=0), 1e-30)
+    compare = {"steps": nf, "f64_plain_mlups": f64["f64"]["mlups"], "f64_plain_ms_per_step": f64["f64"]["ms_per_step"],
+               "f16_mlups_same_steps": f64["f16"]["mlups"],
+               "mixed_over_f64_plain": round(value / max(f64["f64"]["mlups"], 1e-9), 2),
+               "cd_max_rel_err": float(err[0]), "cl_max_rel_err": float(err[1]),
+               "cd_cl_last_f64": [float(c64[-1, 0]), float(c64[-1, 1])],
+               "cd_cl_last_f16": [float(c16[-1, 0]), float(c16[-1, 1])]}
+
+    # ---- end to end through the C-ABI with host buffers: the FP64 host fIn
+    # uploaded from pinned memory, K steps with the markers in and the force
+    # out every step, fIn downloaded
     e2e = None
     if not a.no_e2e:
         try:
             import torch
             host = torch.empty(19 * N, dtype=torch.float64).pin_memory().numpy().reshape(19, X, Y, Z)
-            host[...] = f0
         except Exception:
-            host = np.ascontiguousarray(f0)
+            host = np.empty((19, X, Y, Z))
+        b = fsi_block(F, F.PREC_F16, dh, nu, plate)
+        b.download_f(host)
         te0 = time.perf_counter()
         b.upload_f(host)
-        for s in range(a.steps):
-            b.step(blktime=(s + 1) * 1.0)
+        fsi_steps(b, plate, dh, 0.0, a.steps)
         b.download_f(host)
         te = time.perf_counter() - te0
+        b.close()
+        del host
+        M = plate.M
         e2e = {"value": round(N * a.steps / te / 1e6, 1), "unit": "MLUPS",
-               "h2d_bytes_per_step": int(19 * N * 8 / a.steps), "d2h_bytes_per_step": int(19 * N * 8 / a.steps),
-               "note": "C-ABI fsi_block_upload_f + K x fsi_block_step + fsi_block_download_f, FP64 host fIn"}
-    b.close()
+               "h2d_bytes_per_step": int((19 * N * 8 + a.steps * M * 7 * 8) / a.steps),
+               "d2h_bytes_per_step": int((19 * N * 8 + a.steps * M * 3 * 8) / a.steps),
+               "note": "C-ABI: fsi_block_upload_f (FP64 fIn, pinned host) + K x (fsi_ib_solve with host markers "
+                       "and force + fsi_block_step) + fsi_block_download_f"}
 
-    ib = None
-    if not a.no_ib and rank == 0:
-        ib = ib_case(F, max(20, min(a.steps, 100)))
+    extra = {}
+    if not a.no_extra and rank == 0:
+        extra["tgv256"] = tgv_forms(F, max(20, min(a.steps, 100)), pk)
+        extra["ib160"] = ib160_case(F, max(20, min(a.steps, 100)))
 
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:
         thr = os.cpu_count() or 1
-        mlups_cpu, n, el = cpu_reference_sample(thr, seconds=12.0)
+        mlups_cpu, n, el = cpu_fsi_sample(thr, seconds=12.0)
         cpu = {"value": round(mlups_cpu, 2), "unit": "MLUPS", "cores": thr, "kind": "port",
-               "sample": "oracle (C/OpenMP restatement of the reference step) on TGV 256^3, %d steps, %.1f s" % (n, el)}
+               "sample": "oracle (C/OpenMP restatement of the reference step, FP64 MRT + IB) on the headline "
+                         "workload, %d steps after one warm-up step, %.1f s" % (n, el)}
 
-    traffic = read_traffic()
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f16-offset storage / f32 arithmetic", "data": "synthetic (TGV initial field)",
-        "config": {"workload": "taylor-green vortex 256^3 periodic D3Q19 SRT tau=0.6 u0=0.05", "grid": list(GRID),
-                   "collision": "SRT/BGK", "storage": "fp16 f-w_i", "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (two 1.27 GB distribution buffers)"},
+        "vs_baseline": None, "dtype": "f16-offset storage / f32 arithmetic / f64 Lagrangian force",
+        "data": "synthetic (uniform inflow initial field, prescribed plate kinematics)",
+        "config": {"workload": WORKLOAD, "grid": list(FSI_GRID), "collision": "MRT", "storage": "fp16 f-w_i",
+                   "markers": plate.M, "ib": "ntol=%d dtol=%g" % (NTOL, DTOL), "ib_iterations_per_step":
+                   its / a.steps, "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (two 1.9 GB distribution buffers)",
+                   "wall_ms_per_step": wall / a.steps * 1e3},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk, "unit": "GB/s",
-                     "frac": round(achieved / pk, 4), "peak_kind": pk_kind,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": N * B,
-                     "kernel": "k_step_pair<FSI_PREC_F16,SRT>"},
+                     "frac": round(achieved / pk, 4), "peak_kind": pk_kind, "traffic": read_traffic(),
+                     "algorithmic_bytes_per_launch": N * B,
+                     "kernel": "k_step_pair<FSI_PREC_F16,MRT>", "kernel_ms": kms,
+                     "timing": "CUDA events around %d graph-launched steps of a periodic %dx%dx%d block" % ((nk,) + FSI_GRID)},
+        "vs_f64_plain": compare,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": a.steps,
+        "gpu_launches": a.steps * (2 + n_face_kernels()),
         "clocks": clk,
-        "forms": forms,
-        "ib_case": ib,
+        "extra": extra,
     }
     if rank == 0:
         print(json.dumps(line))
 
 
 def main_reference(a, rank, world, dist):
-    """Reference arm: the reference's CPU path (C/OpenMP restatement, no
-    Fortran compiler exists on these machines) on the host cores, same
-    workload, metric and unit; each step a full 256^3 reference step."""
+    """Reference arm: the reference's CPU path (the C/OpenMP restatement; no
+    Fortran compiler exists on these machines) on the host cores, on the
+    headline workload, metric and unit; a bounded number of full steps."""
     if rank != 0:
         return
     thr = os.cpu_count() or 1
-    # warm-up steps are part of the sample's first call; time a bounded sample
-    steps = max(1, min(a.steps, 20))
-    mlups, n, el = cpu_reference_sample(thr, nsteps=steps)
+    steps = max(1, min(a.steps, 8))
+    mlups, n, el = cpu_fsi_sample(thr, nsteps=steps)
     line = {"impl": "reference", "metric": METRIC, "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": world,
             "steps": n, "warmup": 1, "ms_per_step": el / n * 1e3, "higher_is_better": True,
-            "dtype": "f64", "data": "synthetic (TGV initial field)",
-            "config": {"workload": "taylor-green vortex 256^3 periodic D3Q19 SRT tau=0.6 u0=0.05", "grid": list(GRID)},
+            "dtype": "f64", "data": "synthetic (uniform inflow initial field, prescribed plate kinematics)",
+            "config": {"workload": WORKLOAD, "grid": list(FSI_GRID)},
             "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": thr, "kind": "port",
-                             "sample": "%d reference steps of TGV 256^3 (%.1f s)" % (n, el)},
+                             "sample": "%d reference steps (FP64 MRT + IB) of the headline workload (%.1f s)" % (n, el)},
             "e2e": {"value": round(mlups, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

@@ -55,7 +55,7 @@ SYMBOLS = [
     "fsi_ib_get_stencil", "fsi_ib_get_window", "fsi_pair_create", "fsi_pair_destroy", "fsi_pair_extract",
     "fsi_pair_father_to_son", "fsi_pair_son_to_father", "fsi_pair_father_to_son_static",
     "fsi_mlp_create", "fsi_mlp_destroy", "fsi_mlp_set_params", "fsi_mlp_get_params", "fsi_mlp_set_norm",
-    "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm",
+    "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_block_timer",
 ]
 # the warm-start perceptron (FSI_MLP_* in the header)
 MLP_IN, MLP_OUT, MLP_NPARAM, MLP_NNORM = 12, 3, 5187, 30
@@ -91,6 +91,7 @@ def load_library():
     L.fsi_block_macro.argtypes = [VP, DP, DP, DP]
     L.fsi_block_step.argtypes = [VP, DP, C.c_double]
     L.fsi_block_run.argtypes = [VP, DP, C.c_double, C.c_int, C.POINTER(C.c_float)]
+    L.fsi_block_timer.argtypes = [VP, C.c_int, C.POINTER(C.c_float)]
     L.fsi_ib_set_bodies.argtypes = [VP, C.c_int, IP, IP]
     L.fsi_ib_solve.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                DP, IP, DP]
@@ -257,7 +258,18 @@ class Block:
         _check(load_library().fsi_block_run(self.h, _dp(vf), blktime0, int(nsteps), C.byref(ms)))
         return ms.value
 
+    def timer_start(self):
+        """mark the start of a timed region on the block's stream"""
+        _check(load_library().fsi_block_timer(self.h, 0, None))
+
+    def timer_stop(self):
+        """device milliseconds since timer_start (waits for the stream)"""
+        ms = C.c_float()
+        _check(load_library().fsi_block_timer(self.h, 1, C.byref(ms)))
+        return ms.value
+
     # -- immersed boundary (Solidbody.f90) --
+
     def ib_set_bodies(self, M, bc=None):
         M = np.ascontiguousarray(M, dtype=np.int32)
         bcs = None if bc is None else np.ascontiguousarray(bc, dtype=np.int32)

@@ -491,8 +491,20 @@ int fsi_block_step(fsi_block_t h, const double vf[3], double blktime) {
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
     int rc = enqueue_step(h, vf, blktime, true);
     h->win_valid = false;
-    if (rc) return rc;
-    CK(cudaStreamSynchronize(h->st));
+    return rc;
+}
+
+int fsi_block_timer(fsi_block_t h, int stop, float *ms) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    if (!stop) {
+        CK(cudaEventRecord(h->ev0, h->st));
+        return FSI_OK;
+    }
+    CK(cudaEventRecord(h->ev1, h->st));
+    CK(cudaEventSynchronize(h->ev1));
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, h->ev0, h->ev1));
+    if (ms) *ms = t;
     return FSI_OK;
 }
 
@@ -697,7 +709,12 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     a.aux = wm.aux ? h->d_aux : nullptr;
     a.feat = wm.features ? h->d_feat : nullptr;
     a.Uref = Uref;
-    CK(launch_ib_coop(a, h->prec, h->coop_grid, h->st));
+    // one warp per marker in the penalty loop and a thread per window cell in
+    // the macro phase are all the parallelism there is; a smaller grid makes
+    // each of the grid barriers cheaper
+    long long need = std::max<long long>((h->Mtot + 7) / 8, (h->Nw + 255) / 256);
+    const int grid = (int)std::max<long long>(1, std::min<long long>(need, h->coop_grid));
+    CK(launch_ib_coop(a, h->prec, grid, h->st));
     CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
     if (wm.features)
         CK(cudaMemcpyAsync(wm.features, h->d_feat, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));

@@ -340,6 +340,8 @@ template <> struct V2<FSI_PREC_F32> {
     static __device__ __forceinline__ S lo(S2 s) { return s.x; }
     static __device__ __forceinline__ S hi(S2 s) { return s.y; }
     static __device__ __forceinline__ S2 pack(S a, S b) { return make_float2(a, b); }
+    static __device__ __forceinline__ float dec1(S s) { return s; }
+    static __device__ __forceinline__ S enc1(float c) { return c; }
 };
 template <> struct V2<FSI_PREC_F16> {
     using S2 = __half2; using S = __half;
@@ -348,6 +350,8 @@ template <> struct V2<FSI_PREC_F16> {
     static __device__ __forceinline__ S lo(S2 s) { return __low2half(s); }
     static __device__ __forceinline__ S hi(S2 s) { return __high2half(s); }
     static __device__ __forceinline__ S2 pack(S a, S b) { return __halves2half2(a, b); }
+    static __device__ __forceinline__ float dec1(S s) { return __half2float(s); }
+    static __device__ __forceinline__ S enc1(float c) { return __float2half_rn(c); }
 };
 template <> struct V2<FSI_PREC_BF16> {
     using S2 = __nv_bfloat162; using S = __nv_bfloat16;
@@ -356,6 +360,8 @@ template <> struct V2<FSI_PREC_BF16> {
     static __device__ __forceinline__ S lo(S2 s) { return __low2bfloat16(s); }
     static __device__ __forceinline__ S hi(S2 s) { return __high2bfloat16(s); }
     static __device__ __forceinline__ S2 pack(S a, S b) { return __halves2bfloat162(a, b); }
+    static __device__ __forceinline__ float dec1(S s) { return __bfloat162float(s); }
+    static __device__ __forceinline__ S enc1(float c) { return __float2bfloat16_rn(c); }
 };
 
 // index of z-moving population i among the ten with ez != 0
@@ -398,34 +404,11 @@ __device__ __forceinline__ void setl(float2 &v, int l, float s) {
 }
 __device__ __forceinline__ float getl(float2 v, int l) { return l == 0 ? v.x : v.y; }
 
-template <int P, int MODEL, bool FORCED, bool HOOKS>
-__global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
-    static_assert(!HOOKS || FORCED, "window cells carry their own force");
-    using V = V2<P>;
-    using S2 = typename V::S2;
-    using S = typename V::S;
-    extern __shared__ unsigned char smraw[];
-    const int Z = a.Z, Y = a.Y, X = a.X;
-    const int tz = threadIdx.x, ty = threadIdx.y, R = blockDim.y;
-    const int z0 = 2 * tz;
-    const int y = blockIdx.y * R + ty, x = blockIdx.z;
-    const bool active = (y < Y);
-    S *sm = (S *)smraw;  // [10][R][Z]
-    const int c = z0 + Z * ((active ? y : 0) + Y * x);
-    const int N = (int)a.N;
-
-    float2 g[Q];
-    if (active) {
-        const S *sp = (const S *)a.src + c;
-#pragma unroll
-        for (int i = 0; i < Q; i++) g[i] = V::dec(__ldcs((const S2 *)(sp + of.ld[i])));
-    } else {
-#pragma unroll
-        for (int i = 0; i < Q; i++) g[i] = f2(0.0f);
-    }
-
-    // macro (offsets: rho = 1 + sum g)
-    float2 s = g[0], jx = f2(0.f), jy = f2(0.f), jz = f2(0.f);
+// density offset, density and momentum of two cells (offsets: rho = 1 + sum g)
+__device__ __forceinline__ void macro2(const float2 g[Q], float2 &drho, float2 &rho, float2 &jx, float2 &jy,
+                                       float2 &jz) {
+    float2 s = g[0];
+    jx = f2(0.f); jy = f2(0.f); jz = f2(0.f);
 #pragma unroll
     for (int k = 0; k < 9; k++) {
         const int i = pr_(k), o = opp_(i);
@@ -435,62 +418,38 @@ __global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Sca
         if (ey_(i)) jy = ey_(i) > 0 ? add2(jy, dk) : sub2(jy, dk);
         if (ez_(i)) jz = ez_(i) > 0 ? add2(jz, dk) : sub2(jz, dk);
     }
-    float2 drho = s, rho = add2(f2(1.0f), s);
+    drho = s;
+    rho = add2(f2(1.0f), s);
+}
+
+// velocity with the half-force shift of Guo forcing (calculate_macro_quantities_)
+template <bool FORCED>
+__device__ __forceinline__ void vel2(float2 rho, float2 jx, float2 jy, float2 jz, float2 F0, float2 F1, float2 F2,
+                                     float h, float2 &u0, float2 &u1, float2 &u2) {
     const float2 inv = make_float2(__fdividef(1.0f, rho.x), __fdividef(1.0f, rho.y));
-    const float h = 0.5f * sc.dh;
-    float2 u0, u1, u2, F0 = f2(0.f), F1 = f2(0.f), F2 = f2(0.f);
     if (FORCED) {
-        F0 = f2(sc.vf[0]); F1 = f2(sc.vf[1]); F2 = f2(sc.vf[2]);
         u0 = mul2(fma2(f2(h), F0, jx), inv);
         u1 = mul2(fma2(f2(h), F1, jy), inv);
         u2 = mul2(fma2(f2(h), F2, jz), inv);
     } else {
         u0 = mul2(jx, inv); u1 = mul2(jy, inv); u2 = mul2(jz, inv);
     }
-    if (HOOKS && active) {
-        // cells of the IB window take den/u/force from the IB stage
-        const Win &w = a.win;
-        if (x >= w.x0 && x <= w.x1 && y >= w.y0 && y <= w.y1) {
-#pragma unroll
-            for (int l = 0; l < 2; l++) {
-                const int z = z0 + l;
-                if (z >= w.z0 && z <= w.z1) {
-                    const long long wc =
-                        (long long)(z - w.z0) + (long long)w.WZ * ((long long)(y - w.y0) + (long long)w.WY * (x - w.x0));
-                    const float d = (float)(w.den[wc] - 1.0);
-                    setl(drho, l, d);
-                    setl(rho, l, 1.0f + d);
-                    setl(u0, l, (float)w.u[wc]);
-                    setl(u1, l, (float)w.u[wc + w.n]);
-                    setl(u2, l, (float)w.u[wc + 2 * w.n]);
-                    setl(F0, l, (float)w.force[wc]);
-                    setl(F1, l, (float)w.force[wc + w.n]);
-                    setl(F2, l, (float)w.force[wc + 2 * w.n]);
-                }
-            }
-        }
-        // den/u on the layer-2 planes of 102 faces
-        const bool pxy = (a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2);
-#pragma unroll
-        for (int l = 0; l < 2; l++) {
-            const int z = z0 + l;
-            if (pxy || (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2)) {
-                const long long cc = (long long)c + l;
-                a.den[cc] = 1.0 + (double)getl(drho, l);
-                a.u[cc] = getl(u0, l);
-                a.u[cc + a.N] = getl(u1, l);
-                a.u[cc + 2 * a.N] = getl(u2, l);
-            }
-        }
-    }
+}
 
+// the collision of two cells (offset storage, FP32x2): SRT (FluidDomain.f90:
+// 1218-1227, Omega folded per weight class) or MRT (:1236-1238) in moment
+// space, g += M^-1 S M (feq - g - Flb/2) + Flb, which is M_COLLID (feq - g) +
+// M_FORCE Flb for M_FORCE = I - M_COLLID/2. Opposite velocities are handled
+// as sums (even moments) and differences (odd moments).
+template <int MODEL, bool FORCED>
+__device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1, float2 u2,
+                                         float2 F0, float2 F1, float2 F2, const Scal<float> &sc, const MrtS &ms) {
     const float om = sc.om;
     const float2 k15 = mul2(f2(1.5f), fma2(u0, u0, fma2(u1, u1, mul2(u2, u2))));
     float2 uF = f2(0.f);
     if (FORCED) uF = fma2(u0, F0, fma2(u1, F1, mul2(u2, F2)));
     const float w0 = (float)wt_(0), w1 = (float)wt_(1), w2 = (float)wt_(7);
     if (MODEL == 1) {
-        // SRT (FluidDomain.f90:1218-1227), Omega folded as in collide_srt_free
         const float2 omc = f2(1.0f - om);
         const float2 base = sub2(drho, mul2(rho, k15));
         const float2 orho = mul2(f2(om), rho);
@@ -520,11 +479,6 @@ __global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Sca
             g[o] = no;
         }
     } else {
-        // MRT (FluidDomain.f90:1236-1238) in moment space:
-        //   g += M^-1 S M (feq - g - Flb/2) + Flb,
-        // which is M_COLLID (feq - g) + M_FORCE Flb for M_FORCE = I - M_COLLID/2.
-        // Opposite velocities are handled as sums (even moments) and
-        // differences (odd moments) of r = feq - g - Flb/2.
         const float dh3 = sc.dh3;
         float2 rs[9], rd[9];
         const float2 r0 = FORCED ? sub2(fma2(f2(w0), sub2(drho, mul2(rho, k15)), mul2(f2(0.5f * dh3 * w0), uF)), g[0])
@@ -592,26 +546,41 @@ __global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Sca
             g[o] = add2(g[o], sub2(ev, dv));
         }
     }
+}
 
-    if (HOOKS && active) {
-        // halfwayBCset_ (FluidDomain.f90:567-614): post-collision faces as FP64 f
+// The bulk step: every cell takes den/u from its own distributions and the
+// uniform volume force vf. Cells of the IB window, half-way faces and 102
+// planes are then corrected by the small kernels below, which read the same
+// (unchanged) source buffer.
+template <int P, int MODEL, bool FORCED>
+__global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
+    using V = V2<P>;
+    using S2 = typename V::S2;
+    using S = typename V::S;
+    extern __shared__ unsigned char smraw[];
+    const int Z = a.Z, Y = a.Y, X = a.X;
+    const int tz = threadIdx.x, ty = threadIdx.y, R = blockDim.y;
+    const int z0 = 2 * tz;
+    const int y = blockIdx.y * R + ty, x = blockIdx.z;
+    const bool active = (y < Y);
+    S *sm = (S *)smraw;  // [10][R][Z]
+    const int c = z0 + Z * ((active ? y : 0) + Y * x);
+    const int N = (int)a.N;
+
+    float2 g[Q];
+    if (active) {
+        const S *sp = (const S *)a.src + c;
 #pragma unroll
-        for (int l = 0; l < 2; l++) {
-            const int z = z0 + l;
-            double *hp[6] = {(a.hw[0] && x == 0) ? a.hw[0] + (long long)Q * (z + (long long)Z * y) : nullptr,
-                             (a.hw[1] && x == X - 1) ? a.hw[1] + (long long)Q * (z + (long long)Z * y) : nullptr,
-                             (a.hw[2] && y == 0) ? a.hw[2] + (long long)Q * (z + (long long)Z * x) : nullptr,
-                             (a.hw[3] && y == Y - 1) ? a.hw[3] + (long long)Q * (z + (long long)Z * x) : nullptr,
-                             (a.hw[4] && z == 0) ? a.hw[4] + (long long)Q * (y + (long long)Y * x) : nullptr,
-                             (a.hw[5] && z == Z - 1) ? a.hw[5] + (long long)Q * (y + (long long)Y * x) : nullptr};
+        for (int i = 0; i < Q; i++) g[i] = V::dec(__ldcs((const S2 *)(sp + of.ld[i])));
+    } else {
 #pragma unroll
-            for (int k = 0; k < 6; k++)
-                if (hp[k]) {
-#pragma unroll
-                    for (int i = 0; i < Q; i++) hp[k][i] = (double)getl(g[i], l) + wt_(i);
-                }
-        }
+        for (int i = 0; i < Q; i++) g[i] = f2(0.0f);
     }
+    float2 drho, rho, jx, jy, jz, u0, u1, u2;
+    macro2(g, drho, rho, jx, jy, jz);
+    const float2 F0 = f2(sc.vf[0]), F1 = f2(sc.vf[1]), F2 = f2(sc.vf[2]);
+    vel2<FORCED>(rho, jx, jy, jz, F0, F1, F2, 0.5f * sc.dh, u0, u1, u2);
+    collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
 
     // stage the ten z-moving populations of this row in shared memory
     if (active) {
@@ -643,6 +612,141 @@ __global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Sca
     }
 }
 
+// cell (x, y, z) of window cell wc
+__device__ __forceinline__ void win_cell(const Win &w, long long wc, int &x, int &y, int &z) {
+    z = (int)(wc % w.WZ) + w.z0;
+    const long long t = wc / w.WZ;
+    y = (int)(t % w.WY) + w.y0;
+    x = (int)(t / w.WY) + w.x0;
+}
+
+// One cell of a two-cell lane group, for the fix-up kernels: the 19 source
+// populations, and the destination of each push with periodic wrap.
+template <int P>
+__device__ __forceinline__ void load_cell(const StepArgs &a, int x, int y, int z, float2 g[Q], int l) {
+    using V = V2<P>;
+    const typename V::S *src = (const typename V::S *)a.src;
+    const long long c = (long long)z + (long long)a.Z * ((long long)y + (long long)a.Y * x);
+#pragma unroll
+    for (int i = 0; i < Q; i++) setl(g[i], l, V::dec1(src[c + a.N * i]));
+}
+
+template <int P>
+__device__ __forceinline__ void push_cell(const StepArgs &a, int x, int y, int z, const float2 g[Q], int l) {
+    using V = V2<P>;
+    typename V::S *dst = (typename V::S *)a.dst;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        int xd = x + ex_(i), yd = y + ey_(i), zd = z + ez_(i);
+        xd = xd < 0 ? a.X - 1 : (xd == a.X ? 0 : xd);
+        yd = yd < 0 ? a.Y - 1 : (yd == a.Y ? 0 : yd);
+        zd = zd < 0 ? a.Z - 1 : (zd == a.Z ? 0 : zd);
+        const long long cd = (long long)zd + (long long)a.Z * ((long long)yd + (long long)a.Y * xd);
+        dst[cd + a.N * i] = V::enc1(getl(g[i], l));
+    }
+}
+
+// The IB window: its cells collide with the den/u/force of the IB stage and
+// push again, replacing what the bulk step pushed for them. Two window cells
+// per thread (any two: the lanes are independent).
+template <int P, int MODEL>
+__global__ void __launch_bounds__(128) k_win_fix(StepArgs a, Scal<float> sc, MrtS ms) {
+    const Win &w = a.win;
+    const long long w0 = 2 * (blockIdx.x * (long long)blockDim.x + threadIdx.x);
+    if (w0 >= w.n) return;
+    const bool two = w0 + 1 < w.n;
+    int x[2], y[2], z[2];
+    float2 g[Q], drho, rho, u0, u1, u2, F0, F1, F2;
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        const long long wc = (l == 1 && !two) ? w0 : w0 + l;
+        win_cell(w, wc, x[l], y[l], z[l]);
+        load_cell<P>(a, x[l], y[l], z[l], g, l);
+        const float d = (float)(w.den[wc] - 1.0);
+        setl(drho, l, d);
+        setl(rho, l, 1.0f + d);
+        setl(u0, l, (float)w.u[wc]);
+        setl(u1, l, (float)w.u[wc + w.n]);
+        setl(u2, l, (float)w.u[wc + 2 * w.n]);
+        setl(F0, l, (float)w.force[wc]);
+        setl(F1, l, (float)w.force[wc + w.n]);
+        setl(F2, l, (float)w.force[wc + 2 * w.n]);
+    }
+    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
+    push_cell<P>(a, x[0], y[0], z[0], g, 0);
+    if (two) push_cell<P>(a, x[1], y[1], z[1], g, 1);
+}
+
+// Face hooks of one face k: the post-collision FP64 copy of a half-way face
+// (halfwayBCset_, FluidDomain.f90:567-614) or den/u on the layer-2 plane of a
+// 102 face. Cells of the IB window use the window's den/u/force, as the
+// bulk and window kernels do. Two face cells per thread.
+template <int P, int MODEL>
+__global__ void __launch_bounds__(128) k_face_hook(StepArgs a, Scal<float> sc, MrtS ms, int k, int A, int B) {
+    const long long n = (long long)A * B;
+    const long long f0 = 2 * (blockIdx.x * (long long)blockDim.x + threadIdx.x);
+    if (f0 >= n) return;
+    const bool two = f0 + 1 < n;
+    const bool hw = a.hw[k] != nullptr;
+    const int ax = k >> 1;
+    // face cell (ia, ib): ia runs along z (x/y faces) or y (z faces)
+    int x[2], y[2], z[2];
+    float2 g[Q], drho, rho, jx, jy, jz, u0, u1, u2;
+    float2 F0 = f2(sc.vf[0]), F1 = f2(sc.vf[1]), F2 = f2(sc.vf[2]);
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        const long long fc = (l == 1 && !two) ? f0 : f0 + l;
+        const int ia = (int)(fc % A), ib = (int)(fc / A);
+        // the plane: the face itself (half-way copy) or layer 2 (102)
+        const int lay = hw ? ((k & 1) ? (ax == 0 ? a.X : ax == 1 ? a.Y : a.Z) - 1 : 0)
+                           : ((k & 1) ? (ax == 0 ? a.X : ax == 1 ? a.Y : a.Z) - 2 : 1);
+        if (ax == 0) { x[l] = lay; y[l] = ib; z[l] = ia; }
+        else if (ax == 1) { y[l] = lay; x[l] = ib; z[l] = ia; }
+        else { z[l] = lay; x[l] = ib; y[l] = ia; }
+        load_cell<P>(a, x[l], y[l], z[l], g, l);
+    }
+    macro2(g, drho, rho, jx, jy, jz);
+    vel2<true>(rho, jx, jy, jz, F0, F1, F2, 0.5f * sc.dh, u0, u1, u2);
+    const Win &w = a.win;
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        if (x[l] >= w.x0 && x[l] <= w.x1 && y[l] >= w.y0 && y[l] <= w.y1 && z[l] >= w.z0 && z[l] <= w.z1) {
+            const long long wc = (long long)(z[l] - w.z0) +
+                                 (long long)w.WZ * ((long long)(y[l] - w.y0) + (long long)w.WY * (x[l] - w.x0));
+            const float d = (float)(w.den[wc] - 1.0);
+            setl(drho, l, d);
+            setl(rho, l, 1.0f + d);
+            setl(u0, l, (float)w.u[wc]);
+            setl(u1, l, (float)w.u[wc + w.n]);
+            setl(u2, l, (float)w.u[wc + 2 * w.n]);
+            setl(F0, l, (float)w.force[wc]);
+            setl(F1, l, (float)w.force[wc + w.n]);
+            setl(F2, l, (float)w.force[wc + 2 * w.n]);
+        }
+    }
+    if (!hw) {
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            if (l == 1 && !two) break;
+            const long long c = (long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l]);
+            a.den[c] = 1.0 + (double)getl(drho, l);
+            a.u[c] = getl(u0, l);
+            a.u[c + a.N] = getl(u1, l);
+            a.u[c + 2 * a.N] = getl(u2, l);
+        }
+        return;
+    }
+    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        if (l == 1 && !two) break;
+        const long long fc = f0 + l;
+        double *h = a.hw[k] + (long long)Q * fc;
+#pragma unroll
+        for (int i = 0; i < Q; i++) h[i] = (double)getl(g[i], l) + wt_(i);
+    }
+}
+
 template <int P, int MODEL>
 cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaStream_t st) {
     Offs<int> of{};
@@ -665,9 +769,20 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
     const int R = std::max(1, 256 / tpr);
     dim3 blk(tpr, R), grd(1, (a.Y + R - 1) / R, a.X);
     size_t smem = (size_t)10 * R * a.Z * sizeof(typename V2<P>::S);
-    if (hooks) k_step_pair<P, MODEL, true, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
-    else if (sc.forced) k_step_pair<P, MODEL, true, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
-    else k_step_pair<P, MODEL, false, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    // the face hooks read the source buffer, which the bulk step leaves as is
+    if (hooks) {
+        for (int k = 0; k < 6; k++) {
+            if (!a.hw[k] && !a.l2[k]) continue;
+            const int ax = k >> 1;
+            const int A = ax == 2 ? a.Y : a.Z, B = ax == 0 ? a.Y : a.X;
+            const long long n = (long long)A * B;
+            k_face_hook<P, MODEL><<<(unsigned)((n + 255) / 256), 128, 0, st>>>(a, sc, ms, k, A, B);
+        }
+    }
+    if (sc.forced) k_step_pair<P, MODEL, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    else k_step_pair<P, MODEL, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    if (a.win.x1 >= a.win.x0 && a.win.n > 0)
+        k_win_fix<P, MODEL><<<(unsigned)((a.win.n + 255) / 256), 128, 0, st>>>(a, sc, ms);
     return cudaGetLastError();
 }
 
@@ -1008,18 +1123,138 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     return hooks ? step_launch<P, MODEL, true, long long>(a, m, st) : step_launch<P, MODEL, false, long long>(a, m, st);
 }
 
+// Face kernels of the offset storage forms (FP32, FP16, BF16): the codes of
+// bc_apply with FP32 arithmetic on the offsets g = f - w_i, one launch per
+// face in the reference order (edge and corner cells keep the value of the
+// last face that writes them). Face velocities are evaluated in FP64 (a few
+// operations per cell) and the rest in FP32.
+template <int P, int FACE>
+__global__ void __launch_bounds__(256) k_bc_off(BcArgs a) {
+    using T = ST<P>;
+    using S = typename T::S;
+    const int A = (FACE < 4) ? a.Z : a.Y;
+    const int B = (FACE < 2) ? a.Y : a.X;
+    const int fa = blockIdx.x * blockDim.x + threadIdx.x;
+    const int fb = blockIdx.y * blockDim.y + threadIdx.y;
+    if (fa >= A || fb >= B) return;
+    S *f = (S *)a.f;
+    const long long N = a.N;
+    const long long c1 = face_cell(a, fa, fb, 0);
+    auto ld = [&](long long c, int q) { return (float)T::dec(f[c + N * q]); };
+    auto stq = [&](long long c, int q, float g) { f[c + N * q] = T::enc(g); };
+    // offset equilibrium g_eq = w (rho - 1) + w rho (3 eu + 4.5 eu^2 - 1.5 u^2)
+    auto geq = [](int q, float rho, float u0, float u1, float u2, float k15) {
+        const float eu = (float)ex_(q) * u0 + (float)ey_(q) * u1 + (float)ez_(q) * u2;
+        const float w = (float)wt_(q);
+        return w * (rho - 1.0f) + (w * rho) * ((3.0f + 4.5f * eu) * eu - k15);
+    };
+    switch (a.code) {
+    case BC_EQ: {
+        double v[3];
+        face_vel(a, fa, fb, false, v);
+        const float u0 = (float)v[0], u1 = (float)v[1], u2 = (float)v[2];
+        const float k15 = 1.5f * (u0 * u0 + u1 * u1 + u2 * u2), rho = (float)a.denIn;
+#pragma unroll
+        for (int i = 0; i < Q; i++) stq(c1, i, geq(i, rho, u0, u1, u2, k15));
+    } break;
+    case BC_NEQ: {
+        const long long c2 = face_cell(a, fa, fb, 1);
+        double v[3];
+        face_vel(a, fa, fb, false, v);
+        const float u0 = (float)v[0], u1 = (float)v[1], u2 = (float)v[2];
+        const float k15 = 1.5f * (u0 * u0 + u1 * u1 + u2 * u2), rho = (float)a.denIn;
+        const float w0 = (float)a.u[c2], w1 = (float)a.u[c2 + N], w2 = (float)a.u[c2 + 2 * N];
+        const float d2 = (float)a.den[c2];
+        const float k15b = 1.5f * (w0 * w0 + w1 * w1 + w2 * w2);
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            const int q = inc_(FACE, j);
+            stq(c1, q, geq(q, rho, u0, u1, u2, k15) + (ld(c2, q) - geq(q, d2, w0, w1, w2, k15b)));
+        }
+    } break;
+    case BC_EXT1: {
+        const long long c2 = face_cell(a, fa, fb, 1);
+#pragma unroll
+        for (int j = 0; j < 5; j++) { const int q = inc_(FACE, j); f[c1 + N * q] = f[c2 + N * q]; }
+    } break;
+    case BC_EXT2: {
+        const long long c2 = face_cell(a, fa, fb, 1), c3 = face_cell(a, fa, fb, 2);
+        // 2 f2 - f3 = w + (2 g2 - g3): the offsets extrapolate the same way
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            const int q = inc_(FACE, j);
+            stq(c1, q, 2.0f * ld(c2, q) - ld(c3, q));
+        }
+    } break;
+    case BC_WALL: {
+        S t[5];
+#pragma unroll
+        for (int j = 0; j < 5; j++) t[j] = f[c1 + N * opp_(inc_(FACE, j))];
+#pragma unroll
+        for (int j = 0; j < 5; j++) f[c1 + N * inc_(FACE, j)] = t[j];
+    } break;
+    case BC_WALL_HW: {
+        const double *h = a.hw + (long long)Q * ((long long)fa + (long long)(FACE < 4 ? a.Z : a.Y) * fb);
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            const int q = inc_(FACE, j);
+            stq(c1, q, (float)(h[opp_(q)] - wt_(q)));
+        }
+    } break;
+    case BC_MWALL:
+    case BC_MWALL_HW: {
+        const bool half = (a.code == BC_MWALL_HW);
+        double v[3];
+        face_vel(a, fa, fb, half, v);
+        const double *h = a.hw + (long long)Q * ((long long)fa + (long long)(FACE < 4 ? a.Z : a.Y) * fb);
+        float t[5];
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            const int q = inc_(FACE, j);
+            const float eu = (float)(ex_(q) * v[0] + ey_(q) * v[1] + ez_(q) * v[2]);
+            // f_q = f_opp + 6 w denIn (e.u); the weights of q and opp(q) agree
+            const float gin = half ? (float)(h[opp_(q)] - wt_(q)) : ld(c1, opp_(q));
+            t[j] = gin + (6.0f * (float)wt_(q) * (float)a.denIn) * eu;
+        }
+#pragma unroll
+        for (int j = 0; j < 5; j++) stq(c1, inc_(FACE, j), t[j]);
+    } break;
+    case BC_SYMMETRIC: {
+        S t[5];
+#pragma unroll
+        for (int j = 0; j < 5; j++) t[j] = f[c1 + N * mir_(FACE, j)];
+#pragma unroll
+        for (int j = 0; j < 5; j++) f[c1 + N * inc_(FACE, j)] = t[j];
+    } break;
+    default:
+        break;
+    }
+}
+
 template <int P>
 cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
     const int A = (a.face < 4) ? a.Z : a.Y;
     const int B = (a.face < 2) ? a.Y : a.X;
     dim3 blk(64, 4), grd((A + 63) / 64, (B + 3) / 4);
+    if (P == FSI_PREC_F64_FAST) {
+        switch (a.face) {
+        case 0: k_bc<AccS<P>, 0><<<grd, blk, 0, st>>>(a); break;
+        case 1: k_bc<AccS<P>, 1><<<grd, blk, 0, st>>>(a); break;
+        case 2: k_bc<AccS<P>, 2><<<grd, blk, 0, st>>>(a); break;
+        case 3: k_bc<AccS<P>, 3><<<grd, blk, 0, st>>>(a); break;
+        case 4: k_bc<AccS<P>, 4><<<grd, blk, 0, st>>>(a); break;
+        default: k_bc<AccS<P>, 5><<<grd, blk, 0, st>>>(a); break;
+        }
+        return cudaGetLastError();
+    }
+    constexpr int PO = P == FSI_PREC_F64_FAST ? FSI_PREC_F32 : P;
     switch (a.face) {
-    case 0: k_bc<AccS<P>, 0><<<grd, blk, 0, st>>>(a); break;
-    case 1: k_bc<AccS<P>, 1><<<grd, blk, 0, st>>>(a); break;
-    case 2: k_bc<AccS<P>, 2><<<grd, blk, 0, st>>>(a); break;
-    case 3: k_bc<AccS<P>, 3><<<grd, blk, 0, st>>>(a); break;
-    case 4: k_bc<AccS<P>, 4><<<grd, blk, 0, st>>>(a); break;
-    default: k_bc<AccS<P>, 5><<<grd, blk, 0, st>>>(a); break;
+    case 0: k_bc_off<PO, 0><<<grd, blk, 0, st>>>(a); break;
+    case 1: k_bc_off<PO, 1><<<grd, blk, 0, st>>>(a); break;
+    case 2: k_bc_off<PO, 2><<<grd, blk, 0, st>>>(a); break;
+    case 3: k_bc_off<PO, 3><<<grd, blk, 0, st>>>(a); break;
+    case 4: k_bc_off<PO, 4><<<grd, blk, 0, st>>>(a); break;
+    default: k_bc_off<PO, 5><<<grd, blk, 0, st>>>(a); break;
     }
     return cudaGetLastError();
 }

@@ -109,12 +109,21 @@ int fsi_block_macro(fsi_block_t h, const double vf[3], double *den, double *uuu)
  * halfwayBCset_ (:567), streaming_ (:1514), set_boundary_conditions_ (:616).
  * macro (:1128) and ResetVolumeForce_ (:1195) are folded in: cells outside
  * the IB window take den/u from their own distributions and force = vf;
- * cells inside take the IB-corrected values from the last fsi_ib_solve. */
+ * cells inside take the IB-corrected values from the last fsi_ib_solve.
+ * The one asynchronous call: it reads no host memory after its arguments,
+ * so it returns once the step is queued on the block's stream; every call
+ * that hands data back to the host waits for it (a kernel fault of the step
+ * is reported by that next call). */
 int fsi_block_step(fsi_block_t h, const double vf[3], double blktime);
 
 /* run nsteps of fsi_block_step with constant vf and blktime advanced by dh per
  * step, launched from a captured CUDA graph; *ms = device time (CUDA events) */
 int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps, float *ms);
+
+/* No counterpart in the reference: device time of the work a host loop
+ * queues on the block's stream. stop = 0 records the start mark; stop = 1
+ * records the end mark, waits for it and sets *ms to the time between. */
+int fsi_block_timer(fsi_block_t h, int stop, float *ms);
 
 /* Immersed boundary (Solidbody.f90:869-1049). Bodies are stored back to back:
  * marker m of body b is global marker offs[b]+m, offs = prefix sums of M. */
