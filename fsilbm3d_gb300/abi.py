@@ -56,7 +56,9 @@ SYMBOLS = [
     "fsi_pair_father_to_son", "fsi_pair_son_to_father", "fsi_pair_father_to_son_static",
     "fsi_mlp_create", "fsi_mlp_destroy", "fsi_mlp_set_params", "fsi_mlp_get_params", "fsi_mlp_set_norm",
     "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_block_timer",
+    "fsi_block_set_kernel",
 ]
+KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
 # the warm-start perceptron (FSI_MLP_* in the header)
 MLP_IN, MLP_OUT, MLP_NPARAM, MLP_NNORM = 12, 3, 5187, 30
 # son face cells the allocation-free father-to-son variant can hold
@@ -92,6 +94,7 @@ def load_library():
     L.fsi_block_step.argtypes = [VP, DP, C.c_double]
     L.fsi_block_run.argtypes = [VP, DP, C.c_double, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_timer.argtypes = [VP, C.c_int, C.POINTER(C.c_float)]
+    L.fsi_block_set_kernel.argtypes = [VP, C.c_int]
     L.fsi_ib_set_bodies.argtypes = [VP, C.c_int, IP, IP]
     L.fsi_ib_solve.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                DP, IP, DP]
@@ -257,6 +260,10 @@ class Block:
         ms = C.c_float()
         _check(load_library().fsi_block_run(self.h, _dp(vf), blktime0, int(nsteps), C.byref(ms)))
         return ms.value
+
+    def set_kernel(self, kernel):
+        """bulk step kernel of the offset forms: KERNEL_AUTO, _PAIRED, _PIPELINED"""
+        _check(load_library().fsi_block_set_kernel(self.h, int(kernel)))
 
     def timer_start(self):
         """mark the start of a timed region on the block's stream"""

@@ -155,6 +155,7 @@ __global__ void k_bc(BcArgs a) {
     int fa = blockIdx.x * blockDim.x + threadIdx.x;
     int fb = blockIdx.y * blockDim.y + threadIdx.y;
     if (fa >= A || fb >= B) return;
+    if (FACE < 4 && (fa < a.zlo || fa > a.zhi)) return;
     bc_apply<ACC, FACE>(a, fa, fb);
 }
 

@@ -152,7 +152,10 @@ struct fsi_block {
     int *h_err = nullptr;     // pinned
     // cooperative IB solve of the fast forms
     int coop_grid = 0;
-    int *d_status = nullptr;  // 4 ints: flags, iterations, barrier count, generation
+    // 8 ints: IB flags, iterations, barrier count, generation; [4] the step
+    // kernel's error word (bit 1: a bounded wait ran out)
+    int *d_status = nullptr;
+    int *h_stat = nullptr;  // pinned copy of d_status[0..5)
     double *d_res = nullptr, *d_tolacc = nullptr;
     int tolacc_cap = 0;
     // warm start: per-marker auxiliary inputs and logged features
@@ -167,6 +170,7 @@ struct fsi_block {
     long long list_cap = 0;
     bool win_valid = false;
     // captured graph of two steps (A->B, B->A)
+    int kernel = FSI_KERNEL_AUTO;  // bulk step kernel of the offset forms
     cudaGraphExec_t gexec = nullptr;
     double g_vf[3] = {0, 0, 0};
     void *g_src = nullptr;
@@ -221,10 +225,14 @@ void face_dims(const fsi_block *h, int k, int &A, int &B) {
     B = (ax == 0) ? h->Y : h->X;
 }
 
-int apply_bcs(fsi_block *h, void *f, double blktime) {
+// zdone[s]: the step kernel already wrote z face 4+s (its x/y faces then
+// leave that plane alone, so that the z face stays the last writer there)
+int apply_bcs(fsi_block *h, void *f, double blktime, const int zdone[2] = nullptr) {
+    const int zd0 = zdone ? zdone[0] : 0, zd1 = zdone ? zdone[1] : 0;
     for (int k = 0; k < 6; k++) {
         int code = h->d.bndConds[k];
         if (code == BC_PERIODIC || code == BC_FLUID || code == BC_FLUID_FATHER) continue;
+        if ((k == 4 && zd0) || (k == 5 && zd1)) continue;
         if (code == BC_WALL_HW || code == BC_MWALL_HW) {
             // allocate-on-first-call semantics, FluidDomain.f90:660-662
             if (!h->hw_ready[k]) { h->hw_ready[k] = 1; continue; }
@@ -240,6 +248,8 @@ int apply_bcs(fsi_block *h, void *f, double blktime) {
         a.hw = h->hw[k];
         a.den = h->den;
         a.u = h->u;
+        a.zlo = zd0 ? 1 : 0;
+        a.zhi = h->Z - 1 - (zd1 ? 1 : 0);
         cudaError_t e = is_fast(h) ? launch_bc_fast(a, h->prec, h->st) : launch_bc_f64(a, h->st);
         if (e != cudaSuccess) return fail(FSI_E_CUDA, "boundary kernel: %s", cudaGetErrorString(e));
     }
@@ -271,12 +281,44 @@ int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_wind
     }
     a.den = h->den;
     a.u = h->u;
+    a.kerr = h->d_status + 4;
+    a.variant = h->kernel;
+    // z faces of code 101 with a face velocity uniform over the face: the
+    // paired kernels write their equilibrium while streaming
+    if (is_fast(h) && step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel)) {
+        const Vel v = make_vel(h, blktime);
+        const bool uniform = v.kind == 2 || (v.sr[0] == 0.0 && v.sr[1] == 0.0);
+        for (int s = 0; s < 2; s++) {
+            if (h->d.bndConds[4 + s] != BC_EQ || !uniform) continue;
+            // evaluate_velocity at the face (FluidDomain.f90:1791-1824)
+            const double zc = s ? h->zmax : h->d.zmin;
+            double u[3];
+            if (v.kind == 2) {
+                u[0] = v.osc[0]; u[1] = v.osc[1]; u[2] = v.osc[2];
+            } else {
+                u[0] = ((v.vin[0] + 0.0 * v.sr[0]) + h->d.ymin * v.sr[1]) + zc * v.sr[2];
+                u[1] = ((v.vin[1] + h->d.xmin * v.sr[0]) + 0.0 * v.sr[1]) + zc * v.sr[2];
+                u[2] = ((v.vin[2] + h->d.xmin * v.sr[0]) + h->d.ymin * v.sr[1]) + 0.0 * v.sr[2];
+            }
+            a.zeq[s] = 1;
+            for (int c = 0; c < 3; c++) a.zu[s][c] = (float)u[c];
+        }
+        a.den_in = (float)h->d.denIn;
+    }
     cudaError_t e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
                                : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
     if (e != cudaSuccess) return fail(FSI_E_CUDA, "step kernel: %s", cudaGetErrorString(e));
-    int rc = apply_bcs(h, h->fb, blktime);
+    int rc = apply_bcs(h, h->fb, blktime, a.zeq);
     if (rc) return rc;
     std::swap(h->fa, h->fb);
+    return FSI_OK;
+}
+
+// the step kernel's error word, read after the stream has drained
+int check_kerr(fsi_block *h) {
+    CK(cudaMemcpyAsync(h->h_stat + 4, h->d_status + 4, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (h->h_stat[4]) return fail(FSI_E_TIMEOUT, "step kernel: a bounded wait ran out");
     return FSI_OK;
 }
 
@@ -293,6 +335,7 @@ void free_block(fsi_block *h) {
         if (h->hw[k]) cudaFree(h->hw[k]);
     if (h->h_tol) cudaFreeHost(h->h_tol);
     if (h->h_err) cudaFreeHost(h->h_err);
+    if (h->h_stat) cudaFreeHost(h->h_stat);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->st) cudaStreamDestroy(h->st);
@@ -395,6 +438,9 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     chk(cudaHostAlloc((void **)&h->h_tol, sizeof(double) * 64, cudaHostAllocDefault));
     chk(cudaHostAlloc((void **)&h->h_err, sizeof(int), cudaHostAllocDefault));
     chk(cudaMalloc((void **)&h->d_err, sizeof(int)));
+    chk(cudaMalloc((void **)&h->d_status, sizeof(int) * 8));
+    chk(cudaMalloc((void **)&h->d_res, sizeof(double)));
+    chk(cudaHostAlloc((void **)&h->h_stat, sizeof(int) * 8, cudaHostAllocDefault));
     // every device operation of a block goes to its own (non-blocking)
     // stream: work on the legacy default stream would not be ordered with it
     if (e == cudaSuccess) chk(cudaMemsetAsync(h->den, 0, sizeof(double) * h->N, h->st));
@@ -402,6 +448,7 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     if (e == cudaSuccess) chk(cudaMemsetAsync(h->fa, 0, fbytes, h->st));
     if (e == cudaSuccess) chk(cudaMemsetAsync(h->fb, 0, fbytes, h->st));
     if (e == cudaSuccess) chk(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 8, h->st));
     if (e == cudaSuccess) chk(cudaStreamSynchronize(h->st));
     if (e != cudaSuccess) {
         free_block(h);
@@ -449,8 +496,7 @@ int fsi_block_download_f(fsi_block_t h, double *fIn) {
         CK(launch_convert_from_store(h->fa, h->stage, h->N, h->prec, h->st));
         CK(cudaMemcpyAsync(fIn, h->stage, n * 8, cudaMemcpyDeviceToHost, h->st));
     }
-    CK(cudaStreamSynchronize(h->st));
-    return FSI_OK;
+    return check_kerr(h);
 }
 
 int fsi_block_initialise(fsi_block_t h, double time) {
@@ -483,8 +529,7 @@ int fsi_block_macro(fsi_block_t h, const double vf[3], double *den, double *uuu)
     }
     if (den) CK(cudaMemcpyAsync(den, h->den, sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->st));
     if (uuu) CK(cudaMemcpyAsync(uuu, h->u, sizeof(double) * 3 * h->N, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
-    return FSI_OK;
+    return check_kerr(h);
 }
 
 int fsi_block_step(fsi_block_t h, const double vf[3], double blktime) {
@@ -492,6 +537,19 @@ int fsi_block_step(fsi_block_t h, const double vf[3], double blktime) {
     int rc = enqueue_step(h, vf, blktime, true);
     h->win_valid = false;
     return rc;
+}
+
+int fsi_block_set_kernel(fsi_block_t h, int kernel) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    if (kernel < FSI_KERNEL_AUTO || kernel > FSI_KERNEL_PIPELINED) return fail(FSI_E_ARG, "unknown kernel %d", kernel);
+    if (kernel == FSI_KERNEL_PIPELINED && h->Z % 8 != 0)
+        return fail(FSI_E_ARG, "the pipelined kernel needs zDim a multiple of 8");
+    if (kernel != h->kernel && h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    h->kernel = kernel;
+    return FSI_OK;
 }
 
 int fsi_block_timer(fsi_block_t h, int stop, float *ms) {
@@ -505,7 +563,7 @@ int fsi_block_timer(fsi_block_t h, int stop, float *ms) {
     float t = 0.0f;
     CK(cudaEventElapsedTime(&t, h->ev0, h->ev1));
     if (ms) *ms = t;
-    return FSI_OK;
+    return check_kerr(h);
 }
 
 int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps, float *ms) {
@@ -554,7 +612,7 @@ int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps
     CK(cudaEventRecord(h->ev1, h->st));
     CK(cudaEventSynchronize(h->ev1));
     if (ms) CK(cudaEventElapsedTime(ms, h->ev0, h->ev1));
-    return FSI_OK;
+    return check_kerr(h);
 }
 
 // ------------------------------------------------------------------------ IB
@@ -672,10 +730,6 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         h->coop_grid = ib_coop_grid(h->prec);
         if (h->coop_grid <= 0) return fail(FSI_E_CUDA, "no co-resident grid for the IB kernel");
     }
-    if (!h->d_status) {
-        CK(cudaMalloc((void **)&h->d_status, sizeof(int) * 4));
-        CK(cudaMalloc((void **)&h->d_res, sizeof(double)));
-    }
     if (ntol > h->tolacc_cap) {
         if (h->d_tolacc) cudaFree(h->d_tolacc);
         h->tolacc_cap = std::max(ntol, 64);
@@ -718,17 +772,16 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
     if (wm.features)
         CK(cudaMemcpyAsync(wm.features, h->d_feat, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(h->h_err, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(h->h_tol + 1, h->d_status + 1, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    const int st = *h->h_err;
+    if (h->h_stat[4]) return fail(FSI_E_TIMEOUT, "step kernel: a bounded wait ran out");
+    const int st = h->h_stat[0];
     if (st & 1) return fail(FSI_E_RANGE, "index out of block bounds in IB stencil");
     if (st & 2) return fail(FSI_E_RANGE, "IB stencil outside the IB window");
     if (st & 4) return fail(FSI_E_NAN, "Nan found in PenaltyForce");
     if (st & 8) return fail(FSI_E_TIMEOUT, "IB grid barrier timed out");
-    int it = 0;
-    memcpy(&it, (const void *)(h->h_tol + 1), sizeof(int));
+    const int it = h->h_stat[1];
     if (iters) *iters = it;
     if (residual) *residual = h->h_tol[0];
     h->win_valid = true;

@@ -120,6 +120,14 @@ struct StepArgs {
     double *den;          // full-size den/u, written on layer-2 planes of 102 faces
     double *u;
     int l2[6];            // 1 if face k has code 102
+    int *kerr;            // error word of the pipelined kernel (bit 1: a bounded wait ran out)
+    int variant;          // bulk kernel of the offset forms: 0 auto, 1 paired, 2 pipelined
+    // z- / z+ faces of code 101 with a uniform face velocity, written by the
+    // paired step kernels themselves (the equilibrium at the face velocity);
+    // set only when the host leaves those faces out of the face kernels
+    int zeq[2];
+    float zu[2][3];
+    float den_in;
 };
 
 struct BcArgs {
@@ -134,6 +142,8 @@ struct BcArgs {
     const double *hw;     // half-way copy of this face
     const double *den;    // full-size den/u (102)
     const double *u;
+    int zlo, zhi;         // x/y faces: the z range they act on (the z faces the
+                          // step kernel wrote are left to it)
 };
 
 }  // namespace fsi

@@ -89,6 +89,8 @@ cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, co
 
 // ---- fast kernels (k_fast.cu): FP64 regrouped, FP32/FP16/BF16 storage ----
 cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st);
+// true when launch_step_fast runs the paired kernels (which can write 101 z faces)
+bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model);
 cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st);
 cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st);
 cudaError_t launch_convert_from_store(const void *fs, double *f64, long long N, int prec, cudaStream_t st);

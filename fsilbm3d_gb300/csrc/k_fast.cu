@@ -17,6 +17,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstdint>
 
 #include "bc_impl.cuh"
 #include "fsi_kernels.h"
@@ -82,6 +83,18 @@ template <typename C> __device__ __forceinline__ C sel(int e, C v) { return e > 
 // representatives of the nine opposite pairs (positivedirs, ConstParams.f90:19)
 __host__ __device__ constexpr int pr_(int k) {
     return k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 5 : k == 3 ? 7 : k == 4 ? 8 : k == 5 ? 11 : k == 6 ? 12 : k == 7 ? 15 : 16;
+}
+
+// offset equilibrium g_eq = w (rho - 1) + w rho (3 eu + 4.5 eu^2 - 1.5 u^2),
+// k15 = 1.5 u^2 (the face kernels and the fused z faces)
+__device__ __forceinline__ float geq_off(int q, float rho, float u0, float u1, float u2, float k15) {
+    const float eu = (float)ex_(q) * u0 + (float)ey_(q) * u1 + (float)ez_(q) * u2;
+    const float w = (float)wt_(q);
+    return w * (rho - 1.0f) + (w * rho) * ((3.0f + 4.5f * eu) * eu - k15);
+}
+__device__ __forceinline__ float geq_zface(const StepArgs &a, int side, int q) {
+    const float u0 = a.zu[side][0], u1 = a.zu[side][1], u2 = a.zu[side][2];
+    return geq_off(q, a.den_in, u0, u1, u2, 1.5f * (u0 * u0 + u1 * u1 + u2 * u2));
 }
 
 // density (and its offset from 1) and velocity of one cell,
@@ -436,14 +449,106 @@ __device__ __forceinline__ void vel2(float2 rho, float2 jx, float2 jy, float2 jz
     }
 }
 
+// The moment transform of the D3Q19 basis (mrow_) written out by velocity
+// class, for the pair layout of the paired kernels: r0 (rest), rs[k] = r_i +
+// r_o and rd[k] = r_i - r_o for the nine pairs in pr_ order (x, y, z axes;
+// diagonals (1,1,0), (-1,1,0), (1,0,1), (-1,0,1), (0,1,1), (0,-1,1)).
+// Shared partial sums (axis / diagonal class sums and pair combinations)
+// replace the direct 19-term rows: about 40 packed operations each way
+// instead of about 80. The conserved moments 0, 3, 5, 7 are not formed.
+// t[k] = sd[k] m_k (relaxation rate over |row k|^2).
+__device__ __forceinline__ void mrt_forward(float2 r0, const float2 rs[9], const float2 rd[9], const MrtS &ms,
+                                            float2 t[Q]) {
+    // even moments from the pair sums
+    const float2 Ax = rs[0], Ay = rs[1], Az = rs[2];
+    const float2 Dxy = add2(rs[3], rs[4]), Dxz = add2(rs[5], rs[6]), Dyz = add2(rs[7], rs[8]);
+    const float2 A = add2(add2(Ax, Ay), Az), D = add2(add2(Dxy, Dxz), Dyz);
+    const float2 m1 = fma2(f2(-30.0f), r0, fma2(f2(-11.0f), A, mul2(f2(8.0f), D)));
+    const float2 m2 = fma2(f2(12.0f), r0, fma2(f2(-4.0f), A, D));
+    const float2 U = add2(Ay, Az), V = fma2(f2(-2.0f), Dyz, add2(Dxy, Dxz));
+    const float2 m9 = fma2(f2(2.0f), Ax, sub2(V, U));
+    const float2 m10 = fma2(f2(-4.0f), Ax, fma2(f2(2.0f), U, V));
+    const float2 W = sub2(Ay, Az), Xd = sub2(Dxy, Dxz);
+    const float2 m11 = add2(W, Xd);
+    const float2 m12 = fma2(f2(-2.0f), W, Xd);
+    const float2 m13 = sub2(rs[3], rs[4]), m14 = sub2(rs[7], rs[8]), m15 = sub2(rs[5], rs[6]);
+    // odd moments from the pair differences
+    const float2 p3 = sub2(rd[3], rd[4]), q3 = add2(rd[3], rd[4]);
+    const float2 p5 = sub2(rd[5], rd[6]), q5 = add2(rd[5], rd[6]);
+    const float2 p7 = sub2(rd[7], rd[8]), q7 = add2(rd[7], rd[8]);
+    const float2 m4 = fma2(f2(-4.0f), rd[0], add2(p3, p5));
+    const float2 m16 = sub2(p3, p5);
+    const float2 m6 = fma2(f2(-4.0f), rd[1], add2(q3, p7));
+    const float2 m17 = sub2(p7, q3);
+    const float2 m8 = fma2(f2(-4.0f), rd[2], add2(q5, q7));
+    const float2 m18 = sub2(q5, q7);
+    t[0] = t[3] = t[5] = t[7] = f2(0.0f);
+    t[1] = mul2(f2(ms.sd[1]), m1);
+    t[2] = mul2(f2(ms.sd[2]), m2);
+    t[4] = mul2(f2(ms.sd[4]), m4);
+    t[6] = mul2(f2(ms.sd[6]), m6);
+    t[8] = mul2(f2(ms.sd[8]), m8);
+    t[9] = mul2(f2(ms.sd[9]), m9);
+    t[10] = mul2(f2(ms.sd[10]), m10);
+    t[11] = mul2(f2(ms.sd[11]), m11);
+    t[12] = mul2(f2(ms.sd[12]), m12);
+    t[13] = mul2(f2(ms.sd[13]), m13);
+    t[14] = mul2(f2(ms.sd[14]), m14);
+    t[15] = mul2(f2(ms.sd[15]), m15);
+    t[16] = mul2(f2(ms.sd[16]), m16);
+    t[17] = mul2(f2(ms.sd[17]), m17);
+    t[18] = mul2(f2(ms.sd[18]), m18);
+}
+
+// Delta = M^T t split by parity: Delta_0 = E0; for pair k with representative
+// i: Delta_i = E[k] + O[k], Delta_opp(i) = E[k] - O[k]
+__device__ __forceinline__ void mrt_backward(const float2 t[Q], float2 &E0, float2 E[9], float2 O[9]) {
+    E0 = fma2(f2(-30.0f), t[1], mul2(f2(12.0f), t[2]));
+    // axes
+    const float2 Ca = fma2(f2(-11.0f), t[1], mul2(f2(-4.0f), t[2]));
+    const float2 G = fma2(f2(2.0f), t[10], neg2(t[9]));
+    const float2 H = fma2(f2(-2.0f), t[12], t[11]);
+    E[0] = fma2(f2(-2.0f), G, Ca);
+    E[1] = add2(add2(Ca, G), H);
+    E[2] = sub2(add2(Ca, G), H);
+    O[0] = mul2(f2(-4.0f), t[4]);
+    O[1] = mul2(f2(-4.0f), t[6]);
+    O[2] = mul2(f2(-4.0f), t[8]);
+    // diagonals
+    const float2 Cd = fma2(f2(8.0f), t[1], t[2]);
+    const float2 J = add2(t[9], t[10]), K = add2(t[11], t[12]);
+    const float2 L = add2(Cd, J);
+    const float2 b34 = add2(L, K), b56 = sub2(L, K), b78 = fma2(f2(-2.0f), J, Cd);
+    E[3] = add2(b34, t[13]);
+    E[4] = sub2(b34, t[13]);
+    E[5] = add2(b56, t[15]);
+    E[6] = sub2(b56, t[15]);
+    E[7] = add2(b78, t[14]);
+    E[8] = sub2(b78, t[14]);
+    const float2 a = add2(t[4], t[16]), b = sub2(t[6], t[17]);
+    const float2 c = sub2(t[4], t[16]), d = add2(t[8], t[18]);
+    const float2 e = add2(t[6], t[17]), f = sub2(t[8], t[18]);
+    O[3] = add2(a, b);
+    O[4] = sub2(b, a);
+    O[5] = add2(c, d);
+    O[6] = sub2(d, c);
+    O[7] = add2(e, f);
+    O[8] = sub2(f, e);
+}
+
 // the collision of two cells (offset storage, FP32x2): SRT (FluidDomain.f90:
 // 1218-1227, Omega folded per weight class) or MRT (:1236-1238) in moment
-// space, g += M^-1 S M (feq - g - Flb/2) + Flb, which is M_COLLID (feq - g) +
-// M_FORCE Flb for M_FORCE = I - M_COLLID/2. Opposite velocities are handled
-// as sums (even moments) and differences (odd moments).
-template <int MODEL, bool FORCED>
-__device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1, float2 u2,
-                                         float2 F0, float2 F1, float2 F2, const Scal<float> &sc, const MrtS &ms) {
+// space, g' = g + M^-1 S M (feq - g - Flb/2) + Flb, which is M_COLLID (feq - g)
+// + M_FORCE Flb for M_FORCE = I - M_COLLID/2. Opposite velocities are handled
+// as sums (even moments) and differences (odd moments). Each post-collision
+// population goes to emit(i, value) as soon as it is known, so that the
+// caller can store it at once. With KEEPG false the MRT form does not keep g
+// past the moment transform (g = feq - Flb/2 - r is rebuilt from the sums it
+// keeps); with KEEPG true it adds Delta + Flb to the g it kept.
+template <int MODEL, bool FORCED, bool KEEPG, class EMIT>
+__device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1,
+                                             float2 u2, float2 F0, float2 F1, float2 F2, const Scal<float> &sc,
+                                             const MrtS &ms, EMIT &&emit) {
     const float om = sc.om;
     const float2 k15 = mul2(f2(1.5f), fma2(u0, u0, fma2(u1, u1, mul2(u2, u2))));
     float2 uF = f2(0.f);
@@ -457,8 +562,9 @@ __device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, f
         const float2 ac1 = mul2(f2(om * w1), base), bc1 = mul2(f2(4.5f * w1), orho), cc1 = mul2(f2(3.0f * w1), orho);
         const float2 ac2 = mul2(f2(om * w2), base), bc2 = mul2(f2(4.5f * w2), orho), cc2 = mul2(f2(3.0f * w2), orho);
         const float cf = (1.0f - 0.5f * om) * sc.dh3;
-        g[0] = fma2(omc, g[0], ac0);
-        if (FORCED) g[0] = sub2(g[0], mul2(f2(cf * w0), uF));
+        float2 n0 = fma2(omc, g[0], ac0);
+        if (FORCED) n0 = sub2(n0, mul2(f2(cf * w0), uF));
+        emit(0, n0);
 #pragma unroll
         for (int k = 0; k < 9; k++) {
             const int i = pr_(k), o = opp_(i);
@@ -475,77 +581,120 @@ __device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, f
                 ni = add2(ni, add2(Fs, Fa));
                 no = add2(no, sub2(Fs, Fa));
             }
-            g[i] = ni;
-            g[o] = no;
+            emit(i, ni);
+            emit(o, no);
         }
     } else {
         const float dh3 = sc.dh3;
-        float2 rs[9], rd[9];
-        const float2 r0 = FORCED ? sub2(fma2(f2(w0), sub2(drho, mul2(rho, k15)), mul2(f2(0.5f * dh3 * w0), uF)), g[0])
-                                 : sub2(mul2(f2(w0), sub2(drho, mul2(rho, k15))), g[0]);
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-            const int i = pr_(k), o = opp_(i);
+        // per pair: fsum = feq_i + feq_o, fdif = feq_i - feq_o,
+        // FS = (Flb_i + Flb_o)/2, FA = (Flb_i - Flb_o)/2
+        auto pair_terms = [&](int i, float2 &fsum, float2 &fdif, float2 &FS, float2 &FA) {
             const float w = (float)wt_(i);
             const float2 eu = edot(i, u0, u1, u2);
             const float2 wr = mul2(f2(w), rho);
-            // (feq_i + feq_o) and (feq_i - feq_o)
-            const float2 fsum = mul2(f2(2.0f), fma2(f2(w), drho, mul2(wr, fma2(f2(4.5f), mul2(eu, eu), neg2(k15)))));
-            const float2 fdif = mul2(mul2(f2(6.0f), wr), eu);
+            fsum = mul2(f2(2.0f), fma2(f2(w), drho, mul2(wr, fma2(f2(4.5f), mul2(eu, eu), neg2(k15)))));
+            fdif = mul2(mul2(f2(6.0f), wr), eu);
+            if (FORCED) {
+                const float2 eF = edot(i, F0, F1, F2);
+                FS = mul2(f2(dh3 * w), sub2(mul2(f2(3.0f), mul2(eu, eF)), uF));
+                FA = mul2(f2(dh3 * w), eF);
+            } else {
+                FS = f2(0.f);
+                FA = f2(0.f);
+            }
+        };
+        const float2 feq0 = mul2(f2(w0), sub2(drho, mul2(rho, k15)));
+        const float2 hf0 = FORCED ? mul2(f2(0.5f * dh3 * w0), uF) : f2(0.f);  // -Flb_0/2
+        // r = feq - g - Flb/2: rest r0, pair sums rs = r_i + r_o, differences rd = r_i - r_o
+        const float2 r0 = FORCED ? sub2(add2(feq0, hf0), g[0]) : sub2(feq0, g[0]);
+        float2 rs[9], rd[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int i = pr_(k), o = opp_(i);
+            float2 fsum, fdif, FS, FA;
+            pair_terms(i, fsum, fdif, FS, FA);
             float2 sm = sub2(fsum, add2(g[i], g[o]));
             float2 dm = sub2(fdif, sub2(g[i], g[o]));
             if (FORCED) {
-                // (Flb_i + Flb_o)/2 and (Flb_i - Flb_o)/2
-                const float2 eF = edot(i, F0, F1, F2);
-                sm = sub2(sm, mul2(f2(dh3 * w), sub2(mul2(f2(3.0f), mul2(eu, eF)), uF)));
-                dm = sub2(dm, mul2(f2(dh3 * w), eF));
+                sm = sub2(sm, FS);
+                dm = sub2(dm, FA);
             }
             rs[k] = sm;
             rd[k] = dm;
         }
-        // relaxed moments t_k = S_k/|row k|^2 (M r)_k
-        float2 t[Q];
+        float2 t[Q], E0, E[9], O[9];
+        mrt_forward(r0, rs, rd, ms, t);
+        mrt_backward(t, E0, E, O);
+        if (KEEPG) {
+            // g'_i = g_i + Delta_i + Flb_i
+            float2 n0 = add2(g[0], E0);
+            if (FORCED) n0 = fma2(f2(-2.0f), hf0, n0);
+            emit(0, n0);
 #pragma unroll
-        for (int m = 0; m < Q; m++) {
-            if (m == 0 || m == 3 || m == 5 || m == 7) { t[m] = f2(0.f); continue; }
-            Acc2 acc{f2(0.f), false};
-            if (!modd_(m)) acc_add(acc, mrow_(m, 0), r0);
-#pragma unroll
-            for (int k = 0; k < 9; k++) acc_add(acc, mrow_(m, pr_(k)), modd_(m) ? rd[k] : rs[k]);
-            t[m] = mul2(f2(ms.sd[m]), acc_val(acc));
-        }
-        // back to populations: Delta_i = sum_k M[k][i] t_k, split by parity
-        {
-            Acc2 e{f2(0.f), false};
-#pragma unroll
-            for (int m = 0; m < Q; m++)
-                if (!modd_(m) && m != 0) acc_add(e, mrow_(m, 0), t[m]);
-            float2 d0 = acc_val(e);
-            if (FORCED) d0 = sub2(d0, mul2(f2(dh3 * w0), uF));
-            g[0] = add2(g[0], d0);
-        }
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-            const int i = pr_(k), o = opp_(i);
-            Acc2 e{f2(0.f), false}, d{f2(0.f), false};
-#pragma unroll
-            for (int m = 1; m < Q; m++) {
-                if (m == 3 || m == 5 || m == 7) continue;
-                if (modd_(m)) acc_add(d, mrow_(m, i), t[m]);
-                else acc_add(e, mrow_(m, i), t[m]);
+            for (int k = 0; k < 9; k++) {
+                const int i = pr_(k), o = opp_(i);
+                float2 ev = E[k], dv = O[k];
+                if (FORCED) {
+                    float2 fsum, fdif, FS, FA;
+                    pair_terms(i, fsum, fdif, FS, FA);
+                    ev = add2(ev, FS);
+                    dv = add2(dv, FA);
+                }
+                emit(i, add2(g[i], add2(ev, dv)));
+                emit(o, add2(g[o], sub2(ev, dv)));
             }
-            float2 ev = acc_val(e), dv = acc_val(d);
-            if (FORCED) {
-                const float w = (float)wt_(i);
-                const float2 eu = edot(i, u0, u1, u2);
-                const float2 eF = edot(i, F0, F1, F2);
-                ev = add2(ev, mul2(f2(dh3 * w), sub2(mul2(f2(3.0f), mul2(eu, eF)), uF)));
-                dv = add2(dv, mul2(f2(dh3 * w), eF));
+        } else {
+            // g'_i = g_i + Delta_i + Flb_i with g_i = feq_i - Flb_i/2 - r_i:
+            //   rest:  g'_0 = feq_0 + Flb_0/2 - r_0 + Delta_0
+            //   pairs: g'_i,o = A +- B, A = (fsum + FS - rs)/2 + E, B = (fdif + FA - rd)/2 + O
+            float2 n0 = add2(sub2(feq0, r0), E0);
+            if (FORCED) n0 = sub2(n0, hf0);
+            emit(0, n0);
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                const int i = pr_(k), o = opp_(i);
+                float2 fsum, fdif, FS, FA;
+                pair_terms(i, fsum, fdif, FS, FA);
+                float2 A = fma2(f2(0.5f), sub2(fsum, rs[k]), E[k]);
+                float2 B = fma2(f2(0.5f), sub2(fdif, rd[k]), O[k]);
+                if (FORCED) {
+                    A = fma2(f2(0.5f), FS, A);
+                    B = fma2(f2(0.5f), FA, B);
+                }
+                emit(i, add2(A, B));
+                emit(o, sub2(A, B));
             }
-            g[i] = add2(g[i], add2(ev, dv));
-            g[o] = add2(g[o], sub2(ev, dv));
         }
     }
+}
+
+// collide_emit with the results written back into g
+template <int MODEL, bool FORCED>
+__device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1, float2 u2,
+                                         float2 F0, float2 F1, float2 F2, const Scal<float> &sc, const MrtS &ms) {
+    float2 out[Q];
+    collide_emit<MODEL, FORCED, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms,
+                                      [&](int i, float2 v) { out[i] = v; });
+#pragma unroll
+    for (int i = 0; i < Q; i++) g[i] = out[i];
+}
+
+// resident CTAs per SM the paired bulk kernel is compiled for (its register
+// budget), measured best on GB300: SRT 4 x 256 threads (<= 64 registers);
+// MRT unforced FP16/BF16 3 (<= 85, a little spill), MRT forced or FP32 2
+#ifndef FSI_PAIR_MINB_SRT
+#define FSI_PAIR_MINB_SRT 4
+#endif
+#ifndef FSI_PAIR_MINB_MRT
+#define FSI_PAIR_MINB_MRT 3
+#endif
+#ifndef FSI_PAIR_MINB_MRT_FORCED
+#define FSI_PAIR_MINB_MRT_FORCED 2
+#endif
+template <int P, int MODEL, bool FORCED>
+constexpr int pair_minb() {
+    return MODEL == 1 ? FSI_PAIR_MINB_SRT
+                      : ((FORCED || P == FSI_PREC_F32) ? FSI_PAIR_MINB_MRT_FORCED : FSI_PAIR_MINB_MRT);
 }
 
 // The bulk step: every cell takes den/u from its own distributions and the
@@ -553,7 +702,8 @@ __device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, f
 // planes are then corrected by the small kernels below, which read the same
 // (unchanged) source buffer.
 template <int P, int MODEL, bool FORCED>
-__global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
+__global__ void __launch_bounds__(256, pair_minb<P, MODEL, FORCED>())
+k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
     using V = V2<P>;
     using S2 = typename V::S2;
     using S = typename V::S;
@@ -580,36 +730,249 @@ __global__ void __launch_bounds__(256) k_step_pair(StepArgs a, Offs<int> of, Sca
     macro2(g, drho, rho, jx, jy, jz);
     const float2 F0 = f2(sc.vf[0]), F1 = f2(sc.vf[1]), F2 = f2(sc.vf[2]);
     vel2<FORCED>(rho, jx, jy, jz, F0, F1, F2, 0.5f * sc.dh, u0, u1, u2);
-    collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
 
-    // stage the ten z-moving populations of this row in shared memory
-    if (active) {
-#pragma unroll
-        for (int i = 0; i < Q; i++)
-            if (ez_(i) != 0) *(S2 *)(sm + (zslot_(i) * R + ty) * Z + z0) = V::enc(g[i]);
-    }
-    __syncthreads();
-    if (!active) return;
-
-    // push; the destination row is (y+ey, x+ex) with periodic wrap
+    // push; the destination row is (y+ey, x+ex) with periodic wrap. The nine
+    // populations with ez = 0 are stored as soon as they are collided; the
+    // ten z-moving ones go through shared memory for the +-z shift.
     const int ZY = Z * Y;
     const int cyp = (y == Y - 1) ? -ZY : 0, cym = (y == 0) ? ZY : 0;
     const int cxp = (x == X - 1) ? -N : 0, cxm = (x == 0) ? N : 0;
     S *dp = (S *)a.dst + c;
+    auto corr = [&](int i) {
+        return (ey_(i) > 0 ? cyp : (ey_(i) < 0 ? cym : 0)) + (ex_(i) > 0 ? cxp : (ex_(i) < 0 ? cxm : 0));
+    };
+    // destination cells z0, z0+1 on a z face the kernel writes itself
+    const bool zf0 = a.zeq[0] && z0 == 0, zf1 = a.zeq[1] && z0 + 1 == Z - 1;
+    auto emit = [&](int i, float2 v) {
+        if (!active) return;
+        if (ez_(i) == 0) {
+            if (zf0) v.x = geq_zface(a, 0, i);
+            if (zf1) v.y = geq_zface(a, 1, i);
+            __stcs((S2 *)(dp + corr(i) + of.st[i]), V::enc(v));
+        } else {
+            *(S2 *)(sm + (zslot_(i) * R + ty) * Z + z0) = V::enc(v);
+        }
+    };
+    if (MODEL == 1) {
+        // SRT: stored pair by pair, so that the 64-register budget holds
+        collide_emit<MODEL, FORCED, false>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit);
+    } else {
+        // MRT: all 19 collided first (measured faster at two CTAs per SM)
+        collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
+#pragma unroll
+        for (int i = 0; i < Q; i++) emit(i, g[i]);
+    }
+    __syncthreads();
+    if (!active) return;
     const int zl = (z0 == 0) ? Z - 1 : z0 - 1, zr = (z0 + 2 == Z) ? 0 : z0 + 2;
 #pragma unroll
     for (int i = 0; i < Q; i++) {
-        const int corr = (ey_(i) > 0 ? cyp : (ey_(i) < 0 ? cym : 0)) + (ex_(i) > 0 ? cxp : (ex_(i) < 0 ? cxm : 0));
-        S2 v;
-        if (ez_(i) == 0) {
-            v = V::enc(g[i]);
-        } else {
-            const S *row = sm + (zslot_(i) * R + ty) * Z;
-            // ez = +1: cells z0, z0+1 receive z0-1, z0; ez = -1: they receive z0+1, z0+2
-            v = ez_(i) > 0 ? V::pack(row[zl], row[z0]) : V::pack(row[z0 + 1], row[zr]);
-        }
-        __stcs((S2 *)(dp + corr + of.st[i]), v);
+        if (ez_(i) == 0) continue;
+        const S *row = sm + (zslot_(i) * R + ty) * Z;
+        // ez = +1: cells z0, z0+1 receive z0-1, z0; ez = -1: they receive z0+1, z0+2
+        S lo = ez_(i) > 0 ? row[zl] : row[z0 + 1], hi = ez_(i) > 0 ? row[z0] : row[zr];
+        if (zf0) lo = V::enc1(geq_zface(a, 0, i));
+        if (zf1) hi = V::enc1(geq_zface(a, 1, i));
+        __stcs((S2 *)(dp + corr(i) + of.st[i]), V::pack(lo, hi));
     }
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined persistent form of the bulk step (Z a multiple of 8): each CTA
+// walks row groups (R consecutive z-rows of one x-plane) with a stride of the
+// grid, and keeps the next groups' 19 population rows in flight as 1-D bulk
+// copies global -> shared (cp.async.bulk, completion on an mbarrier per
+// stage), so that loads stream while the CTA collides. All waits are bounded:
+// a wait that runs out sets bit 1 of the error word, waits (bounded) for the
+// copies still in flight into this CTA and returns.
+// ---------------------------------------------------------------------------
+constexpr int PIPE_NS = 3;                 // stages
+constexpr long long PIPE_WAIT = 1LL << 22;  // try_wait rounds before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(b))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity) {
+    for (long long k = 0; k < PIPE_WAIT; k++)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+
+struct PipeGeom {
+    int R, ngy, G;  // rows per group, groups per x-plane, groups
+};
+
+// queue the bulk copies of group j into stage buffer st (19 contiguous runs of
+// rows*Z elements, one per population)
+template <typename S>
+__device__ __forceinline__ void pipe_issue(const StepArgs &a, const PipeGeom &pg, int j, S *st, uint64_t *bar) {
+    const int x = j / pg.ngy, y0 = (j % pg.ngy) * pg.R;
+    const int rows = min(pg.R, a.Y - y0);
+    const unsigned bytes = (unsigned)(rows * a.Z * (int)sizeof(S));
+    const S *src = (const S *)a.src + (long long)a.Z * ((long long)y0 + (long long)a.Y * x);
+    mbar_arrive_tx(bar, bytes * Q);
+#pragma unroll 1
+    for (int i = 0; i < Q; i++) bulk_g2s(st + (long long)i * pg.R * a.Z, src + a.N * i, bytes, bar);
+}
+
+template <int P, int MODEL, bool FORCED>
+__global__ void __launch_bounds__(256, 2) k_step_pipe(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms, PipeGeom pg) {
+    using V = V2<P>;
+    using S2 = typename V::S2;
+    using S = typename V::S;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    const int Z = a.Z, Y = a.Y, X = a.X;
+    const int tz = threadIdx.x, ty = threadIdx.y, R = pg.R;
+    const int tid = ty * blockDim.x + tz;
+    const int z0 = 2 * tz;
+    const int RZ = R * Z;
+    S *stage = (S *)smraw;                       // [NS][19][R*Z]
+    S *zsm = stage + (long long)PIPE_NS * Q * RZ;  // [10][R][Z]
+    uint64_t *bar = (uint64_t *)(((uintptr_t)(zsm + 10 * RZ) + 7) & ~(uintptr_t)7);
+    const int N = (int)a.N;
+    const int stride = gridDim.x;
+
+    if (tid == 0) {
+        for (int s = 0; s < PIPE_NS; s++) mbar_init(bar + s, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < PIPE_NS; s++) {
+            const int j = blockIdx.x + s * stride;
+            if (j < pg.G) pipe_issue(a, pg, j, stage + (long long)s * Q * RZ, bar + s);
+        }
+    }
+
+    int it = 0;
+    for (int j = blockIdx.x; j < pg.G; j += stride, it++) {
+        const int s = it % PIPE_NS;
+        const unsigned par = (unsigned)((it / PIPE_NS) & 1);
+        const bool ok = mbar_wait(bar + s, par);
+        if (!__syncthreads_and(ok)) {
+            // drain: every copy queued for this CTA lands before it returns
+            if (tid == 0) {
+                atomicOr(a.kerr, 1);
+                for (int k = 0; k < PIPE_NS; k++) {
+                    const int jk = j + k * stride;
+                    if (jk < pg.G) mbar_wait(bar + (it + k) % PIPE_NS, (unsigned)(((it + k) / PIPE_NS) & 1));
+                }
+            }
+            return;
+        }
+        const int x = j / pg.ngy, y0 = (j % pg.ngy) * R;
+        const int y = y0 + ty;
+        const bool active = (y < Y);
+        const S *sb = stage + (long long)s * Q * RZ + ty * Z + z0;
+        float2 g[Q];
+#pragma unroll
+        for (int i = 0; i < Q; i++) g[i] = active ? V::dec(*(const S2 *)(sb + i * RZ)) : f2(0.0f);
+        __syncthreads();  // stage s is read; zsm of the previous group is free
+        if (tid == 0) {
+            const int jn = j + PIPE_NS * stride;
+            if (jn < pg.G) {
+                fence_proxy_async();
+                pipe_issue(a, pg, jn, stage + (long long)s * Q * RZ, bar + s);
+            }
+        }
+
+        float2 drho, rho, jx, jy, jz, u0, u1, u2;
+        macro2(g, drho, rho, jx, jy, jz);
+        const float2 F0 = f2(sc.vf[0]), F1 = f2(sc.vf[1]), F2 = f2(sc.vf[2]);
+        vel2<FORCED>(rho, jx, jy, jz, F0, F1, F2, 0.5f * sc.dh, u0, u1, u2);
+        collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
+
+        if (active) {
+#pragma unroll
+            for (int i = 0; i < Q; i++)
+                if (ez_(i) != 0) *(S2 *)(zsm + (zslot_(i) * R + ty) * Z + z0) = V::enc(g[i]);
+        }
+        __syncthreads();
+        if (active) {
+            const int c = z0 + Z * (y + Y * x);
+            const int ZY = Z * Y;
+            const int cyp = (y == Y - 1) ? -ZY : 0, cym = (y == 0) ? ZY : 0;
+            const int cxp = (x == X - 1) ? -N : 0, cxm = (x == 0) ? N : 0;
+            S *dp = (S *)a.dst + c;
+            const int zl = (z0 == 0) ? Z - 1 : z0 - 1, zr = (z0 + 2 == Z) ? 0 : z0 + 2;
+#pragma unroll
+            for (int i = 0; i < Q; i++) {
+                const int corr =
+                    (ey_(i) > 0 ? cyp : (ey_(i) < 0 ? cym : 0)) + (ex_(i) > 0 ? cxp : (ex_(i) < 0 ? cxm : 0));
+                S lo, hi;
+                if (ez_(i) == 0) {
+                    lo = V::lo(V::enc(g[i]));
+                    hi = V::hi(V::enc(g[i]));
+                } else {
+                    const S *row = zsm + (zslot_(i) * R + ty) * Z;
+                    lo = ez_(i) > 0 ? row[zl] : row[z0 + 1];
+                    hi = ez_(i) > 0 ? row[z0] : row[zr];
+                }
+                if (a.zeq[0] && z0 == 0) lo = V::enc1(geq_zface(a, 0, i));
+                if (a.zeq[1] && z0 + 1 == Z - 1) hi = V::enc1(geq_zface(a, 1, i));
+                __stcs((S2 *)(dp + corr + of.st[i]), V::pack(lo, hi));
+            }
+        }
+    }
+}
+
+template <int P>
+size_t pipe_smem(int R, int Z) {
+    using S = typename V2<P>::S;
+    return (size_t)(PIPE_NS * Q + 10) * R * Z * sizeof(S) + 16 + 8 * PIPE_NS;
+}
+
+// persistent grid of the pipelined kernel: co-resident CTAs on this device
+template <int P, int MODEL, bool FORCED>
+cudaError_t pipe_run(const StepArgs &a, const Offs<int> &of, const Scal<float> &sc, const MrtS &ms, int tpr, int R,
+                     cudaStream_t st) {
+    auto kern = k_step_pipe<P, MODEL, FORCED>;
+    const size_t smem = pipe_smem<P>(R, a.Z);
+    static int grid_cache[64][2] = {};  // per device: grid, smem it was sized for
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (grid_cache[dev][1] != (int)smem) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int nb = 0, sms = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, tpr * R, smem);
+        if (e != cudaSuccess) return e;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        if (nb < 1) return cudaErrorInvalidConfiguration;
+        grid_cache[dev][0] = nb * sms;
+        grid_cache[dev][1] = (int)smem;
+    }
+    PipeGeom pg;
+    pg.R = R;
+    pg.ngy = (a.Y + R - 1) / R;
+    pg.G = pg.ngy * a.X;
+    const int grid = std::min(grid_cache[dev][0], pg.G);
+    kern<<<grid, dim3(tpr, R), smem, st>>>(a, of, sc, ms, pg);
+    return cudaGetLastError();
 }
 
 // cell (x, y, z) of window cell wc
@@ -642,7 +1005,10 @@ __device__ __forceinline__ void push_cell(const StepArgs &a, int x, int y, int z
         yd = yd < 0 ? a.Y - 1 : (yd == a.Y ? 0 : yd);
         zd = zd < 0 ? a.Z - 1 : (zd == a.Z ? 0 : zd);
         const long long cd = (long long)zd + (long long)a.Z * ((long long)yd + (long long)a.Y * xd);
-        dst[cd + a.N * i] = V::enc1(getl(g[i], l));
+        float v = getl(g[i], l);
+        if (a.zeq[0] && zd == 0) v = geq_zface(a, 0, i);
+        if (a.zeq[1] && zd == a.Z - 1) v = geq_zface(a, 1, i);
+        dst[cd + a.N * i] = V::enc1(v);
     }
 }
 
@@ -779,8 +1145,18 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
             k_face_hook<P, MODEL><<<(unsigned)((n + 255) / 256), 128, 0, st>>>(a, sc, ms, k, A, B);
         }
     }
-    if (sc.forced) k_step_pair<P, MODEL, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
-    else k_step_pair<P, MODEL, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    // the pipelined persistent form (on request; it needs 16-byte aligned
+    // population rows) or the paired form
+    const bool pipe = a.variant == 2 && a.Z % 8 == 0;
+    if (pipe) {
+        cudaError_t e = sc.forced ? pipe_run<P, MODEL, true>(a, of, sc, ms, tpr, R, st)
+                                  : pipe_run<P, MODEL, false>(a, of, sc, ms, tpr, R, st);
+        if (e != cudaSuccess) return e;
+    } else if (sc.forced) {
+        k_step_pair<P, MODEL, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    } else {
+        k_step_pair<P, MODEL, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    }
     if (a.win.x1 >= a.win.x0 && a.win.n > 0)
         k_win_fix<P, MODEL><<<(unsigned)((a.win.n + 255) / 256), 128, 0, st>>>(a, sc, ms);
     return cudaGetLastError();
@@ -1117,7 +1493,7 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     for (int k = 0; k < 6; k++) hooks = hooks || a.hw[k] != nullptr || a.l2[k] != 0;
     // 32-bit element indices while all 19 populations fit
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
-    if (P != FSI_PREC_F64_FAST && (MODEL == 1 || mm->diag) && small && a.Z % 2 == 0 && a.Z <= 512)
+    if (step_fast_paired(a, mm, P, MODEL))
         return pair_launch<P == FSI_PREC_F64_FAST ? FSI_PREC_F32 : P, MODEL>(a, mm, hooks, st);
     if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
     return hooks ? step_launch<P, MODEL, true, long long>(a, m, st) : step_launch<P, MODEL, false, long long>(a, m, st);
@@ -1137,16 +1513,14 @@ __global__ void __launch_bounds__(256) k_bc_off(BcArgs a) {
     const int fa = blockIdx.x * blockDim.x + threadIdx.x;
     const int fb = blockIdx.y * blockDim.y + threadIdx.y;
     if (fa >= A || fb >= B) return;
+    if (FACE < 4 && (fa < a.zlo || fa > a.zhi)) return;
     S *f = (S *)a.f;
     const long long N = a.N;
     const long long c1 = face_cell(a, fa, fb, 0);
     auto ld = [&](long long c, int q) { return (float)T::dec(f[c + N * q]); };
     auto stq = [&](long long c, int q, float g) { f[c + N * q] = T::enc(g); };
-    // offset equilibrium g_eq = w (rho - 1) + w rho (3 eu + 4.5 eu^2 - 1.5 u^2)
     auto geq = [](int q, float rho, float u0, float u1, float u2, float k15) {
-        const float eu = (float)ex_(q) * u0 + (float)ey_(q) * u1 + (float)ez_(q) * u2;
-        const float w = (float)wt_(q);
-        return w * (rho - 1.0f) + (w * rho) * ((3.0f + 4.5f * eu) * eu - k15);
+        return geq_off(q, rho, u0, u1, u2, k15);
     };
     switch (a.code) {
     case BC_EQ: {
@@ -1269,6 +1643,11 @@ cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
     case FSI_PREC_BF16: { constexpr int PP = FSI_PREC_BF16; __VA_ARGS__; }         \
     default: return cudaErrorInvalidValue;                                         \
     }
+
+bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
+    const bool small = (long long)Q * a.N < (1LL << 31) - 1;
+    return prec != FSI_PREC_F64_FAST && (model == 1 || mm->diag) && small && a.Z % 2 == 0 && a.Z <= 512;
+}
 
 cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st) {
     if (model == 3) { FSI_DISPATCH(prec, return (step_inst<PP, 3>(a, mm, st))) }

@@ -120,6 +120,16 @@ int fsi_block_step(fsi_block_t h, const double vf[3], double blktime);
  * step, launched from a captured CUDA graph; *ms = device time (CUDA events) */
 int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps, float *ms);
 
+/* No counterpart in the reference: the bulk step kernel of the offset forms
+ * (FSI_PREC_F32/F16/BF16): the paired form (one group of z-rows per CTA,
+ * FSI_KERNEL_AUTO) or the pipelined persistent form (bulk copies into shared
+ * memory, zDim a multiple of 8). Both compute the same values, bitwise. The
+ * FP64 forms ignore it. */
+#define FSI_KERNEL_AUTO      0
+#define FSI_KERNEL_PAIRED    1
+#define FSI_KERNEL_PIPELINED 2
+int fsi_block_set_kernel(fsi_block_t h, int kernel);
+
 /* No counterpart in the reference: device time of the work a host loop
  * queues on the block's stream. stop = 0 records the start mark; stop = 1
  * records the end mark, waits for it and sets *ms to the time between. */

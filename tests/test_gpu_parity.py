@@ -50,6 +50,9 @@ BC_CASES = {
                            volumeForceAmp=1e-5, volumeForceFreq=0.1, volumeForcePhi=15.0),
     "zfaces": dict(bnd=(301, 301, 302, 302, 102, 104), uvwIn=(0.0, 0.0, 0.03)),
     "zhalfway": dict(bnd=(101, 104, 301, 301, 203, 204), uvwIn=(0.04, 0.0, 0.0), shearRateIn=(0.0, 0.0, 0.002)),
+    # uniform inflow on every face but x+: the paired kernels write the z faces
+    "box_inflow": dict(bnd=(101, 104, 101, 101, 101, 101), uvwIn=(0.05, 0.01, -0.005)),
+    "box_shear_z": dict(bnd=(103, 104, 302, 302, 101, 101), uvwIn=(0.04, 0.0, 0.0), shearRateIn=(0.0, 0.0, 0.002)),
 }
 
 
@@ -174,7 +177,8 @@ def test_mixed_forced_periodic(gpu_lib, dims, prec, tol, model):
 @pytest.mark.parametrize("model", [1, 3])
 @pytest.mark.parametrize("zdim", [20, 19])
 @pytest.mark.parametrize("prec,tol", [(F.PREC_F32, 1e-4), (F.PREC_F16, 5e-3), (F.PREC_BF16, 5e-2)])
-@pytest.mark.parametrize("name", ["neq_walls", "halfway", "zfaces", "zhalfway", "inflow_ext2"])
+@pytest.mark.parametrize("name", ["neq_walls", "halfway", "zfaces", "zhalfway", "inflow_ext2", "box_inflow",
+                                  "box_shear_z"])
 def test_mixed_boundaries(gpu_lib, name, prec, tol, zdim, model):
     # face hooks (half-way copies, 102 layer-2 planes) in both step kernels:
     # even z extent -> paired cells, odd -> one cell per thread
@@ -303,3 +307,48 @@ def test_large_block_initialise_is_ordered(gpu_lib, prec):
         assert np.all(den == den[0, 0, 0]) and abs(den[0, 0, 0] - 1.0) < 1e-3
         assert np.allclose(uuu[0], 0.05, rtol=0, atol=1e-3) and np.allclose(uuu[1], 0.01, rtol=0, atol=1e-3)
         b.close()
+
+
+# ------------------------------------------- pipelined vs paired bulk kernel
+
+@pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F16, F.PREC_BF16])
+@pytest.mark.parametrize("name", ["neq_walls", "zhalfway", "forced_channel"])
+def test_pipelined_equals_paired(gpu_lib, prec, model, name):
+    # the persistent bulk-copy pipeline computes the same values as the
+    # one-group-per-CTA form: bitwise equal states. 160 x 8 row groups
+    # (ragged last group) give every CTA several groups, so each pipeline
+    # stage is reused with both mbarrier phases.
+    dims = (160, 60, 64)
+    cfg = dict(BC_CASES[name])
+    cfg.pop("volumeForceIn", None)
+    for k in ("volumeForceAmp", "volumeForceFreq", "volumeForcePhi"):
+        cfg.pop(k, None)
+    bnd = cfg.pop("bnd")
+    blocks = []
+    for kern in (F.abi.KERNEL_PAIRED, F.abi.KERNEL_PIPELINED):
+        b = F.Block(*dims, bndConds=bnd, iCollidModel=model, nu=0.01, precision=prec, **cfg)
+        b.set_kernel(kern)
+        b.initialise(0.0)
+        b.set_boundary_conditions(0.0)
+        blocks.append(b)
+    vf = (2e-5, 0.0, 1e-6) if name == "forced_channel" else (0.0, 0.0, 0.0)
+    for s in range(5):
+        for b in blocks:
+            b.step(volumeForce=vf, blktime=s + 1.0)
+    fa, fb = blocks[0].download_f(), blocks[1].download_f()
+    assert np.array_equal(fa.view(np.uint64), fb.view(np.uint64)), first_diff(fa, fb)
+    # and from a captured graph
+    for b in blocks:
+        b.run(6, volumeForce=vf, blktime0=6.0)
+    fa, fb = blocks[0].download_f(), blocks[1].download_f()
+    assert np.array_equal(fa.view(np.uint64), fb.view(np.uint64)), first_diff(fa, fb)
+
+
+def test_pipelined_kernel_needs_aligned_rows(gpu_lib):
+    b = F.Block(16, 12, 10, precision=F.PREC_F16)
+    with pytest.raises(F.FsiError) as e:
+        b.set_kernel(F.abi.KERNEL_PIPELINED)
+    assert e.value.code == F.FSI_E_ARG
+    b.set_kernel(F.abi.KERNEL_PAIRED)
+    b.set_kernel(F.abi.KERNEL_AUTO)
