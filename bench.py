@@ -9,7 +9,8 @@ prescribed (rigid heave): the flexible plate of that case needs the
 reference's host-side structural solver, which stays outside the GPU path.
 One step = the IB stage (markers host -> device, the penalty loop to
 ntol = 5 / dtol = 1e-4 in one cooperative launch, the Lagrangian force
-device -> host) + the fused collide/stream kernel + the face kernels.
+device -> host) + the fused collide/stream kernel + the face kernels, through
+one fsi_block_ib_step call (the fluid step is queued behind the IB stage).
 Distributions are stored as FP16 offsets f - w_i, collision runs in FP32,
 the Lagrangian force in FP64.
 
@@ -204,9 +205,8 @@ def fsi_steps(b, plate, dh, t, n, forces=None):
     its = 0
     for _ in range(n):
         xyz, vel, area = plate.markers(t)
-        ef, it, res = b.ib_solve(xyz, vel, area, denIn=1.0, dt=dh, Uref=U, ntol=NTOL, dtol=DTOL)
+        ef, it, res = b.ib_step(xyz, vel, area, denIn=1.0, dt=dh, Uref=U, ntol=NTOL, dtol=DTOL, blktime=t + dh)
         t += dh
-        b.step(blktime=t)
         its += it
         if forces is not None:
             forces.append(force_coefficients(ef, 1.0, U, plate.area))

@@ -56,7 +56,7 @@ SYMBOLS = [
     "fsi_pair_father_to_son", "fsi_pair_son_to_father", "fsi_pair_father_to_son_static",
     "fsi_mlp_create", "fsi_mlp_destroy", "fsi_mlp_set_params", "fsi_mlp_get_params", "fsi_mlp_set_norm",
     "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_block_timer",
-    "fsi_block_set_kernel",
+    "fsi_block_set_kernel", "fsi_block_ib_step",
 ]
 KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
 # the warm-start perceptron (FSI_MLP_* in the header)
@@ -95,6 +95,8 @@ def load_library():
     L.fsi_block_run.argtypes = [VP, DP, C.c_double, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_timer.argtypes = [VP, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_set_kernel.argtypes = [VP, C.c_int]
+    L.fsi_block_ib_step.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
+                                    C.c_double, DP, IP, DP]
     L.fsi_ib_set_bodies.argtypes = [VP, C.c_int, IP, IP]
     L.fsi_ib_solve.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                DP, IP, DP]
@@ -303,6 +305,24 @@ class Block:
         _check(load_library().fsi_ib_solve(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(vf), denIn,
                                            self.dh if dt is None else dt, Uref, int(ntol), dtol,
                                            _dp(eforce), C.byref(it), C.byref(res)))
+        return eforce.reshape(-1, 3), it.value, res.value
+
+    def ib_step(self, xyz, vel, area, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0, ntol=3, dtol=1e-5,
+                blktime=0.0):
+        """ib_solve then step(volumeForce, blktime) in one call; returns
+        (eforce (Mtot,3), iterations, residual) while the fluid step runs"""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        area = np.ascontiguousarray(area, dtype=np.float64).reshape(-1)
+        if area.size != self.Mtot or xyz.size != 3 * self.Mtot or vel.size != 3 * self.Mtot:
+            raise ValueError("marker arrays do not match the bodies set with ib_set_bodies")
+        eforce = np.empty(3 * self.Mtot)
+        vf = _vec3(volumeForce)
+        it = C.c_int()
+        res = C.c_double()
+        _check(load_library().fsi_block_ib_step(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(vf), denIn,
+                                                self.dh if dt is None else dt, Uref, int(ntol), dtol, blktime,
+                                                _dp(eforce), C.byref(it), C.byref(res)))
         return eforce.reshape(-1, 3), it.value, res.value
 
     def ib_solve_warm(self, xyz, vel, area, aux=None, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0,

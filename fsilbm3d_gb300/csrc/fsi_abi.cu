@@ -138,7 +138,9 @@ struct fsi_block {
     double *hw[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int hw_ready[6] = {0, 0, 0, 0, 0, 0};
     cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_ib = nullptr;
+    double *h_ef = nullptr;  // pinned staging of the Lagrangian force (fsi_block_ib_step)
+    int h_ef_cap = 0;
     // immersed boundary
     int nb = 0, Mtot = 0;
     std::vector<int> M, offs;
@@ -300,10 +302,15 @@ int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_wind
                 u[1] = ((v.vin[1] + h->d.xmin * v.sr[0]) + 0.0 * v.sr[1]) + zc * v.sr[2];
                 u[2] = ((v.vin[2] + h->d.xmin * v.sr[0]) + h->d.ymin * v.sr[1]) + 0.0 * v.sr[2];
             }
+            // offset equilibrium of the face (calculate_distribution_funcion,
+            // FluidDomain.f90:1827-1834, minus the weight)
+            const double rho = h->d.denIn, usq = (u[0] * u[0] + u[1] * u[1]) + u[2] * u[2];
+            for (int q = 0; q < 19; q++) {
+                const double eu = (u[0] * ex_(q) + u[1] * ey_(q)) + u[2] * ez_(q);
+                a.zg[s][q] = (float)(wt_(q) * (rho - 1.0) + (wt_(q) * rho) * ((3.0 + 4.5 * eu) * eu - 1.5 * usq));
+            }
             a.zeq[s] = 1;
-            for (int c = 0; c < 3; c++) a.zu[s][c] = (float)u[c];
         }
-        a.den_in = (float)h->d.denIn;
     }
     cudaError_t e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
                                : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
@@ -338,6 +345,8 @@ void free_block(fsi_block *h) {
     if (h->h_stat) cudaFreeHost(h->h_stat);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->ev_ib) cudaEventDestroy(h->ev_ib);
+    if (h->h_ef) cudaFreeHost(h->h_ef);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }
@@ -420,6 +429,7 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     chk(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     chk(cudaEventCreate(&h->ev0));
     chk(cudaEventCreate(&h->ev1));
+    chk(cudaEventCreateWithFlags(&h->ev_ib, cudaEventDisableTiming));
     chk(cudaMalloc(&h->fa, fbytes));
     chk(cudaMalloc(&h->fb, fbytes));
     chk(cudaMalloc((void **)&h->den, sizeof(double) * h->N));
@@ -722,6 +732,10 @@ struct Warm {
     const fsi_mlp *mlp = nullptr;  // network of the warm start, or null
     bool aux = false;              // d_aux holds this call's auxiliary inputs
     float *features = nullptr;     // host (12,Mtot) out, or null
+    // queue the fluid step right behind the IB stage (fsi_block_ib_step)
+    bool step = false;
+    const double *step_vf = nullptr;
+    double step_time = 0.0;
 };
 
 int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol,
@@ -769,12 +783,34 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     long long need = std::max<long long>((h->Mtot + 7) / 8, (h->Nw + 255) / 256);
     const int grid = (int)std::max<long long>(1, std::min<long long>(need, h->coop_grid));
     CK(launch_ib_coop(a, h->prec, grid, h->st));
-    CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
-    if (wm.features)
-        CK(cudaMemcpyAsync(wm.features, h->d_feat, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
+    if (wm.step) {
+        // force, status and residual into pinned staging, then the fluid step
+        // behind them on the stream; the host waits for the copies only
+        if (h->h_ef_cap < h->Mtot) {
+            if (h->h_ef) cudaFreeHost(h->h_ef);
+            h->h_ef = nullptr;
+            h->h_ef_cap = 0;
+            CK(cudaHostAlloc((void **)&h->h_ef, sizeof(double) * 3 * h->Mtot, cudaHostAllocDefault));
+            h->h_ef_cap = h->Mtot;
+        }
+        CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaEventRecord(h->ev_ib, h->st));
+        h->win_valid = true;
+        int rc = enqueue_step(h, wm.step_vf, wm.step_time, true);
+        h->win_valid = false;
+        if (rc) return rc;
+        CK(cudaEventSynchronize(h->ev_ib));
+        memcpy(eforce, h->h_ef, sizeof(double) * 3 * h->Mtot);
+    } else {
+        CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
+        if (wm.features)
+            CK(cudaMemcpyAsync(wm.features, h->d_feat, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
     if (h->h_stat[4]) return fail(FSI_E_TIMEOUT, "step kernel: a bounded wait ran out");
     const int st = h->h_stat[0];
     if (st & 1) return fail(FSI_E_RANGE, "index out of block bounds in IB stencil");
@@ -784,7 +820,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     const int it = h->h_stat[1];
     if (iters) *iters = it;
     if (residual) *residual = h->h_tol[0];
-    h->win_valid = true;
+    h->win_valid = !wm.step;
     return FSI_OK;
 }
 
@@ -898,6 +934,28 @@ int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const
     wm.mlp = warm;
     wm.aux = aux != nullptr;
     wm.features = features;
+    return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
+}
+
+int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
+                      double denIn, double dt, double Uref, int ntol, double dtol, double blktime, double *eforce,
+                      int *iters, double *residual) {
+    if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    if (h->prec == FSI_PREC_F64 || h->nb == 0 || h->Mtot == 0) {
+        int rc = fsi_ib_solve(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, eforce, iters, residual);
+        if (rc) return rc;
+        return fsi_block_step(h, vf, blktime);
+    }
+    h->win_valid = false;
+    if (iters) *iters = 0;
+    if (residual) *residual = 0.0;
+    if (!xyz || !vel || !area || !eforce) return fail(FSI_E_ARG, "null marker array");
+    int rc = ib_upload(h, xyz, vel, area);
+    if (rc) return rc;
+    Warm wm;
+    wm.step = true;
+    wm.step_vf = vf;
+    wm.step_time = blktime;
     return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
 }
 

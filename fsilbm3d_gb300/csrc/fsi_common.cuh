@@ -123,11 +123,11 @@ struct StepArgs {
     int *kerr;            // error word of the pipelined kernel (bit 1: a bounded wait ran out)
     int variant;          // bulk kernel of the offset forms: 0 auto, 1 paired, 2 pipelined
     // z- / z+ faces of code 101 with a uniform face velocity, written by the
-    // paired step kernels themselves (the equilibrium at the face velocity);
-    // set only when the host leaves those faces out of the face kernels
+    // paired step kernels themselves: zg holds the 19 offset equilibrium
+    // populations g = feq(denIn, u_face) - w of the face; set only when the
+    // host leaves those faces out of the face kernels
     int zeq[2];
-    float zu[2][3];
-    float den_in;
+    float zg[2][19];
 };
 
 struct BcArgs {

@@ -92,10 +92,7 @@ __device__ __forceinline__ float geq_off(int q, float rho, float u0, float u1, f
     const float w = (float)wt_(q);
     return w * (rho - 1.0f) + (w * rho) * ((3.0f + 4.5f * eu) * eu - k15);
 }
-__device__ __forceinline__ float geq_zface(const StepArgs &a, int side, int q) {
-    const float u0 = a.zu[side][0], u1 = a.zu[side][1], u2 = a.zu[side][2];
-    return geq_off(q, a.den_in, u0, u1, u2, 1.5f * (u0 * u0 + u1 * u1 + u2 * u2));
-}
+__device__ __forceinline__ float geq_zface(const StepArgs &a, int side, int q) { return a.zg[side][q]; }
 
 // density (and its offset from 1) and velocity of one cell,
 // calculate_macro_quantities_ (FluidDomain.f90:1136-1139) regrouped
@@ -757,10 +754,21 @@ k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
         // SRT: stored pair by pair, so that the 64-register budget holds
         collide_emit<MODEL, FORCED, false>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit);
     } else {
-        // MRT: all 19 collided first (measured faster at two CTAs per SM)
+        // MRT: all 19 collided first, then stored under one branch
         collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
+        if (active) {
 #pragma unroll
-        for (int i = 0; i < Q; i++) emit(i, g[i]);
+            for (int i = 0; i < Q; i++) {
+                float2 v = g[i];
+                if (ez_(i) == 0) {
+                    if (zf0) v.x = geq_zface(a, 0, i);
+                    if (zf1) v.y = geq_zface(a, 1, i);
+                    __stcs((S2 *)(dp + corr(i) + of.st[i]), V::enc(v));
+                } else {
+                    *(S2 *)(sm + (zslot_(i) * R + ty) * Z + z0) = V::enc(v);
+                }
+            }
+        }
     }
     __syncthreads();
     if (!active) return;

@@ -150,6 +150,17 @@ int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const doub
                  const double vf[3], double denIn, double dt, double Uref,
                  int ntol, double dtol, double *eforce, int *iters, double *residual);
 
+/* fsi_ib_solve followed by fsi_block_step(h, vf, blktime), the order of one
+ * step in LBMBlockComm.f90:279-305. For the fast forms the fluid step is
+ * queued behind the IB stage on the block's stream and the call returns as
+ * soon as the Lagrangian force has reached the host, while the step runs;
+ * the IB window of this solve is used by that step only. (If the IB stage
+ * fails, the step has been queued on its result: the state must be discarded
+ * with the error.) FSI_PREC_F64 runs the two calls one after the other. */
+int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const double *area,
+                      const double vf[3], double denIn, double dt, double Uref, int ntol,
+                      double dtol, double blktime, double *eforce, int *iters, double *residual);
+
 /* the stencil of the last fsi_ib_solve: v_Ei (12,Mtot) 1-based, v_Ew (12,Mtot) */
 int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew);
 

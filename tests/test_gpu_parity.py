@@ -352,3 +352,26 @@ def test_pipelined_kernel_needs_aligned_rows(gpu_lib):
     assert e.value.code == F.FSI_E_ARG
     b.set_kernel(F.abi.KERNEL_PAIRED)
     b.set_kernel(F.abi.KERNEL_AUTO)
+
+
+@pytest.mark.parametrize("prec,tol", [(F.PREC_F64, 0.0), (F.PREC_F64_FAST, 1e-12), (F.PREC_F32, 1e-6)])
+def test_ib_step_equals_solve_then_step(gpu_lib, prec, tol):
+    dims = (40, 24, 20)
+    blocks = []
+    plate = plate_in(dims, n=5, heave=1.0, freq=0.02)
+    for _ in range(2):
+        b = F.Block(*dims, bndConds=(101, 104, 101, 101, 101, 101), iCollidModel=3, nu=0.02, precision=prec,
+                    uvwIn=(0.05, 0.0, 0.0))
+        b.initialise(0.0)
+        b.set_boundary_conditions(0.0)
+        b.ib_set_bodies([plate.M])
+        blocks.append(b)
+    for s in range(4):
+        xyz, vel, area = plate.markers(float(s))
+        e0, i0, r0 = blocks[0].ib_solve(xyz, vel, area, Uref=0.05, ntol=4, dtol=1e-12)
+        blocks[0].step(blktime=s + 1.0)
+        e1, i1, r1 = blocks[1].ib_step(xyz, vel, area, Uref=0.05, ntol=4, dtol=1e-12, blktime=s + 1.0)
+        assert i0 == i1
+        assert np.max(np.abs(e1 - e0)) <= tol * np.max(np.abs(e0))
+    f0, f1 = blocks[0].download_f(), blocks[1].download_f()
+    assert np.max(np.abs(f1 - f0)) <= tol * np.max(np.abs(f0))
