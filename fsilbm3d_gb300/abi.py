@@ -57,6 +57,7 @@ SYMBOLS = [
     "fsi_mlp_create", "fsi_mlp_destroy", "fsi_mlp_set_params", "fsi_mlp_get_params", "fsi_mlp_set_norm",
     "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_block_timer",
     "fsi_block_set_kernel", "fsi_block_ib_step",
+    "fsi_batch_create", "fsi_batch_destroy", "fsi_batch_ib_step", "fsi_batch_tune", "fsi_batch_set_threads",
 ]
 KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
 # the warm-start perceptron (FSI_MLP_* in the header)
@@ -95,6 +96,11 @@ def load_library():
     L.fsi_block_run.argtypes = [VP, DP, C.c_double, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_timer.argtypes = [VP, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_set_kernel.argtypes = [VP, C.c_int]
+    L.fsi_batch_create.argtypes = [C.POINTER(VP), C.c_int, C.POINTER(VP)]
+    L.fsi_batch_destroy.argtypes = [VP]
+    L.fsi_batch_ib_step.argtypes = [VP, DP, DP, DP, DP, DP, DP, DP, C.c_int, C.c_double, DP, DP, IP, DP]
+    L.fsi_batch_tune.argtypes = [VP, C.c_int, IP, C.POINTER(C.c_float)]
+    L.fsi_batch_set_threads.argtypes = [VP, C.c_int]
     L.fsi_block_ib_step.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                     C.c_double, DP, IP, DP]
     L.fsi_ib_set_bodies.argtypes = [VP, C.c_int, IP, IP]
@@ -479,3 +485,71 @@ class Mlp:
         _check(load_library().fsi_mlp_train(self.h, _fp(X), _fp(Y), int(X.shape[0]), int(epochs), int(batch),
                                             C.c_float(lr), C.c_ulonglong(seed), _fp(hist)))
         return hist
+
+
+class Batch:
+    """Many independent blocks stepped together (one CUDA graph per step):
+    each step is the IB stage of every block then its fluid step."""
+
+    def __init__(self, blocks):
+        self.blocks = list(blocks)
+        arr = (C.c_void_p * len(self.blocks))(*[b.h for b in self.blocks])
+        h = C.c_void_p()
+        _check(load_library().fsi_batch_create(C.byref(h), len(self.blocks), arr))
+        self.h = h
+        self.M = [b.Mtot for b in self.blocks]
+        self.moff = np.concatenate([[0], np.cumsum(self.M)]).astype(int)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().fsi_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ib_step(self, markers, vf=None, denIn=None, dt=None, Uref=None, ntol=3, dtol=1e-5, blktime=None):
+        """markers: one (xyz, vel, area) per block (None for a block without
+        bodies). Returns (list of eforce (M,3), iterations (n,), residual (n,))."""
+        n = len(self.blocks)
+        Mall = int(self.moff[-1])
+        xyz = np.zeros(3 * max(Mall, 1))
+        vel = np.zeros(3 * max(Mall, 1))
+        area = np.zeros(max(Mall, 1))
+        for c, mk in enumerate(markers):
+            if self.M[c] == 0:
+                continue
+            m0, m1 = self.moff[c], self.moff[c + 1]
+            xyz[3 * m0:3 * m1] = np.asarray(mk[0], dtype=np.float64).reshape(-1)
+            vel[3 * m0:3 * m1] = np.asarray(mk[1], dtype=np.float64).reshape(-1)
+            area[m0:m1] = np.asarray(mk[2], dtype=np.float64).reshape(-1)
+        def per(v, default):
+            a = np.full(n, default, dtype=np.float64) if v is None else np.asarray(v, dtype=np.float64)
+            return np.ascontiguousarray(np.broadcast_to(a, (n,)))
+        vfa = np.zeros(3 * n) if vf is None else np.ascontiguousarray(np.asarray(vf, dtype=np.float64).reshape(-1))
+        den = per(denIn, 1.0)
+        dta = np.ascontiguousarray(np.array([b.dh for b in self.blocks]) if dt is None else per(dt, 1.0))
+        ur = per(Uref, 1.0)
+        bt = per(blktime, 0.0)
+        ef = np.empty(3 * max(Mall, 1))
+        its = np.zeros(n, dtype=np.int32)
+        res = np.zeros(n)
+        IPt = C.POINTER(C.c_int)
+        _check(load_library().fsi_batch_ib_step(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(vfa), _dp(den), _dp(dta),
+                                                _dp(ur), int(ntol), dtol, _dp(bt), _dp(ef), its.ctypes.data_as(IPt),
+                                                _dp(res)))
+        out = [ef[3 * self.moff[c]:3 * self.moff[c + 1]].reshape(-1, 3).copy() for c in range(n)]
+        return out, its, res
+
+    def tune(self, reps=10):
+        """autotune the bulk kernel's CTA size; returns (threads, ms per step)"""
+        t = C.c_int()
+        ms = C.c_float()
+        _check(load_library().fsi_batch_tune(self.h, int(reps), C.byref(t), C.byref(ms)))
+        return t.value, ms.value
+
+    def set_threads(self, threads):
+        _check(load_library().fsi_batch_set_threads(self.h, int(threads)))

@@ -227,39 +227,49 @@ void face_dims(const fsi_block *h, int k, int &A, int &B) {
     B = (ax == 0) ? h->Y : h->X;
 }
 
-// zdone[s]: the step kernel already wrote z face 4+s (its x/y faces then
-// leave that plane alone, so that the z face stays the last writer there)
-int apply_bcs(fsi_block *h, void *f, double blktime, const int zdone[2] = nullptr) {
+// The arguments of face k's kernel on buffer f; false when face k has no
+// kernel (periodic, fluid, a z face the step kernel wrote, or a half-way face
+// on its first call). zdone[s]: the step kernel already wrote z face 4+s (the
+// x/y faces then leave that plane alone, so that the z face stays the last
+// writer there).
+bool fill_bc(fsi_block *h, int k, void *f, double blktime, const int zdone[2], BcArgs &a) {
     const int zd0 = zdone ? zdone[0] : 0, zd1 = zdone ? zdone[1] : 0;
+    int code = h->d.bndConds[k];
+    if (code == BC_PERIODIC || code == BC_FLUID || code == BC_FLUID_FATHER) return false;
+    if ((k == 4 && zd0) || (k == 5 && zd1)) return false;
+    if (code == BC_WALL_HW || code == BC_MWALL_HW) {
+        // allocate-on-first-call semantics, FluidDomain.f90:660-662
+        if (!h->hw_ready[k]) { h->hw_ready[k] = 1; return false; }
+    }
+    a = BcArgs{};
+    a.f = f;
+    a.X = h->X; a.Y = h->Y; a.Z = h->Z; a.N = h->N;
+    a.face = k; a.code = code;
+    a.dh = h->d.dh; a.xmin = h->d.xmin; a.ymin = h->d.ymin; a.zmin = h->d.zmin;
+    a.xmax = h->xmax; a.ymax = h->ymax; a.zmax = h->zmax;
+    a.denIn = h->d.denIn;
+    a.vel = make_vel(h, blktime);
+    a.hw = h->hw[k];
+    a.den = h->den;
+    a.u = h->u;
+    a.zlo = zd0 ? 1 : 0;
+    a.zhi = h->Z - 1 - (zd1 ? 1 : 0);
+    return true;
+}
+
+int apply_bcs(fsi_block *h, void *f, double blktime, const int zdone[2] = nullptr) {
     for (int k = 0; k < 6; k++) {
-        int code = h->d.bndConds[k];
-        if (code == BC_PERIODIC || code == BC_FLUID || code == BC_FLUID_FATHER) continue;
-        if ((k == 4 && zd0) || (k == 5 && zd1)) continue;
-        if (code == BC_WALL_HW || code == BC_MWALL_HW) {
-            // allocate-on-first-call semantics, FluidDomain.f90:660-662
-            if (!h->hw_ready[k]) { h->hw_ready[k] = 1; continue; }
-        }
-        BcArgs a{};
-        a.f = f;
-        a.X = h->X; a.Y = h->Y; a.Z = h->Z; a.N = h->N;
-        a.face = k; a.code = code;
-        a.dh = h->d.dh; a.xmin = h->d.xmin; a.ymin = h->d.ymin; a.zmin = h->d.zmin;
-        a.xmax = h->xmax; a.ymax = h->ymax; a.zmax = h->zmax;
-        a.denIn = h->d.denIn;
-        a.vel = make_vel(h, blktime);
-        a.hw = h->hw[k];
-        a.den = h->den;
-        a.u = h->u;
-        a.zlo = zd0 ? 1 : 0;
-        a.zhi = h->Z - 1 - (zd1 ? 1 : 0);
+        BcArgs a;
+        if (!fill_bc(h, k, f, blktime, zdone, a)) continue;
         cudaError_t e = is_fast(h) ? launch_bc_fast(a, h->prec, h->st) : launch_bc_f64(a, h->st);
         if (e != cudaSuccess) return fail(FSI_E_CUDA, "boundary kernel: %s", cudaGetErrorString(e));
     }
     return FSI_OK;
 }
 
-int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_window) {
-    StepArgs a{};
+// the arguments of one fluid step of h (fa -> fb)
+void fill_step(fsi_block *h, const double vf[3], double blktime, bool use_window, StepArgs &a) {
+    a = StepArgs{};
     a.src = h->fa;
     a.dst = h->fb;
     a.X = h->X; a.Y = h->Y; a.Z = h->Z; a.N = h->N;
@@ -312,6 +322,11 @@ int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_wind
             a.zeq[s] = 1;
         }
     }
+}
+
+int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_window) {
+    StepArgs a;
+    fill_step(h, vf, blktime, use_window, a);
     cudaError_t e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
                                : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
     if (e != cudaSuccess) return fail(FSI_E_CUDA, "step kernel: %s", cudaGetErrorString(e));
@@ -738,20 +753,11 @@ struct Warm {
     double step_time = 0.0;
 };
 
-int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol,
-                  const Warm &wm, double *eforce, int *iters, double *residual) {
-    if (!h->coop_grid) {
-        h->coop_grid = ib_coop_grid(h->prec);
-        if (h->coop_grid <= 0) return fail(FSI_E_CUDA, "no co-resident grid for the IB kernel");
-    }
-    if (ntol > h->tolacc_cap) {
-        if (h->d_tolacc) cudaFree(h->d_tolacc);
-        h->tolacc_cap = std::max(ntol, 64);
-        CK(cudaMalloc((void **)&h->d_tolacc, sizeof(double) * h->tolacc_cap));
-    }
-    CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 4, h->st));
+// the IB stage's arguments for block h after compute_window (its own marker,
+// force, status and residual arrays)
+void fill_ib(fsi_block *h, const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol, IbCoop &a) {
     const double ih = 1.0 / h->d.dh;
-    IbCoop a{};
+    a = IbCoop{};
     a.g = h->geom;
     a.N = h->N;
     a.Nw = h->Nw;
@@ -772,6 +778,23 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     a.tol_acc = h->d_tolacc;
     a.status = h->d_status;
     a.res = h->d_res;
+    a.Uref = Uref;
+}
+
+int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol,
+                  const Warm &wm, double *eforce, int *iters, double *residual) {
+    if (!h->coop_grid) {
+        h->coop_grid = ib_coop_grid(h->prec);
+        if (h->coop_grid <= 0) return fail(FSI_E_CUDA, "no co-resident grid for the IB kernel");
+    }
+    if (ntol > h->tolacc_cap) {
+        if (h->d_tolacc) cudaFree(h->d_tolacc);
+        h->tolacc_cap = std::max(ntol, 64);
+        CK(cudaMalloc((void **)&h->d_tolacc, sizeof(double) * h->tolacc_cap));
+    }
+    CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 4, h->st));
+    IbCoop a;
+    fill_ib(h, vf, denIn, dt, Uref, ntol, dtol, a);
     a.mlp = wm.mlp ? wm.mlp->P : nullptr;
     a.mlp_nrm = wm.mlp ? wm.mlp->nrm : nullptr;
     a.aux = wm.aux ? h->d_aux : nullptr;
@@ -1329,6 +1352,341 @@ int fsi_mlp_train(fsi_mlp_t m, const float *x, const float *y, int n, int epochs
     if (loss_per_epoch)
         for (int e = 0; e < epochs; e++) loss_per_epoch[e] = hl[e] / (float)nbatch;
     return FSI_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------- batched blocks
+// Many independent blocks stepped together: per step one upload of every
+// block's tables and markers, one launch of the IB stage of all blocks (one
+// CTA each), one launch of the bulk step of all blocks, one of their window
+// fix-ups, one per face index, and one download of every force and status;
+// captured once as a CUDA graph and replayed.
+
+struct fsi_batch {
+    int n = 0;
+    std::vector<fsi_block *> blk;
+    int prec = 0, model = 1;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int threads = BATCH_THREADS[0];  // bulk kernel CTA size (the autotuner's choice)
+    std::vector<int> moff;           // first packed marker of each block (n+1)
+    int Mall = 0;
+    int ntol_cap = 0;
+    // one device region and its pinned mirror: [BatchCase n][IbCoop n][BcArgs 6n][xyz 3M][vel 3M][area M]
+    size_t off_ib = 0, off_bc = 0, off_mk = 0, in_bytes = 0;
+    unsigned char *d_in = nullptr, *h_in = nullptr;
+    double *d_ef = nullptr, *h_ef = nullptr;  // 3M
+    int *d_stat = nullptr, *h_stat = nullptr;  // 8 per block
+    double *d_res = nullptr, *h_res = nullptr;  // per block
+    double *d_tol = nullptr;                    // ntol_cap per block
+    bool face_on[6] = {false, false, false, false, false, false};
+    int Amax[6] = {0, 0, 0, 0, 0, 0}, Bmax[6] = {0, 0, 0, 0, 0, 0};
+    cudaGraphExec_t gexec = nullptr;
+    int g_threads = 0, g_ntol = 0;
+    long long g_wmax = -1;
+    bool g_forced = false;
+};
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+void free_batch(fsi_batch *b) {
+    if (!b) return;
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    void *dp[] = {b->d_in, b->d_ef, b->d_stat, b->d_res, b->d_tol};
+    for (void *p : dp)
+        if (p) cudaFree(p);
+    void *hp[] = {b->h_in, b->h_ef, b->h_stat, b->h_res};
+    for (void *p : hp)
+        if (p) cudaFreeHost(p);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+// row groups of every block for CTAs of T threads; returns the total
+int batch_groups(fsi_batch *b, int T, BatchCase *cs) {
+    int g0 = 0;
+    for (int c = 0; c < b->n; c++) {
+        const fsi_block *h = b->blk[c];
+        const int tpr = h->Z / 2;
+        const int R = std::max(1, T / tpr);
+        cs[c].tpr = tpr;
+        cs[c].R = R;
+        cs[c].ngy = (h->Y + R - 1) / R;
+        cs[c].g0 = g0;
+        g0 += cs[c].ngy * h->X;
+    }
+    return g0;
+}
+
+// the bulk step tables of every block (fa -> fb) into the staging area
+void batch_fill_steps(fsi_batch *b, const double *vf, const double *blktime, bool use_window) {
+    BatchCase *cs = (BatchCase *)b->h_in;
+    for (int c = 0; c < b->n; c++) {
+        fsi_block *h = b->blk[c];
+        fill_step(h, vf + 3 * c, blktime[c], use_window, cs[c].a);
+        for (int k = 0; k < 19; k++) cs[c].sd[k] = (float)h->mm.sd[k];
+    }
+}
+
+int batch_capture(fsi_batch *b, int G, long long wmax, bool forced) {
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemcpyAsync(b->d_in, b->h_in, b->in_bytes, cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_stat, 0, sizeof(int) * 8 * b->n, b->st);
+    if (e == cudaSuccess) e = launch_batch_ib((const IbCoop *)(b->d_in + b->off_ib), b->n, 512, b->prec, b->st);
+    if (e == cudaSuccess)
+        e = launch_batch_step((const BatchCase *)b->d_in, b->n, G, b->threads, wmax, b->prec, b->model, forced, b->st);
+    for (int k = 0; k < 6 && e == cudaSuccess; k++)
+        if (b->face_on[k])
+            e = launch_batch_bc((const BcArgs *)(b->d_in + b->off_bc) + (size_t)k * b->n, b->n, k, b->Amax[k],
+                                b->Bmax[k], b->prec, b->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->h_ef, b->d_ef, sizeof(double) * 3 * std::max(1, b->Mall), cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->h_stat, b->d_stat, sizeof(int) * 8 * b->n, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->h_res, b->d_res, sizeof(double) * b->n, cudaMemcpyDeviceToHost, b->st);
+    cudaError_t ce = cudaStreamEndCapture(b->st, &g);
+    if (e != cudaSuccess) return fail(FSI_E_CUDA, "batch capture: %s", cudaGetErrorString(e));
+    if (ce != cudaSuccess) return fail(FSI_E_CUDA, "batch capture: %s", cudaGetErrorString(ce));
+    e = cudaGraphInstantiate(&b->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(FSI_E_CUDA, "batch graph: %s", cudaGetErrorString(e));
+    b->g_threads = b->threads;
+    b->g_wmax = wmax;
+    b->g_forced = forced;
+    b->g_ntol = b->ntol_cap;
+    return FSI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
+    if (!out || n <= 0 || !blocks) return fail(FSI_E_ARG, "invalid argument");
+    *out = nullptr;
+    for (int c = 0; c < n; c++) {
+        fsi_block *h = blocks[c];
+        if (!h) return fail(FSI_E_ARG, "block %d is null", c);
+        if (h->prec != FSI_PREC_F32 && h->prec != FSI_PREC_F16 && h->prec != FSI_PREC_BF16)
+            return fail(FSI_E_ARG, "block %d: batches take the offset storage forms (F32, F16, BF16)", c);
+        if (h->prec != blocks[0]->prec || h->d.iCollidModel != blocks[0]->d.iCollidModel)
+            return fail(FSI_E_ARG, "block %d: all blocks of a batch share the storage form and collision model", c);
+        StepArgs a;
+        double z3[3] = {0, 0, 0};
+        fill_step(h, z3, 0.0, false, a);
+        if (!step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel) || h->Z / 2 > 512)
+            return fail(FSI_E_ARG, "block %d: needs the paired kernels (even zDim <= 1024, diagonal MRT)", c);
+        for (int k = 0; k < 6; k++) {
+            const int code = h->d.bndConds[k];
+            if (code == BC_NEQ || code == BC_WALL_HW || code == BC_MWALL_HW || code == BC_FLUID ||
+                code == BC_FLUID_FATHER)
+                return fail(FSI_E_ARG, "block %d face %d: code %d is not supported in a batch", c, k, code);
+        }
+        for (int c2 = 0; c2 < c; c2++)
+            if (blocks[c2] == h) return fail(FSI_E_ARG, "block %d appears twice", c);
+    }
+    fsi_batch *b = new fsi_batch;
+    b->n = n;
+    b->blk.assign(blocks, blocks + n);
+    b->prec = blocks[0]->prec;
+    b->model = blocks[0]->d.iCollidModel;
+    b->moff.assign(n + 1, 0);
+    for (int c = 0; c < n; c++) b->moff[c + 1] = b->moff[c] + b->blk[c]->Mtot;
+    b->Mall = b->moff[n];
+    for (int c = 0; c < n; c++) {
+        const fsi_block *h = b->blk[c];
+        for (int k = 0; k < 6; k++) {
+            const int code = h->d.bndConds[k];
+            if (code == BC_PERIODIC) continue;
+            b->face_on[k] = true;
+            const int ax = k >> 1;
+            b->Amax[k] = std::max(b->Amax[k], ax < 2 ? h->Z : h->Y);
+            b->Bmax[k] = std::max(b->Bmax[k], ax == 0 ? h->Y : h->X);
+        }
+    }
+    const int Mt = std::max(1, b->Mall);
+    b->off_ib = align256(sizeof(BatchCase) * n);
+    b->off_bc = b->off_ib + align256(sizeof(IbCoop) * n);
+    b->off_mk = b->off_bc + align256(sizeof(BcArgs) * 6 * n);
+    b->in_bytes = b->off_mk + sizeof(double) * 7 * Mt;
+    auto bail = [&](cudaError_t e) {
+        free_batch(b);
+        return fail(FSI_E_CUDA, "batch allocation: %s", cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreate(&b->ev1)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc((void **)&b->d_in, b->in_bytes)) != cudaSuccess) return bail(e);
+    if ((e = cudaHostAlloc((void **)&b->h_in, b->in_bytes, cudaHostAllocDefault)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc((void **)&b->d_ef, sizeof(double) * 3 * Mt)) != cudaSuccess) return bail(e);
+    if ((e = cudaHostAlloc((void **)&b->h_ef, sizeof(double) * 3 * Mt, cudaHostAllocDefault)) != cudaSuccess)
+        return bail(e);
+    if ((e = cudaMalloc((void **)&b->d_stat, sizeof(int) * 8 * n)) != cudaSuccess) return bail(e);
+    if ((e = cudaHostAlloc((void **)&b->h_stat, sizeof(int) * 8 * n, cudaHostAllocDefault)) != cudaSuccess)
+        return bail(e);
+    if ((e = cudaMalloc((void **)&b->d_res, sizeof(double) * n)) != cudaSuccess) return bail(e);
+    if ((e = cudaHostAlloc((void **)&b->h_res, sizeof(double) * n, cudaHostAllocDefault)) != cudaSuccess)
+        return bail(e);
+    memset(b->h_in, 0, b->in_bytes);
+    // the blocks' own queued work finishes before the batch takes them over
+    for (int c = 0; c < n; c++)
+        if ((e = cudaStreamSynchronize(b->blk[c]->st)) != cudaSuccess) return bail(e);
+    *out = b;
+    return FSI_OK;
+}
+
+int fsi_batch_destroy(fsi_batch_t b) {
+    if (!b) return FSI_OK;
+    cudaStreamSynchronize(b->st);
+    free_batch(b);
+    return FSI_OK;
+}
+
+int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const double *area, const double *vf,
+                      const double *denIn, const double *dt, const double *Uref, int ntol, double dtol,
+                      const double *blktime, double *eforce, int *iters, double *residual) {
+    if (!b || !vf || !denIn || !dt || !Uref || !blktime || ntol < 0) return fail(FSI_E_ARG, "null argument");
+    if (b->Mall > 0 && (!xyz || !vel || !area || !eforce)) return fail(FSI_E_ARG, "null marker array");
+    const int n = b->n;
+    // the penalty residual sums of every block
+    if (ntol > b->ntol_cap) {
+        CK(cudaStreamSynchronize(b->st));
+        if (b->d_tol) cudaFree(b->d_tol);
+        b->d_tol = nullptr;
+        b->ntol_cap = 0;
+        const int cap = std::max(ntol, 64);
+        CK(cudaMalloc((void **)&b->d_tol, sizeof(double) * cap * n));
+        b->ntol_cap = cap;
+    }
+    // windows (host, from the markers) and the tables
+    long long wmax = 0;
+    bool forced = false;
+    BatchCase *cs = (BatchCase *)b->h_in;
+    IbCoop *ib = (IbCoop *)(b->h_in + b->off_ib);
+    BcArgs *bc = (BcArgs *)(b->h_in + b->off_bc);
+    double *mk = (double *)(b->h_in + b->off_mk);
+    double *dmk = (double *)(b->d_in + b->off_mk);
+    const int Mt = std::max(1, b->Mall);
+    for (int c = 0; c < n; c++) {
+        fsi_block *h = b->blk[c];
+        const int m0 = b->moff[c];
+        h->win_valid = false;
+        if (h->Mtot > 0) {
+            int rc = compute_window(h, xyz + 3LL * m0);
+            if (rc) return fail(rc, "block %d: %s", c, g_err.c_str());
+            h->win_valid = true;
+            wmax = std::max(wmax, h->Nw_cap);
+        }
+        for (int k = 0; k < 3; k++) forced = forced || vf[3 * c + k] != 0.0;
+        fill_step(h, vf + 3 * c, blktime[c], h->Mtot > 0, cs[c].a);
+        for (int k = 0; k < 19; k++) cs[c].sd[k] = (float)h->mm.sd[k];
+        if (h->Mtot > 0) {
+            fill_ib(h, vf + 3 * c, denIn[c], dt[c], Uref[c], ntol, dtol, ib[c]);
+            ib[c].xyz = dmk + 3LL * m0;
+            ib[c].vel = dmk + 3LL * Mt + 3LL * m0;
+            ib[c].area = dmk + 6LL * Mt + m0;
+            ib[c].eforce = b->d_ef + 3LL * m0;
+            ib[c].tol_acc = b->d_tol + (size_t)b->ntol_cap * c;
+            ib[c].status = b->d_stat + 8 * c;
+            ib[c].res = b->d_res + c;
+        } else {
+            ib[c] = IbCoop{};
+        }
+        for (int k = 0; k < 6; k++) {
+            BcArgs a;
+            if (fill_bc(h, k, h->fb, blktime[c], cs[c].a.zeq, a)) bc[(size_t)k * n + c] = a;
+            else {
+                bc[(size_t)k * n + c] = BcArgs{};
+                bc[(size_t)k * n + c].code = BC_FLUID;
+            }
+        }
+    }
+    const int G = batch_groups(b, b->threads, cs);
+    if (b->Mall > 0) {
+        memcpy(mk, xyz, sizeof(double) * 3 * b->Mall);
+        memcpy(mk + 3LL * Mt, vel, sizeof(double) * 3 * b->Mall);
+        memcpy(mk + 6LL * Mt, area, sizeof(double) * b->Mall);
+    }
+    if (!b->gexec || b->g_threads != b->threads || b->g_wmax < wmax || b->g_forced != forced || b->g_ntol != b->ntol_cap) {
+        int rc = batch_capture(b, G, wmax, forced);
+        if (rc) return rc;
+    }
+    CK(cudaGraphLaunch(b->gexec, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    for (int c = 0; c < n; c++) {
+        fsi_block *h = b->blk[c];
+        std::swap(h->fa, h->fb);
+        h->win_valid = false;
+    }
+    for (int c = 0; c < n; c++) {
+        if (b->blk[c]->Mtot == 0) {
+            if (iters) iters[c] = 0;
+            if (residual) residual[c] = 0.0;
+            continue;
+        }
+        const int stt = b->h_stat[8 * c];
+        if (stt & 1) return fail(FSI_E_RANGE, "block %d: index out of block bounds in IB stencil", c);
+        if (stt & 2) return fail(FSI_E_RANGE, "block %d: IB stencil outside the IB window", c);
+        if (stt & 4) return fail(FSI_E_NAN, "block %d: Nan found in PenaltyForce", c);
+        if (iters) iters[c] = b->h_stat[8 * c + 1];
+        if (residual) residual[c] = b->h_res[c];
+    }
+    if (b->Mall > 0) memcpy(eforce, b->h_ef, sizeof(double) * 3 * b->Mall);
+    return FSI_OK;
+}
+
+int fsi_batch_tune(fsi_batch_t b, int reps, int *threads, float *ms_per_step) {
+    if (!b || reps <= 0) return fail(FSI_E_ARG, "invalid argument");
+    // the bulk step of every block, fa -> fb without swapping: the state does
+    // not change (fb is rewritten by the next step)
+    std::vector<double> vf(3 * b->n, 0.0), t(b->n, 0.0);
+    batch_fill_steps(b, vf.data(), t.data(), false);
+    BatchCase *cs = (BatchCase *)b->h_in;
+    float best = 1e30f;
+    int best_t = b->threads;
+    for (int T : BATCH_THREADS) {
+        const int G = batch_groups(b, T, cs);
+        CK(cudaMemcpyAsync(b->d_in, b->h_in, b->off_ib, cudaMemcpyHostToDevice, b->st));
+        for (int w = 0; w < 2; w++)
+            CK(launch_batch_step((const BatchCase *)b->d_in, b->n, G, T, 0, b->prec, b->model, false, b->st));
+        CK(cudaEventRecord(b->ev0, b->st));
+        for (int r = 0; r < reps; r++)
+            CK(launch_batch_step((const BatchCase *)b->d_in, b->n, G, T, 0, b->prec, b->model, false, b->st));
+        CK(cudaEventRecord(b->ev1, b->st));
+        CK(cudaEventSynchronize(b->ev1));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        ms /= (float)reps;
+        if (ms < best) {
+            best = ms;
+            best_t = T;
+        }
+    }
+    b->threads = best_t;
+    if (threads) *threads = best_t;
+    if (ms_per_step) *ms_per_step = best;
+    return FSI_OK;
+}
+
+int fsi_batch_set_threads(fsi_batch_t b, int threads) {
+    if (!b) return fail(FSI_E_ARG, "null handle");
+    for (int T : BATCH_THREADS)
+        if (T == threads) {
+            b->threads = threads;
+            return FSI_OK;
+        }
+    return fail(FSI_E_ARG, "unsupported CTA size %d", threads);
 }
 
 }  // extern "C"

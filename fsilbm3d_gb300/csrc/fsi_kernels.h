@@ -99,6 +99,26 @@ cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, 
 cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double *wu, const IbGeom &g, long long N,
                                   const double vf[3], cudaStream_t st);
 
+// ---- many blocks stepped together (k_fast.cu; offset forms, paired kernels) ----
+// One entry per block: its step arguments (src/dst of this step, window, z
+// faces), the MRT rates S_k/|row k|^2, and its row groups: tpr = zDim/2 pairs
+// per z-row, R rows per group, ngy groups per x-plane, g0 = first global group.
+struct BatchCase {
+    StepArgs a;
+    float sd[19];
+    int tpr, R, ngy, g0;
+};
+// the bulk step of every block (G groups in all) with CTAs of `threads`;
+// then the IB-window fix-up of every block (wmax >= each block's window cells)
+cudaError_t launch_batch_step(const BatchCase *d_cases, int n, int G, int threads, long long wmax, int prec, int model,
+                              bool forced, cudaStream_t st);
+// face k of every block (bcs: n entries for this face; code BC_FLUID = none)
+cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int Bmax, int prec, cudaStream_t st);
+// the IB stage of every block, one CTA per block
+cudaError_t launch_batch_ib(const IbCoop *d_ib, int n, int threads, int prec, cudaStream_t st);
+// thread counts the batched bulk kernel is built for (the autotuner's choices)
+constexpr int BATCH_THREADS[3] = {256, 512, 128};
+
 // ---- warm-start perceptron (k_mlp.cu) ----
 cudaError_t launch_mlp_forward(const float *P, const float *nrm, const float *X, float *Y, int n, cudaStream_t st);
 cudaError_t launch_mlp_grad(const float *P, const float *nrm, const float *X, const float *Y, const int *perm,

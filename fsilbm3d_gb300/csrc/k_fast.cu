@@ -698,19 +698,20 @@ constexpr int pair_minb() {
 // uniform volume force vf. Cells of the IB window, half-way faces and 102
 // planes are then corrected by the small kernels below, which read the same
 // (unchanged) source buffer.
+// One row group of the bulk step: thread (tz, ty) of the group owns the cells
+// (2 tz, 2 tz + 1) of z-row y = y0 + ty in x-plane x; R rows per group; sm
+// holds [10][R][Z] elements. Every thread of the CTA calls it (the ones
+// outside the group with in_group false): it contains a CTA barrier.
 template <int P, int MODEL, bool FORCED>
-__global__ void __launch_bounds__(256, pair_minb<P, MODEL, FORCED>())
-k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
+__device__ __forceinline__ void pair_body(const StepArgs &a, const Offs<int> &of, const Scal<float> &sc,
+                                          const MrtS &ms, int tz, int ty, int R, int y, int x, bool in_group,
+                                          typename V2<P>::S *sm) {
     using V = V2<P>;
     using S2 = typename V::S2;
     using S = typename V::S;
-    extern __shared__ unsigned char smraw[];
     const int Z = a.Z, Y = a.Y, X = a.X;
-    const int tz = threadIdx.x, ty = threadIdx.y, R = blockDim.y;
     const int z0 = 2 * tz;
-    const int y = blockIdx.y * R + ty, x = blockIdx.z;
-    const bool active = (y < Y);
-    S *sm = (S *)smraw;  // [10][R][Z]
+    const bool active = in_group && (y < Y);
     const int c = z0 + Z * ((active ? y : 0) + Y * x);
     const int N = (int)a.N;
 
@@ -783,6 +784,16 @@ k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
         if (zf1) hi = V::enc1(geq_zface(a, 1, i));
         __stcs((S2 *)(dp + corr(i) + of.st[i]), V::pack(lo, hi));
     }
+}
+
+
+template <int P, int MODEL, bool FORCED>
+__global__ void __launch_bounds__(256, pair_minb<P, MODEL, FORCED>())
+k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
+    extern __shared__ unsigned char smraw[];
+    const int R = blockDim.y;
+    pair_body<P, MODEL, FORCED>(a, of, sc, ms, threadIdx.x, threadIdx.y, R, blockIdx.y * R + threadIdx.y, blockIdx.z,
+                                true, (typename V2<P>::S *)smraw);
 }
 
 // ---------------------------------------------------------------------------
@@ -1024,9 +1035,8 @@ __device__ __forceinline__ void push_cell(const StepArgs &a, int x, int y, int z
 // push again, replacing what the bulk step pushed for them. Two window cells
 // per thread (any two: the lanes are independent).
 template <int P, int MODEL>
-__global__ void __launch_bounds__(128) k_win_fix(StepArgs a, Scal<float> sc, MrtS ms) {
+__device__ __forceinline__ void win_fix_body(const StepArgs &a, const Scal<float> &sc, const MrtS &ms, long long w0) {
     const Win &w = a.win;
-    const long long w0 = 2 * (blockIdx.x * (long long)blockDim.x + threadIdx.x);
     if (w0 >= w.n) return;
     const bool two = w0 + 1 < w.n;
     int x[2], y[2], z[2];
@@ -1049,6 +1059,11 @@ __global__ void __launch_bounds__(128) k_win_fix(StepArgs a, Scal<float> sc, Mrt
     collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
     push_cell<P>(a, x[0], y[0], z[0], g, 0);
     if (two) push_cell<P>(a, x[1], y[1], z[1], g, 1);
+}
+
+template <int P, int MODEL>
+__global__ void __launch_bounds__(128) k_win_fix(StepArgs a, Scal<float> sc, MrtS ms) {
+    win_fix_body<P, MODEL>(a, sc, ms, 2 * (blockIdx.x * (long long)blockDim.x + threadIdx.x));
 }
 
 // Face hooks of one face k: the post-collision FP64 copy of a half-way face
@@ -1256,13 +1271,13 @@ __device__ __forceinline__ double ib_weight(const float *w, int p) {
     return ((double)w[p >> 4] * (double)w[4 + ((p >> 2) & 3)]) * (double)w[8 + (p & 3)];
 }
 
-template <int P>
-__global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
+// The IB stage of one block, by nth threads (tid = 0..nth-1) that meet at
+// bar(): the whole grid of a cooperative launch (k_ib_coop, grid barrier) or
+// one CTA (k_ib_batch, one block per CTA, __syncthreads).
+template <int P, class BAR>
+__device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long long nth, BAR &&bar) {
     using T = ST<P>;
     using C = typename T::C;
-    const unsigned nblk = gridDim.x;
-    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long nth = (long long)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
     const long long gw = tid >> 5, nw = nth >> 5;
     const IbGeom &g = a.g;
@@ -1294,7 +1309,7 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
         a.eforce[3 * m] = 0.0; a.eforce[3 * m + 1] = 0.0; a.eforce[3 * m + 2] = 0.0;
     }
     for (long long i = tid; i < a.ntol; i += nth) a.tol_acc[i] = 0.0;
-    if (!gbar(a.status, nblk)) return;
+    if (!bar()) return;
     if (*(volatile int *)a.status & 3) return;
 
     // learned warm start (no counterpart in the reference): features of every
@@ -1351,7 +1366,7 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
             }
         }
         if (a.mlp) {
-            if (!gbar(a.status, nblk)) return;
+            if (!bar()) return;
             for (long long m = gw; m < a.Mtot; m += nw) {
                 const int16_t *s = a.ei + 12 * m;
                 const float *w = a.ew + 12 * m;
@@ -1364,7 +1379,7 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
                     atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
                 }
             }
-            if (!gbar(a.status, nblk)) return;
+            if (!bar()) return;
         }
     }
 
@@ -1402,7 +1417,7 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
                     atomicAdd(a.tol_acc + it, (fabs(d0) + fabs(d1)) + fabs(d2));
                 }
             }
-            if (!gbar(a.status, nblk)) return;
+            if (!bar()) return;
             // the velocity correction of the support (Solidbody.f90:1034-1048)
             for (long long m = m0 + gw; m < m1; m += nw) {
                 const int16_t *s = a.ei + 12 * m;
@@ -1416,7 +1431,7 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
                     atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
                 }
             }
-            if (!gbar(a.status, nblk)) return;
+            if (!bar()) return;
         }
         const double tol = __ldcg(a.tol_acc + it);
         if (!isfinite(tol)) {
@@ -1444,6 +1459,25 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
         a.status[1] = it;
         *a.res = dmax;
     }
+}
+
+template <int P>
+__global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
+    const unsigned nblk = gridDim.x;
+    ib_body<P>(a, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x,
+               [&]() { return gbar(a.status, nblk); });
+}
+
+// the IB stage of many blocks, one CTA per block
+template <int P>
+__global__ void __launch_bounds__(512) k_ib_batch(const IbCoop *__restrict__ cases, int n) {
+    if ((int)blockIdx.x >= n) return;
+    const IbCoop &a = cases[blockIdx.x];
+    if (a.Mtot <= 0) return;
+    ib_body<P>(a, threadIdx.x, blockDim.x, []() {
+        __syncthreads();
+        return true;
+    });
 }
 
 template <int P>
@@ -1513,13 +1547,11 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
 // last face that writes them). Face velocities are evaluated in FP64 (a few
 // operations per cell) and the rest in FP32.
 template <int P, int FACE>
-__global__ void __launch_bounds__(256) k_bc_off(BcArgs a) {
+__device__ __forceinline__ void bc_off_body(const BcArgs &a, int fa, int fb) {
     using T = ST<P>;
     using S = typename T::S;
     const int A = (FACE < 4) ? a.Z : a.Y;
     const int B = (FACE < 2) ? a.Y : a.X;
-    const int fa = blockIdx.x * blockDim.x + threadIdx.x;
-    const int fb = blockIdx.y * blockDim.y + threadIdx.y;
     if (fa >= A || fb >= B) return;
     if (FACE < 4 && (fa < a.zlo || fa > a.zhi)) return;
     S *f = (S *)a.f;
@@ -1613,6 +1645,116 @@ __global__ void __launch_bounds__(256) k_bc_off(BcArgs a) {
     }
 }
 
+template <int P, int FACE>
+__global__ void __launch_bounds__(256) k_bc_off(BcArgs a) {
+    bc_off_body<P, FACE>(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+// face FACE of many blocks, blockIdx.z = block (code BC_FLUID: nothing to do)
+template <int P, int FACE>
+__global__ void __launch_bounds__(256) k_bc_off_batch(const BcArgs *__restrict__ bcs, int n) {
+    if ((int)blockIdx.z >= n) return;
+    const BcArgs &a = bcs[blockIdx.z];
+    if (a.code == BC_FLUID) return;
+    bc_off_body<P, FACE>(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+// ---------------------------------------------------------------------------
+// Many blocks in one launch: CTA j takes global row group j, finds its block
+// in the case table (sorted by first group), copies the block's step
+// arguments into shared memory with the offsets and collision constants the
+// single-block launcher passes as kernel parameters, and runs pair_body.
+// The per-block values are the same as the single-block path's, so a batch
+// step equals stepping each block alone.
+// ---------------------------------------------------------------------------
+struct BatchCta {
+    StepArgs a;
+    Offs<int> of;
+    Scal<float> sc;
+    MrtS ms;
+    int R, tpr, x, yb;
+};
+
+__device__ __forceinline__ void batch_prologue(const BatchCase *__restrict__ cases, int n, int j, BatchCta &cta) {
+    __shared__ int s_case;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (cases[mid].g0 <= j) lo = mid;
+            else hi = mid - 1;
+        }
+        s_case = lo;
+    }
+    __syncthreads();
+    const BatchCase &C = cases[s_case];
+    // the step arguments, word by word
+    const int nw = (int)(sizeof(StepArgs) / 4);
+    for (int k = threadIdx.x; k < nw; k += blockDim.x) ((int *)&cta.a)[k] = ((const int *)&C.a)[k];
+    const int t = threadIdx.x;
+    if (t < Q) {
+        const long long ZY = (long long)C.a.Z * C.a.Y;
+        cta.of.ld[t] = (int)((long long)t * C.a.N);
+        cta.of.st[t] = (int)((long long)t * C.a.N + (long long)C.a.Z * ey_(t) + ZY * ex_(t));
+        cta.ms.sd[t] = C.sd[t];
+    }
+    if (t == 0) {
+        cta.sc.om = (float)C.a.omega;
+        cta.sc.dh = (float)C.a.dh;
+        cta.sc.dh3 = 3.0f * (float)C.a.dh;
+        for (int k = 0; k < 3; k++) cta.sc.vf[k] = (float)C.a.vf[k];
+        cta.sc.forced = (C.a.vf[0] != 0.0 || C.a.vf[1] != 0.0 || C.a.vf[2] != 0.0) ? 1 : 0;
+        cta.R = C.R;
+        cta.tpr = C.tpr;
+        const int jj = j - C.g0;
+        cta.x = jj / C.ngy;
+        cta.yb = jj % C.ngy;
+    }
+    __syncthreads();
+}
+
+template <int P, int MODEL, bool FORCED, int T>
+__global__ void __launch_bounds__(T, T == 512 ? 1 : (T == 128 ? 2 * pair_minb<P, MODEL, FORCED>() : pair_minb<P, MODEL, FORCED>()))
+k_step_batch(const BatchCase *__restrict__ cases, int n) {
+    using S = typename V2<P>::S;
+    __shared__ BatchCta cta;
+    __shared__ S rows[10 * 2 * T];  // [10][R][Z], R*Z <= 2T
+    batch_prologue(cases, n, blockIdx.x, cta);
+    const int t = threadIdx.x;
+    const int tz = t % cta.tpr, ty = t / cta.tpr;
+    pair_body<P, MODEL, FORCED>(cta.a, cta.of, cta.sc, cta.ms, tz, ty, cta.R, cta.yb * cta.R + ty, cta.x,
+                                ty < cta.R, rows);
+}
+
+// the IB-window fix-up of every block: blockIdx.y = block
+template <int P, int MODEL>
+__global__ void __launch_bounds__(128) k_win_fix_batch(const BatchCase *__restrict__ cases, int n) {
+    if ((int)blockIdx.y >= n) return;
+    const BatchCase &C = cases[blockIdx.y];
+    if (C.a.win.x1 < C.a.win.x0 || C.a.win.n <= 0) return;
+    Scal<float> sc{};
+    sc.om = (float)C.a.omega;
+    sc.dh = (float)C.a.dh;
+    sc.dh3 = 3.0f * (float)C.a.dh;
+    MrtS ms;
+#pragma unroll
+    for (int k = 0; k < Q; k++) ms.sd[k] = C.sd[k];
+    win_fix_body<P, MODEL>(C.a, sc, ms, 2 * (blockIdx.x * (long long)blockDim.x + threadIdx.x));
+}
+
+template <int P, int MODEL, bool FORCED>
+cudaError_t batch_step_inst(const BatchCase *d, int n, int G, int threads, long long wmax, cudaStream_t st) {
+    switch (threads) {
+    case 128: k_step_batch<P, MODEL, FORCED, 128><<<G, 128, 0, st>>>(d, n); break;
+    case 512: k_step_batch<P, MODEL, FORCED, 512><<<G, 512, 0, st>>>(d, n); break;
+    default: k_step_batch<P, MODEL, FORCED, 256><<<G, 256, 0, st>>>(d, n); break;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || wmax <= 0) return e;
+    k_win_fix_batch<P, MODEL><<<dim3((unsigned)((wmax + 255) / 256), n), 128, 0, st>>>(d, n);
+    return cudaGetLastError();
+}
+
 template <int P>
 cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
     const int A = (a.face < 4) ? a.Z : a.Y;
@@ -1664,6 +1806,43 @@ cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int
 
 cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
     FSI_DISPATCH(prec, return bc_inst<PP>(a, st))
+}
+
+#define FSI_DISPATCH_OFF(prec, ...)                                          \
+    switch (prec) {                                                          \
+    case FSI_PREC_F32: { constexpr int PP = FSI_PREC_F32; __VA_ARGS__; }     \
+    case FSI_PREC_F16: { constexpr int PP = FSI_PREC_F16; __VA_ARGS__; }     \
+    case FSI_PREC_BF16: { constexpr int PP = FSI_PREC_BF16; __VA_ARGS__; }   \
+    default: return cudaErrorInvalidValue;                                   \
+    }
+
+cudaError_t launch_batch_step(const BatchCase *d_cases, int n, int G, int threads, long long wmax, int prec, int model,
+                              bool forced, cudaStream_t st) {
+    if (n <= 0 || G <= 0) return cudaSuccess;
+    if (model == 3) {
+        if (forced) { FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, true>(d_cases, n, G, threads, wmax, st))) }
+        FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, false>(d_cases, n, G, threads, wmax, st)))
+    }
+    if (forced) { FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, true>(d_cases, n, G, threads, wmax, st))) }
+    FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, false>(d_cases, n, G, threads, wmax, st)))
+}
+
+cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int Bmax, int prec, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    dim3 blk(64, 4), grd((Amax + 63) / 64, (Bmax + 3) / 4, n);
+    FSI_DISPATCH_OFF(prec, switch (face) {
+        case 0: k_bc_off_batch<PP, 0><<<grd, blk, 0, st>>>(d_bcs, n); break;
+        case 1: k_bc_off_batch<PP, 1><<<grd, blk, 0, st>>>(d_bcs, n); break;
+        case 2: k_bc_off_batch<PP, 2><<<grd, blk, 0, st>>>(d_bcs, n); break;
+        case 3: k_bc_off_batch<PP, 3><<<grd, blk, 0, st>>>(d_bcs, n); break;
+        case 4: k_bc_off_batch<PP, 4><<<grd, blk, 0, st>>>(d_bcs, n); break;
+        default: k_bc_off_batch<PP, 5><<<grd, blk, 0, st>>>(d_bcs, n); break;
+    } return cudaGetLastError())
+}
+
+cudaError_t launch_batch_ib(const IbCoop *d_ib, int n, int threads, int prec, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    FSI_DISPATCH_OFF(prec, k_ib_batch<PP><<<n, threads, 0, st>>>(d_ib, n); return cudaGetLastError())
 }
 
 cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st) {

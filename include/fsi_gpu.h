@@ -220,6 +220,35 @@ int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const
                       int ntol, double dtol, fsi_mlp_t warm, float *features, double *eforce,
                       int *iters, double *residual);
 
+/* No counterpart in the reference: many independent blocks stepped together
+ * (a parameter sweep of cases on one GPU). The blocks keep their handles and
+ * state; while batched they are stepped only through fsi_batch_ib_step (the
+ * other block calls stay valid between batch steps). Requirements: offset
+ * storage (FSI_PREC_F32/F16/BF16, the same for all), one collision model,
+ * even zDim up to 1024 with a moment-form MRT matrix, bodies already set
+ * (zero bodies allowed), no face of code 0, 1, 102, 203 or 204. */
+typedef struct fsi_batch *fsi_batch_t;
+int fsi_batch_create(fsi_batch_t *out, int nblocks, const fsi_block_t *blocks);
+int fsi_batch_destroy(fsi_batch_t b);
+/* One time step of every block: the IB stage (fsi_ib_solve) then the fluid
+ * step (fsi_block_step), as fsi_block_ib_step does for one block. Markers of
+ * all blocks are packed in block order: xyz, vel (3, sum Mtot), area (sum
+ * Mtot), eforce (3, sum Mtot) out; vf (3, n), denIn, dt, Uref, blktime (n);
+ * iters, residual (n) out (may be NULL). The device work of the step is one
+ * CUDA graph: an upload of every block's tables and markers, the IB stage of
+ * all blocks (one CTA per block), the bulk step of all blocks, their IB-window
+ * fix-ups, one launch per face index and one download. */
+int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const double *area,
+                      const double *vf, const double *denIn, const double *dt, const double *Uref,
+                      int ntol, double dtol, const double *blktime, double *eforce, int *iters,
+                      double *residual);
+/* Autotuner: times the bulk step of all blocks with each CTA size the kernel
+ * is built for (reps launches each, reading the current state and writing the
+ * spare buffer, so the state does not change) and keeps the fastest. */
+int fsi_batch_tune(fsi_batch_t b, int reps, int *threads, float *ms_per_step);
+/* the bulk kernel's CTA size by hand (128, 256 or 512) */
+int fsi_batch_set_threads(fsi_batch_t b, int threads);
+
 /* Block refinement, LBMBlockComm.f90:340-979. A pair links a father and a
  * son block; the son's faces with code 0 (BCfluid) receive father data. */
 typedef struct fsi_pair *fsi_pair_t;
