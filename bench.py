@@ -18,8 +18,10 @@ Beside it on the same workload: the FP64 plain path (reference operation
 order) with the force-coefficient error of the mixed path against it, and
 the CPU restatement of the reference step (OpenMP, host cores) on a bounded
 sample. Then the periodic Taylor-Green 256^3 throughput forms (FP64 plain,
-FP64 regrouped, FP32, FP16, BF16 storage; SRT and MRT) and the 160x96x96
-plate case at dh = L/16.
+FP64 regrouped, FP32, FP16, BF16 storage; SRT and MRT), the 160x96x96
+plate case at dh = L/16, a batched sweep of 32 plate cases (one graph per
+step vs one case at a time) and the learned IB warm start on three plates in
+tandem (penalty sub-iterations per step at the same residual).
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -348,6 +350,198 @@ def ib160_case(F, steps):
     return out
 
 
+# ------------------------------------------- batched sweep of plate cases
+
+def batched_sweep(F, steps, ncase=32, seed=7):
+    """ncase independent heaving-plate cases from a seed (grids 64^3 to
+    128x96x96, plates of 9x9 to 17x17 markers, Re 100-400, f* 0.15-0.35,
+    A 0.2L-0.6L, FP16 MRT): K steps one block at a time (one fsi_block_ib_step
+    per case and step) against K steps of the batch (one graph per step). The
+    host side is the same for both: the rigid-heave kinematics of all plates
+    as one array operation per step (reference positions + displacement)."""
+    from fsilbm3d_gb300.bodies import RigidPlate
+    rng = np.random.default_rng(seed)
+    specs = []
+    for c in range(ncase):
+        X = int(rng.integers(32, 65)) * 2
+        Y = int(rng.integers(32, 49)) * 2
+        Z = int(rng.integers(32, 49)) * 2
+        nodes = int(rng.integers(9, 18))
+        L = nodes - 1
+        dh = 1.0 / L
+        Re = float(rng.uniform(100.0, 400.0))
+        fstar = float(rng.uniform(0.15, 0.35))
+        A = float(rng.uniform(0.2, 0.6))
+        specs.append((X, Y, Z, nodes, dh, Re, fstar, A))
+    plates = [RigidPlate(n_chord=sp[3], n_span=sp[3], chord=1.0, span=1.0,
+                         le=(0.3 * sp[0] * sp[4], 0.5 * sp[1] * sp[4], 0.5 * sp[2] * sp[4]),
+                         heave_ampl=(0.0, sp[7], 0.0), freq=sp[6] * U) for sp in specs]
+    M = np.array([p.M for p in plates])
+    moff = np.concatenate([[0], np.cumsum(M)])
+    ref = [p.markers(0.0) for p in plates]  # phase 0: y displaced by A
+    base = np.concatenate([r[0] for r in ref]) - np.repeat(np.array([[0.0, sp[7], 0.0] for sp in specs]), M, axis=0)
+    area = np.concatenate([r[2] for r in ref])
+    amp = np.repeat(np.array([sp[7] for sp in specs]), M)
+    om = np.repeat(np.array([2 * np.pi * sp[6] * U for sp in specs]), M)
+    dts = np.array([sp[4] for sp in specs])
+    xyz = base.copy()
+    vel = np.zeros_like(base)
+
+    def kin(t):  # t per case -> packed xyz, vel (rigid heave in y)
+        tm = np.repeat(t, M)
+        xyz[:, 1] = base[:, 1] + amp * np.cos(om * tm)
+        vel[:, 1] = -om * amp * np.sin(om * tm)
+
+    def make():
+        blocks = []
+        for (X, Y, Z, nodes, dh, Re, fstar, A), p in zip(specs, plates):
+            b = F.Block(X, Y, Z, dh=dh, bndConds=BND, iCollidModel=3, nu=U / Re, precision=F.PREC_F16, uvwIn=(U, 0, 0))
+            b.initialise(0.0)
+            b.set_boundary_conditions(0.0)
+            b.ib_set_bodies([p.M])
+            blocks.append(b)
+        return blocks
+
+    cells = sum(sp[0] * sp[1] * sp[2] for sp in specs)
+    # one block at a time
+    blocks = make()
+    t = np.zeros(ncase)
+
+    def one_step():
+        kin(t)
+        efs = []
+        for c in range(ncase):
+            m0, m1 = moff[c], moff[c + 1]
+            ef, it, res = blocks[c].ib_step(xyz[m0:m1], vel[m0:m1], area[m0:m1], dt=dts[c], Uref=U, ntol=NTOL,
+                                            dtol=DTOL, blktime=t[c] + dts[c])
+            efs.append(ef)
+        t[:] += dts
+        return efs
+
+    for s in range(3):
+        one_step()
+    w0 = time.perf_counter()
+    for s in range(steps):
+        one_step()
+    for b in blocks:
+        b.calculate_macro_quantities(download=False)  # drain every block's stream
+    one_ms = (time.perf_counter() - w0) * 1e3 / steps
+    ef_one = np.concatenate(one_step())
+    for b in blocks:
+        b.close()
+    # the batch
+    blocks = make()
+    batch = F.Batch(blocks)
+    threads, tune_ms = batch.tune(reps=5)
+    t = np.zeros(ncase)
+    ef = np.empty(3 * int(moff[-1]))
+
+    def bat_step():
+        kin(t)
+        out = batch.ib_step_packed(xyz, vel, area, dt=dts, Uref=U, ntol=NTOL, dtol=DTOL, blktime=t + dts, eforce=ef)
+        t[:] += dts
+        return out
+
+    for s in range(3):
+        bat_step()
+    w0 = time.perf_counter()
+    for s in range(steps):
+        bat_step()
+    bat_ms = (time.perf_counter() - w0) * 1e3 / steps
+    ef_bat = bat_step()[0].copy()
+    dev = float(np.max(np.abs(ef_bat - ef_one)) / np.max(np.abs(ef_one)))
+    batch.close()
+    for b in blocks:
+        b.close()
+    return {"cases": ncase, "cells": cells, "markers": int(moff[-1]), "steps": steps, "seed": seed,
+            "one_by_one_mlups": round(cells / (one_ms * 1e-3) / 1e6, 1), "one_by_one_ms_per_step": one_ms,
+            "batched_mlups": round(cells / (bat_ms * 1e-3) / 1e6, 1), "batched_ms_per_step": bat_ms,
+            "speedup": round(one_ms / bat_ms, 2), "autotuned_cta_threads": threads, "autotune_bulk_ms": tune_ms,
+            "eforce_max_rel_dev_batched_vs_single": dev,
+            "workload": "%d heaving-plate cases from seed %d: grids 64^3..128x96x96 (even), plates 9x9..17x17 markers, "
+                        "Re 100-400, f* 0.15-0.35, A 0.2L-0.6L, FP16 MRT; wall time of K steps incl. the host "
+                        "kinematics (one array operation per step)" % (ncase, seed)}
+
+
+# ------------------------------------------------ learned IB warm start
+
+def warm_start_case(F, dtols=(0.005, 0.002), gen_steps=306, eval_steps=20, epochs=10, grid=(320, 192, 192)):
+    out = {}
+    for d in dtols:
+        out["dtol_%g" % d] = warm_start_run(F, d, gen_steps, eval_steps, epochs, grid)
+    return out
+
+
+def warm_start_run(F, dtol, gen_steps, eval_steps, epochs, grid):
+    """Three plates in tandem (spacing 1.5L, phases 0/90/180 deg, 33x33
+    markers, prescribed heave A = 0.3L, f* = 0.2) in a 320x192x192 block at
+    Re = 500 (dh = L/32, FP16 MRT). Training pairs are logged from the plain
+    solver (gen_steps x 3267 pairs, ~1e6), the network is trained on the GPU,
+    then plain and warm-started solves run from the same states to the same
+    residual; the warm result advances the flow."""
+    from fsilbm3d_gb300.bodies import RigidPlate
+    X, Y, Z = grid
+    L = 32
+    dh = 1.0 / L
+    nu = U / 500.0
+    b = F.Block(X, Y, Z, dh=dh, bndConds=BND, iCollidModel=3, nu=nu, precision=F.PREC_F16, uvwIn=(U, 0, 0))
+    b.initialise(0.0)
+    b.set_boundary_conditions(0.0)
+    plates = [RigidPlate(n_chord=33, n_span=33, chord=1.0, span=1.0, le=(2.0 + 1.5 * k, 0.5 * Y * dh, 0.5 * Z * dh),
+                         heave_ampl=(0.0, 0.3, 0.0), heave_phase_deg=(0.0, 90.0 * k, 0.0), freq=0.2 * U)
+              for k in range(3)]
+    b.ib_set_bodies([p.M for p in plates])
+    ntol = 400
+
+    def markers(t):
+        xs, vs, ar, ax = [], [], [], []
+        for p in plates:
+            xyz, vel, area = p.markers(t)
+            arg = 2 * np.pi * p.freq * t + p.phi
+            acc = -(2 * np.pi * p.freq) ** 2 * p.ampl * np.cos(arg)
+            a = np.zeros((p.M, 6))
+            a[:, :3] = acc
+            a[:, 4] = 1.0  # plate normal (x-z plane)
+            xs.append(xyz); vs.append(vel); ar.append(area); ax.append(a)
+        return np.concatenate(xs), np.concatenate(vs), np.concatenate(ar), np.concatenate(ax)
+
+    t = 0.0
+    Xf, Yf, gen_it = [], [], []
+    w0 = time.perf_counter()
+    for s in range(gen_steps):
+        xyz, vel, area, aux = markers(t)
+        ef, it, res, ft = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol, features=True)
+        Xf.append(ft)
+        Yf.append(ef / (area[:, None] * U))
+        gen_it.append(it)
+        t += dh
+        b.step(blktime=t)
+    gen_s = time.perf_counter() - w0
+    Xf, Yf = np.concatenate(Xf), np.concatenate(Yf)
+    m = F.Mlp(seed=1)
+    m.fit_norm(Xf, Yf)
+    w0 = time.perf_counter()
+    hist = m.train(Xf, Yf, epochs=epochs, batch=512, lr=2e-3, seed=2)
+    train_s = time.perf_counter() - w0
+    plain, warm, rp, rw = [], [], [], []
+    for s in range(eval_steps):
+        xyz, vel, area, aux = markers(t)
+        e0, i0, r0 = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol)
+        e1, i1, r1 = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol, warm=m)
+        plain.append(i0); warm.append(i1); rp.append(r0); rw.append(r1)
+        t += dh
+        b.step(blktime=t)
+    b.close()
+    return {"pairs": int(Xf.shape[0]), "gen_steps": gen_steps, "gen_s": round(gen_s, 2), "epochs": epochs,
+            "train_s": round(train_s, 2), "train_samples_per_s": round(Xf.shape[0] * epochs / train_s, 0),
+            "loss_first_last": [float(hist[0]), float(hist[-1])], "eval_steps": eval_steps, "dtol": dtol,
+            "plain_subiters_per_step": float(np.mean(plain)), "warm_subiters_per_step": float(np.mean(warm)),
+            "subiter_reduction": round(float(np.sum(plain)) / max(1.0, float(np.sum(warm))), 2),
+            "plain_residual_mean": float(np.mean(rp)), "warm_residual_mean": float(np.mean(rw)),
+            "workload": "3 rigid plates in tandem (1.5L, phases 0/90/180), 33x33 markers each, 320x192x192 FP16 "
+                        "MRT, Re=500, heave A=0.3L f*=0.2 (prescribed)"}
+
+
 # ------------------------------------------------------------------ main
 
 def main():
@@ -442,6 +636,8 @@ def main():
     if not a.no_extra and rank == 0:
         extra["tgv256"] = tgv_forms(F, max(20, min(a.steps, 100)), pk)
         extra["ib160"] = ib160_case(F, max(20, min(a.steps, 100)))
+        extra["batched_sweep"] = batched_sweep(F, max(10, min(a.steps, 50)))
+        extra["warm_start"] = warm_start_case(F)
 
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:

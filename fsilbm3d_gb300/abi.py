@@ -514,7 +514,6 @@ class Batch:
     def ib_step(self, markers, vf=None, denIn=None, dt=None, Uref=None, ntol=3, dtol=1e-5, blktime=None):
         """markers: one (xyz, vel, area) per block (None for a block without
         bodies). Returns (list of eforce (M,3), iterations (n,), residual (n,))."""
-        n = len(self.blocks)
         Mall = int(self.moff[-1])
         xyz = np.zeros(3 * max(Mall, 1))
         vel = np.zeros(3 * max(Mall, 1))
@@ -526,6 +525,21 @@ class Batch:
             xyz[3 * m0:3 * m1] = np.asarray(mk[0], dtype=np.float64).reshape(-1)
             vel[3 * m0:3 * m1] = np.asarray(mk[1], dtype=np.float64).reshape(-1)
             area[m0:m1] = np.asarray(mk[2], dtype=np.float64).reshape(-1)
+        ef, its, res = self.ib_step_packed(xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, blktime)
+        out = [ef[self.moff[c]:self.moff[c + 1]].copy() for c in range(len(self.blocks))]
+        return out, its, res
+
+    def ib_step_packed(self, xyz, vel, area, vf=None, denIn=None, dt=None, Uref=None, ntol=3, dtol=1e-5,
+                       blktime=None, eforce=None):
+        """the markers of all blocks packed in block order: xyz, vel (sum M, 3),
+        area (sum M); returns (eforce (sum M, 3), iterations (n,), residual (n,))"""
+        n = len(self.blocks)
+        Mall = int(self.moff[-1])
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        area = np.ascontiguousarray(area, dtype=np.float64).reshape(-1)
+        if Mall and (xyz.size < 3 * Mall or vel.size < 3 * Mall or area.size < Mall):
+            raise ValueError("packed marker arrays are shorter than the blocks' bodies")
         def per(v, default):
             a = np.full(n, default, dtype=np.float64) if v is None else np.asarray(v, dtype=np.float64)
             return np.ascontiguousarray(np.broadcast_to(a, (n,)))
@@ -534,15 +548,14 @@ class Batch:
         dta = np.ascontiguousarray(np.array([b.dh for b in self.blocks]) if dt is None else per(dt, 1.0))
         ur = per(Uref, 1.0)
         bt = per(blktime, 0.0)
-        ef = np.empty(3 * max(Mall, 1))
+        ef = np.empty(3 * max(Mall, 1)) if eforce is None else eforce
         its = np.zeros(n, dtype=np.int32)
         res = np.zeros(n)
         IPt = C.POINTER(C.c_int)
         _check(load_library().fsi_batch_ib_step(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(vfa), _dp(den), _dp(dta),
                                                 _dp(ur), int(ntol), dtol, _dp(bt), _dp(ef), its.ctypes.data_as(IPt),
                                                 _dp(res)))
-        out = [ef[3 * self.moff[c]:3 * self.moff[c + 1]].reshape(-1, 3).copy() for c in range(n)]
-        return out, its, res
+        return ef[:3 * Mall].reshape(-1, 3), its, res
 
     def tune(self, reps=10):
         """autotune the bulk kernel's CTA size; returns (threads, ms per step)"""
