@@ -1367,8 +1367,8 @@ struct fsi_batch {
     int n = 0;
     std::vector<fsi_block *> blk;
     int prec = 0, model = 1;
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t st = nullptr, st2 = nullptr;  // st2: the IB stage, beside the bulk step
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evf = nullptr, evj = nullptr;
     int threads = BATCH_THREADS[0];  // bulk kernel CTA size (the autotuner's choice)
     std::vector<int> moff;           // first packed marker of each block (n+1)
     int Mall = 0;
@@ -1380,6 +1380,9 @@ struct fsi_batch {
     int *d_stat = nullptr, *h_stat = nullptr;  // 8 per block
     double *d_res = nullptr, *h_res = nullptr;  // per block
     double *d_tol = nullptr;                    // ntol_cap per block
+    // block of each row group, for each CTA size (filled once)
+    int *d_gcase[3] = {nullptr, nullptr, nullptr};
+    int G[3] = {0, 0, 0};
     bool face_on[6] = {false, false, false, false, false, false};
     int Amax[6] = {0, 0, 0, 0, 0, 0}, Bmax[6] = {0, 0, 0, 0, 0, 0};
     cudaGraphExec_t gexec = nullptr;
@@ -1392,17 +1395,25 @@ namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+int thread_slot(int T) {
+    for (int k = 0; k < 3; k++)
+        if (BATCH_THREADS[k] == T) return k;
+    return 0;
+}
+
 void free_batch(fsi_batch *b) {
     if (!b) return;
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
-    void *dp[] = {b->d_in, b->d_ef, b->d_stat, b->d_res, b->d_tol};
+    void *dp[] = {b->d_in, b->d_ef, b->d_stat, b->d_res, b->d_tol, b->d_gcase[0], b->d_gcase[1], b->d_gcase[2]};
     for (void *p : dp)
         if (p) cudaFree(p);
     void *hp[] = {b->h_in, b->h_ef, b->h_stat, b->h_res};
     for (void *p : hp)
         if (p) cudaFreeHost(p);
-    if (b->ev0) cudaEventDestroy(b->ev0);
-    if (b->ev1) cudaEventDestroy(b->ev1);
+    cudaEvent_t evs[] = {b->ev0, b->ev1, b->evf, b->evj};
+    for (cudaEvent_t ev : evs)
+        if (ev) cudaEventDestroy(ev);
+    if (b->st2) cudaStreamDestroy(b->st2);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
 }
@@ -1442,9 +1453,17 @@ int batch_capture(fsi_batch *b, int G, long long wmax, bool forced) {
     CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemcpyAsync(b->d_in, b->h_in, b->in_bytes, cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_stat, 0, sizeof(int) * 8 * b->n, b->st);
-    if (e == cudaSuccess) e = launch_batch_ib((const IbCoop *)(b->d_in + b->off_ib), b->n, 512, b->prec, b->st);
+    // the IB stage (second stream) and the bulk step only read the state;
+    // the window fix-up needs both
+    if (e == cudaSuccess) e = cudaEventRecord(b->evf, b->st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st2, b->evf, 0);
+    if (e == cudaSuccess) e = launch_batch_ib((const IbCoop *)(b->d_in + b->off_ib), b->n, 512, b->prec, b->st2);
+    if (e == cudaSuccess) e = cudaEventRecord(b->evj, b->st2);
     if (e == cudaSuccess)
-        e = launch_batch_step((const BatchCase *)b->d_in, b->n, G, b->threads, wmax, b->prec, b->model, forced, b->st);
+        e = launch_batch_step((const BatchCase *)b->d_in, b->d_gcase[thread_slot(b->threads)], b->n, G, b->threads, 0,
+                              b->prec, b->model, forced, b->st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->evj, 0);
+    if (e == cudaSuccess) e = launch_batch_winfix((const BatchCase *)b->d_in, b->n, wmax, b->prec, b->model, b->st);
     for (int k = 0; k < 6 && e == cudaSuccess; k++)
         if (b->face_on[k])
             e = launch_batch_bc((const BcArgs *)(b->d_in + b->off_bc) + (size_t)k * b->n, b->n, k, b->Amax[k],
@@ -1527,6 +1546,9 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
     if ((e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&b->ev1)) != cudaSuccess) return bail(e);
+    if ((e = cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreateWithFlags(&b->evf, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreateWithFlags(&b->evj, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc((void **)&b->d_in, b->in_bytes)) != cudaSuccess) return bail(e);
     if ((e = cudaHostAlloc((void **)&b->h_in, b->in_bytes, cudaHostAllocDefault)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc((void **)&b->d_ef, sizeof(double) * 3 * Mt)) != cudaSuccess) return bail(e);
@@ -1539,6 +1561,19 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
     if ((e = cudaHostAlloc((void **)&b->h_res, sizeof(double) * n, cudaHostAllocDefault)) != cudaSuccess)
         return bail(e);
     memset(b->h_in, 0, b->in_bytes);
+    // the block of every row group, for each CTA size
+    for (int k = 0; k < 3; k++) {
+        std::vector<BatchCase> cs(n);
+        b->G[k] = batch_groups(b, BATCH_THREADS[k], cs.data());
+        std::vector<int> gc(b->G[k]);
+        for (int c = 0; c < n; c++)
+            for (int j = cs[c].g0; j < (c + 1 < n ? cs[c + 1].g0 : b->G[k]); j++) gc[j] = c;
+        if ((e = cudaMalloc((void **)&b->d_gcase[k], sizeof(int) * std::max(1, b->G[k]))) != cudaSuccess) return bail(e);
+        if ((e = cudaMemcpyAsync(b->d_gcase[k], gc.data(), sizeof(int) * b->G[k], cudaMemcpyHostToDevice, b->st)) !=
+            cudaSuccess)
+            return bail(e);
+        if ((e = cudaStreamSynchronize(b->st)) != cudaSuccess) return bail(e);
+    }
     // the blocks' own queued work finishes before the batch takes them over
     for (int c = 0; c < n; c++)
         if ((e = cudaStreamSynchronize(b->blk[c]->st)) != cudaSuccess) return bail(e);
@@ -1658,11 +1693,12 @@ int fsi_batch_tune(fsi_batch_t b, int reps, int *threads, float *ms_per_step) {
     for (int T : BATCH_THREADS) {
         const int G = batch_groups(b, T, cs);
         CK(cudaMemcpyAsync(b->d_in, b->h_in, b->off_ib, cudaMemcpyHostToDevice, b->st));
+        const int *gc = b->d_gcase[thread_slot(T)];
         for (int w = 0; w < 2; w++)
-            CK(launch_batch_step((const BatchCase *)b->d_in, b->n, G, T, 0, b->prec, b->model, false, b->st));
+            CK(launch_batch_step((const BatchCase *)b->d_in, gc, b->n, G, T, 0, b->prec, b->model, false, b->st));
         CK(cudaEventRecord(b->ev0, b->st));
         for (int r = 0; r < reps; r++)
-            CK(launch_batch_step((const BatchCase *)b->d_in, b->n, G, T, 0, b->prec, b->model, false, b->st));
+            CK(launch_batch_step((const BatchCase *)b->d_in, gc, b->n, G, T, 0, b->prec, b->model, false, b->st));
         CK(cudaEventRecord(b->ev1, b->st));
         CK(cudaEventSynchronize(b->ev1));
         float ms = 0.0f;

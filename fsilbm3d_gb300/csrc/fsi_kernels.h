@@ -108,10 +108,13 @@ struct BatchCase {
     float sd[19];
     int tpr, R, ngy, g0;
 };
-// the bulk step of every block (G groups in all) with CTAs of `threads`;
-// then the IB-window fix-up of every block (wmax >= each block's window cells)
-cudaError_t launch_batch_step(const BatchCase *d_cases, int n, int G, int threads, long long wmax, int prec, int model,
-                              bool forced, cudaStream_t st);
+// the bulk step of every block (G groups in all, gcase[j] = block of group
+// j) with CTAs of `threads`; then the IB-window fix-up of every block (wmax >=
+// each block's window cells)
+cudaError_t launch_batch_step(const BatchCase *d_cases, const int *d_gcase, int n, int G, int threads, long long wmax,
+                              int prec, int model, bool forced, cudaStream_t st);
+// the IB-window fix-up alone (after the bulk step and the IB stage)
+cudaError_t launch_batch_winfix(const BatchCase *d_cases, int n, long long wmax, int prec, int model, cudaStream_t st);
 // face k of every block (bcs: n entries for this face; code BC_FLUID = none)
 cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int Bmax, int prec, cudaStream_t st);
 // the IB stage of every block, one CTA per block

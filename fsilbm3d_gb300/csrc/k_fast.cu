@@ -1468,14 +1468,26 @@ __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
                [&]() { return gbar(a.status, nblk); });
 }
 
-// the IB stage of many blocks, one CTA per block
+// the IB stage of many blocks, one thread-block cluster of IB_CLUSTER CTAs
+// per block; the cluster barrier (release/acquire at cluster scope, with a
+// device fence for the global-memory atomics) separates the phases
+constexpr int IB_CLUSTER = 8;
+
+__device__ __forceinline__ void cluster_barrier() {
+    __threadfence();
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
 template <int P>
-__global__ void __launch_bounds__(512) k_ib_batch(const IbCoop *__restrict__ cases, int n) {
-    if ((int)blockIdx.x >= n) return;
-    const IbCoop &a = cases[blockIdx.x];
+__global__ void __cluster_dims__(IB_CLUSTER, 1, 1) __launch_bounds__(512) k_ib_batch(const IbCoop *__restrict__ cases,
+                                                                                      int n) {
+    const int c = blockIdx.x / IB_CLUSTER, rank = blockIdx.x % IB_CLUSTER;
+    if (c >= n) return;  // whole clusters only: the grid is n * IB_CLUSTER
+    const IbCoop &a = cases[c];
     if (a.Mtot <= 0) return;
-    ib_body<P>(a, threadIdx.x, blockDim.x, []() {
-        __syncthreads();
+    ib_body<P>(a, (long long)rank * blockDim.x + threadIdx.x, (long long)IB_CLUSTER * blockDim.x, []() {
+        cluster_barrier();
         return true;
     });
 }
@@ -1675,19 +1687,9 @@ struct BatchCta {
     int R, tpr, x, yb;
 };
 
-__device__ __forceinline__ void batch_prologue(const BatchCase *__restrict__ cases, int n, int j, BatchCta &cta) {
-    __shared__ int s_case;
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = n - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (cases[mid].g0 <= j) lo = mid;
-            else hi = mid - 1;
-        }
-        s_case = lo;
-    }
-    __syncthreads();
-    const BatchCase &C = cases[s_case];
+__device__ __forceinline__ void batch_prologue(const BatchCase *__restrict__ cases, const int *__restrict__ gcase,
+                                               int j, BatchCta &cta) {
+    const BatchCase &C = cases[gcase[j]];
     // the step arguments, word by word
     const int nw = (int)(sizeof(StepArgs) / 4);
     for (int k = threadIdx.x; k < nw; k += blockDim.x) ((int *)&cta.a)[k] = ((const int *)&C.a)[k];
@@ -1715,11 +1717,11 @@ __device__ __forceinline__ void batch_prologue(const BatchCase *__restrict__ cas
 
 template <int P, int MODEL, bool FORCED, int T>
 __global__ void __launch_bounds__(T, T == 512 ? 1 : (T == 128 ? 2 * pair_minb<P, MODEL, FORCED>() : pair_minb<P, MODEL, FORCED>()))
-k_step_batch(const BatchCase *__restrict__ cases, int n) {
+k_step_batch(const BatchCase *__restrict__ cases, const int *__restrict__ gcase) {
     using S = typename V2<P>::S;
     __shared__ BatchCta cta;
     __shared__ S rows[10 * 2 * T];  // [10][R][Z], R*Z <= 2T
-    batch_prologue(cases, n, blockIdx.x, cta);
+    batch_prologue(cases, gcase, blockIdx.x, cta);
     const int t = threadIdx.x;
     const int tz = t % cta.tpr, ty = t / cta.tpr;
     pair_body<P, MODEL, FORCED>(cta.a, cta.of, cta.sc, cta.ms, tz, ty, cta.R, cta.yb * cta.R + ty, cta.x,
@@ -1743,14 +1745,22 @@ __global__ void __launch_bounds__(128) k_win_fix_batch(const BatchCase *__restri
 }
 
 template <int P, int MODEL, bool FORCED>
-cudaError_t batch_step_inst(const BatchCase *d, int n, int G, int threads, long long wmax, cudaStream_t st) {
+cudaError_t batch_step_inst(const BatchCase *d, const int *gcase, int n, int G, int threads, long long wmax,
+                            cudaStream_t st) {
     switch (threads) {
-    case 128: k_step_batch<P, MODEL, FORCED, 128><<<G, 128, 0, st>>>(d, n); break;
-    case 512: k_step_batch<P, MODEL, FORCED, 512><<<G, 512, 0, st>>>(d, n); break;
-    default: k_step_batch<P, MODEL, FORCED, 256><<<G, 256, 0, st>>>(d, n); break;
+    case 128: k_step_batch<P, MODEL, FORCED, 128><<<G, 128, 0, st>>>(d, gcase); break;
+    case 512: k_step_batch<P, MODEL, FORCED, 512><<<G, 512, 0, st>>>(d, gcase); break;
+    default: k_step_batch<P, MODEL, FORCED, 256><<<G, 256, 0, st>>>(d, gcase); break;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || wmax <= 0) return e;
+    k_win_fix_batch<P, MODEL><<<dim3((unsigned)((wmax + 255) / 256), n), 128, 0, st>>>(d, n);
+    return cudaGetLastError();
+}
+
+template <int P, int MODEL>
+cudaError_t batch_winfix_inst(const BatchCase *d, int n, long long wmax, cudaStream_t st) {
+    if (wmax <= 0) return cudaSuccess;
     k_win_fix_batch<P, MODEL><<<dim3((unsigned)((wmax + 255) / 256), n), 128, 0, st>>>(d, n);
     return cudaGetLastError();
 }
@@ -1816,15 +1826,23 @@ cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
     default: return cudaErrorInvalidValue;                                   \
     }
 
-cudaError_t launch_batch_step(const BatchCase *d_cases, int n, int G, int threads, long long wmax, int prec, int model,
-                              bool forced, cudaStream_t st) {
+cudaError_t launch_batch_step(const BatchCase *d_cases, const int *d_gcase, int n, int G, int threads, long long wmax,
+                              int prec, int model, bool forced, cudaStream_t st) {
     if (n <= 0 || G <= 0) return cudaSuccess;
     if (model == 3) {
-        if (forced) { FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, true>(d_cases, n, G, threads, wmax, st))) }
-        FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, false>(d_cases, n, G, threads, wmax, st)))
+        if (forced) {
+            FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, true>(d_cases, d_gcase, n, G, threads, wmax, st)))
+        }
+        FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, false>(d_cases, d_gcase, n, G, threads, wmax, st)))
     }
-    if (forced) { FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, true>(d_cases, n, G, threads, wmax, st))) }
-    FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, false>(d_cases, n, G, threads, wmax, st)))
+    if (forced) { FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, true>(d_cases, d_gcase, n, G, threads, wmax, st))) }
+    FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, false>(d_cases, d_gcase, n, G, threads, wmax, st)))
+}
+
+cudaError_t launch_batch_winfix(const BatchCase *d_cases, int n, long long wmax, int prec, int model, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (model == 3) { FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, 3>(d_cases, n, wmax, st))) }
+    FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, 1>(d_cases, n, wmax, st)))
 }
 
 cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int Bmax, int prec, cudaStream_t st) {
@@ -1842,7 +1860,7 @@ cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int 
 
 cudaError_t launch_batch_ib(const IbCoop *d_ib, int n, int threads, int prec, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    FSI_DISPATCH_OFF(prec, k_ib_batch<PP><<<n, threads, 0, st>>>(d_ib, n); return cudaGetLastError())
+    FSI_DISPATCH_OFF(prec, k_ib_batch<PP><<<n * IB_CLUSTER, threads, 0, st>>>(d_ib, n); return cudaGetLastError())
 }
 
 cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st) {
