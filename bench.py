@@ -66,9 +66,15 @@ def parse():
     p.add_argument("--no-extra", action="store_true", help="skip the TGV forms and the 160x96x96 case")
     p.add_argument("--f64-steps", type=int, default=24, help="steps of the FP64 plain comparison")
     p.add_argument("--grid", default="384x256x256", help="headline grid (profiling runs use a smaller one)")
+    p.add_argument("--only", default="all", choices=["all", "tgv256", "ib160", "batched_sweep", "warm_start"],
+                   help="run one side section alone and print its result (profiling runs)")
+    p.add_argument("--tgv-grid", type=int, default=256, help="edge of the periodic TGV cube")
+    p.add_argument("--tgv-forms", default="f64,f64_fast,f32,f16,bf16", help="TGV storage forms")
+    p.add_argument("--tgv-models", default="1,3", help="TGV collision models (1 SRT, 3 MRT)")
     a = p.parse_args()
-    global FSI_GRID
+    global FSI_GRID, TGV_GRID
     FSI_GRID = tuple(int(v) for v in a.grid.split("x"))
+    TGV_GRID = (a.tgv_grid,) * 3
     return a
 
 
@@ -274,15 +280,17 @@ def tgv_f64(grid):
     return f
 
 
-def tgv_forms(F, steps, pk):
+def tgv_forms(F, steps, pk, forms=("f64", "f64_fast", "f32", "f16", "bf16"), models=(1, 3)):
     X, Y, Z = TGV_GRID
     N = X * Y * Z
     nu = (TAU - 0.5) / 3.0
     f0 = tgv_f64(TGV_GRID)
     out = {}
     for model, mname in ((1, "srt"), (3, "mrt")):
-        ref_u = None
-        for name in ("f64", "f64_fast", "f32", "f16", "bf16"):
+        if model not in models:
+            continue
+        ref_u, ref_n = None, None
+        for name in forms:
             b = F.Block(X, Y, Z, nu=nu, precision=F.PRECISIONS[name], iCollidModel=model)
             b.upload_f(f0)
             b.run(3)
@@ -300,8 +308,10 @@ def tgv_forms(F, steps, pk):
                 r["u_max_rel_err_vs_f64"] = float(np.max(np.abs(uuu - ref_u)) / np.max(np.abs(ref_u)))
             out["%s_%s" % (name, mname)] = r
             b.close()
+        if ref_u is None:
+            continue
         # the error of every form after the same steps as FP64 plain
-        for name in ("f64_fast", "f32", "f16", "bf16"):
+        for name in [f for f in forms if f != "f64"]:
             key = "%s_%s" % (name, mname)
             if "u_max_rel_err_vs_f64" in out[key]:
                 continue
@@ -312,7 +322,7 @@ def tgv_forms(F, steps, pk):
             out[key]["u_max_rel_err_vs_f64"] = float(np.max(np.abs(uuu - ref_u)) / np.max(np.abs(ref_u)))
             out[key]["err_after_steps"] = ref_n
             b.close()
-    out["workload"] = "taylor-green vortex 256^3 periodic, tau=0.6, u0=0.05, inputs larger than L2"
+    out["workload"] = "taylor-green vortex %d^3 periodic, tau=0.6, u0=0.05, inputs larger than L2" % X
     return out
 
 
@@ -551,6 +561,20 @@ def main():
         return main_reference(a, rank, world, dist)
     import fsilbm3d_gb300 as F
     a.warmup = max(a.warmup, 3)
+    if a.only != "all":
+        pk, _ = peaks()
+        steps = max(10, min(a.steps, 100))
+        if a.only == "tgv256":
+            r = tgv_forms(F, steps, pk, forms=a.tgv_forms.split(","), models=[int(m) for m in a.tgv_models.split(",")])
+        elif a.only == "ib160":
+            r = ib160_case(F, steps)
+        elif a.only == "batched_sweep":
+            r = batched_sweep(F, max(10, min(a.steps, 50)))
+        else:
+            r = warm_start_case(F)
+        if rank == 0:
+            print(json.dumps({a.only: r}))
+        return
     X, Y, Z = FSI_GRID
     N = X * Y * Z
     pk, pk_kind = peaks()
