@@ -58,7 +58,9 @@ SYMBOLS = [
     "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_block_timer",
     "fsi_block_set_kernel", "fsi_block_ib_step",
     "fsi_batch_create", "fsi_batch_destroy", "fsi_batch_ib_step", "fsi_batch_tune", "fsi_batch_set_threads",
+    "fsi_block_set_ib_mode",
 ]
+IB_AUTO, IB_GRID, IB_CLUSTER = 0, 1, 2
 KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
 # the warm-start perceptron (FSI_MLP_* in the header)
 MLP_IN, MLP_OUT, MLP_NPARAM, MLP_NNORM = 12, 3, 5187, 30
@@ -96,6 +98,7 @@ def load_library():
     L.fsi_block_run.argtypes = [VP, DP, C.c_double, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_timer.argtypes = [VP, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_set_kernel.argtypes = [VP, C.c_int]
+    L.fsi_block_set_ib_mode.argtypes = [VP, C.c_int]
     L.fsi_batch_create.argtypes = [C.POINTER(VP), C.c_int, C.POINTER(VP)]
     L.fsi_batch_destroy.argtypes = [VP]
     L.fsi_batch_ib_step.argtypes = [VP, DP, DP, DP, DP, DP, DP, DP, C.c_int, C.c_double, DP, DP, IP, DP]
@@ -272,6 +275,11 @@ class Block:
     def set_kernel(self, kernel):
         """bulk step kernel of the offset forms: KERNEL_AUTO, _PAIRED, _PIPELINED"""
         _check(load_library().fsi_block_set_kernel(self.h, int(kernel)))
+
+    def set_ib_mode(self, mode):
+        """IB stage of ib_step: IB_GRID (cooperative, then the step) or
+        IB_CLUSTER (one cluster beside the bulk step)"""
+        _check(load_library().fsi_block_set_ib_mode(self.h, int(mode)))
 
     def timer_start(self):
         """mark the start of a timed region on the block's stream"""

@@ -139,6 +139,10 @@ struct fsi_block {
     int hw_ready[6] = {0, 0, 0, 0, 0, 0};
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_ib = nullptr;
+    // the IB stage beside the bulk step (fsi_block_ib_step, FSI_IB_CLUSTER)
+    int ib_mode = FSI_IB_AUTO;
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr;
     double *h_ef = nullptr;  // pinned staging of the Lagrangian force (fsi_block_ib_step)
     int h_ef_cap = 0;
     // immersed boundary
@@ -324,9 +328,10 @@ void fill_step(fsi_block *h, const double vf[3], double blktime, bool use_window
     }
 }
 
-int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_window) {
+int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_window, cudaEvent_t join = nullptr) {
     StepArgs a;
     fill_step(h, vf, blktime, use_window, a);
+    a.join = (void *)join;
     cudaError_t e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
                                : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
     if (e != cudaSuccess) return fail(FSI_E_CUDA, "step kernel: %s", cudaGetErrorString(e));
@@ -361,6 +366,8 @@ void free_block(fsi_block *h) {
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->ev_ib) cudaEventDestroy(h->ev_ib);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->st2) cudaStreamDestroy(h->st2);
     if (h->h_ef) cudaFreeHost(h->h_ef);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
@@ -445,6 +452,13 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     chk(cudaEventCreate(&h->ev0));
     chk(cudaEventCreate(&h->ev1));
     chk(cudaEventCreateWithFlags(&h->ev_ib, cudaEventDisableTiming));
+    chk(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    {
+        // the IB stage's stream is served first when SMs free up
+        int lo = 0, hi = 0;
+        chk(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        chk(cudaStreamCreateWithPriority(&h->st2, cudaStreamNonBlocking, hi));
+    }
     chk(cudaMalloc(&h->fa, fbytes));
     chk(cudaMalloc(&h->fb, fbytes));
     chk(cudaMalloc((void **)&h->den, sizeof(double) * h->N));
@@ -574,6 +588,13 @@ int fsi_block_set_kernel(fsi_block_t h, int kernel) {
         h->gexec = nullptr;
     }
     h->kernel = kernel;
+    return FSI_OK;
+}
+
+int fsi_block_set_ib_mode(fsi_block_t h, int mode) {
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    if (mode < FSI_IB_AUTO || mode > FSI_IB_CLUSTER) return fail(FSI_E_ARG, "unknown IB mode %d", mode);
+    h->ib_mode = mode;
     return FSI_OK;
 }
 
@@ -800,6 +821,31 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     a.aux = wm.aux ? h->d_aux : nullptr;
     a.feat = wm.features ? h->d_feat : nullptr;
     a.Uref = Uref;
+    if (wm.step && h->ib_mode == FSI_IB_CLUSTER && !wm.mlp && !wm.features && h->prec != FSI_PREC_F64_FAST) {
+        // the IB stage on one cluster on the second stream, beside the bulk
+        // step (both only read the state); the window fix-up and the face
+        // hooks wait for it
+        if (h->h_ef_cap < h->Mtot) {
+            if (h->h_ef) cudaFreeHost(h->h_ef);
+            h->h_ef = nullptr;
+            h->h_ef_cap = 0;
+            CK(cudaHostAlloc((void **)&h->h_ef, sizeof(double) * 3 * h->Mtot, cudaHostAllocDefault));
+            h->h_ef_cap = h->Mtot;
+        }
+        CK(cudaEventRecord(h->ev_fork, h->st));
+        CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+        CK(launch_ib_cluster(a, h->prec, h->st2));
+        CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st2));
+        CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st2));
+        CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st2));
+        CK(cudaEventRecord(h->ev_ib, h->st2));
+        h->win_valid = true;
+        int rc = enqueue_step(h, wm.step_vf, wm.step_time, true, h->ev_ib);
+        h->win_valid = false;
+        if (rc) return rc;
+        CK(cudaEventSynchronize(h->ev_ib));
+        memcpy(eforce, h->h_ef, sizeof(double) * 3 * h->Mtot);
+    } else {
     // one warp per marker in the penalty loop and a thread per window cell in
     // the macro phase are all the parallelism there is; a smaller grid makes
     // each of the grid barriers cheaper
@@ -833,6 +879,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st));
         CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
         CK(cudaStreamSynchronize(h->st));
+    }
     }
     if (h->h_stat[4]) return fail(FSI_E_TIMEOUT, "step kernel: a bounded wait ran out");
     const int st = h->h_stat[0];
@@ -1546,7 +1593,11 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
     if ((e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&b->ev1)) != cudaSuccess) return bail(e);
-    if ((e = cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    {
+        int lo = 0, hi = 0;
+        if ((e = cudaDeviceGetStreamPriorityRange(&lo, &hi)) != cudaSuccess) return bail(e);
+        if ((e = cudaStreamCreateWithPriority(&b->st2, cudaStreamNonBlocking, hi)) != cudaSuccess) return bail(e);
+    }
     if ((e = cudaEventCreateWithFlags(&b->evf, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreateWithFlags(&b->evj, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc((void **)&b->d_in, b->in_bytes)) != cudaSuccess) return bail(e);

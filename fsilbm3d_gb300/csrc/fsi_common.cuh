@@ -128,6 +128,9 @@ struct StepArgs {
     // host leaves those faces out of the face kernels
     int zeq[2];
     float zg[2][19];
+    // host only: an event the window fix-up and face hooks wait for (the IB
+    // stage running beside the bulk step on another stream), or null
+    void *join;
 };
 
 struct BcArgs {

@@ -68,6 +68,9 @@ struct IbCoop {
     double Uref;
 };
 cudaError_t launch_ib_coop(const IbCoop &a, int prec, int grid, cudaStream_t st);
+// the same on one thread-block cluster, which may run beside other kernels
+// (offset storage forms)
+cudaError_t launch_ib_cluster(const IbCoop &a, int prec, cudaStream_t st);
 int ib_coop_grid(int prec);  // co-resident CTAs (256 threads) on this device, 0 on error
 
 // ---- block refinement (k_f64_exact.cu) ----

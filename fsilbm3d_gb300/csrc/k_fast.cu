@@ -1158,16 +1158,6 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
     const int R = std::max(1, 256 / tpr);
     dim3 blk(tpr, R), grd(1, (a.Y + R - 1) / R, a.X);
     size_t smem = (size_t)10 * R * a.Z * sizeof(typename V2<P>::S);
-    // the face hooks read the source buffer, which the bulk step leaves as is
-    if (hooks) {
-        for (int k = 0; k < 6; k++) {
-            if (!a.hw[k] && !a.l2[k]) continue;
-            const int ax = k >> 1;
-            const int A = ax == 2 ? a.Y : a.Z, B = ax == 0 ? a.Y : a.X;
-            const long long n = (long long)A * B;
-            k_face_hook<P, MODEL><<<(unsigned)((n + 255) / 256), 128, 0, st>>>(a, sc, ms, k, A, B);
-        }
-    }
     // the pipelined persistent form (on request; it needs 16-byte aligned
     // population rows) or the paired form
     const bool pipe = a.variant == 2 && a.Z % 8 == 0;
@@ -1179,6 +1169,21 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
         k_step_pair<P, MODEL, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
     } else {
         k_step_pair<P, MODEL, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
+    }
+    // what needs the IB stage's window waits for it
+    if (a.join) {
+        cudaError_t e = cudaStreamWaitEvent(st, (cudaEvent_t)a.join, 0);
+        if (e != cudaSuccess) return e;
+    }
+    // the face hooks read the source buffer, which the bulk step leaves as is
+    if (hooks) {
+        for (int k = 0; k < 6; k++) {
+            if (!a.hw[k] && !a.l2[k]) continue;
+            const int ax = k >> 1;
+            const int A = ax == 2 ? a.Y : a.Z, B = ax == 0 ? a.Y : a.X;
+            const long long n = (long long)A * B;
+            k_face_hook<P, MODEL><<<(unsigned)((n + 255) / 256), 128, 0, st>>>(a, sc, ms, k, A, B);
+        }
     }
     if (a.win.x1 >= a.win.x0 && a.win.n > 0)
         k_win_fix<P, MODEL><<<(unsigned)((a.win.n + 255) / 256), 128, 0, st>>>(a, sc, ms);
@@ -1477,6 +1482,17 @@ __device__ __forceinline__ void cluster_barrier() {
     __threadfence();
     asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// the IB stage of one block on one cluster (so that it can run beside the
+// bulk step: a cluster needs no grid-wide co-residency)
+template <int P>
+__global__ void __cluster_dims__(IB_CLUSTER, 1, 1) __launch_bounds__(512) k_ib_cluster(IbCoop a) {
+    if (a.Mtot <= 0) return;
+    ib_body<P>(a, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)IB_CLUSTER * blockDim.x, []() {
+        cluster_barrier();
+        return true;
+    });
 }
 
 template <int P>
@@ -1856,6 +1872,10 @@ cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int 
         case 4: k_bc_off_batch<PP, 4><<<grd, blk, 0, st>>>(d_bcs, n); break;
         default: k_bc_off_batch<PP, 5><<<grd, blk, 0, st>>>(d_bcs, n); break;
     } return cudaGetLastError())
+}
+
+cudaError_t launch_ib_cluster(const IbCoop &a, int prec, cudaStream_t st) {
+    FSI_DISPATCH_OFF(prec, k_ib_cluster<PP><<<IB_CLUSTER, 512, 0, st>>>(a); return cudaGetLastError())
 }
 
 cudaError_t launch_batch_ib(const IbCoop *d_ib, int n, int threads, int prec, cudaStream_t st) {

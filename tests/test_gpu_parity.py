@@ -354,17 +354,21 @@ def test_pipelined_kernel_needs_aligned_rows(gpu_lib):
     b.set_kernel(F.abi.KERNEL_AUTO)
 
 
-@pytest.mark.parametrize("prec,tol", [(F.PREC_F64, 0.0), (F.PREC_F64_FAST, 1e-12), (F.PREC_F32, 1e-6)])
-def test_ib_step_equals_solve_then_step(gpu_lib, prec, tol):
+@pytest.mark.parametrize("prec,tol,mode", [(F.PREC_F64, 0.0, 0), (F.PREC_F64_FAST, 1e-12, 0), (F.PREC_F32, 1e-6, 1),
+                                           (F.PREC_F32, 1e-6, 2), (F.PREC_F16, 1e-3, 2)])
+def test_ib_step_equals_solve_then_step(gpu_lib, prec, tol, mode):
+    # mode 2: the IB stage on one cluster beside the bulk step
     dims = (40, 24, 20)
     blocks = []
     plate = plate_in(dims, n=5, heave=1.0, freq=0.02)
-    for _ in range(2):
+    for k in range(2):
         b = F.Block(*dims, bndConds=(101, 104, 101, 101, 101, 101), iCollidModel=3, nu=0.02, precision=prec,
                     uvwIn=(0.05, 0.0, 0.0))
         b.initialise(0.0)
         b.set_boundary_conditions(0.0)
         b.ib_set_bodies([plate.M])
+        if k == 1:
+            b.set_ib_mode(mode)
         blocks.append(b)
     for s in range(4):
         xyz, vel, area = plate.markers(float(s))
