@@ -66,6 +66,32 @@ def test_shear_wave_viscous_decay():
     assert abs(amp / expect - 1.0) < 1e-2  # O((k dx)^2) lattice error at N=32
 
 
+def test_tgv_kinetic_energy_decay():
+    # 3-D Taylor-Green field (the added initialiser) at small amplitude: the
+    # linear regime decays its kinetic energy as exp(-2 nu |k|^2 t)
+    N = 32
+    fl = O.make_flow(nu=0.05)
+    b = O.Block(N, N, N, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    b.init_tgv(1e-3)
+
+    def energy():
+        b.macro()
+        u = b.u.reshape(3, -1)
+        return 0.5 * float(np.sum(b.den * np.sum(u * u, axis=0)))
+
+    t1, t2 = 50, 300
+    for _ in range(t1):
+        b.step()
+    e1 = energy()
+    for _ in range(t2 - t1):
+        b.step()
+    e2 = energy()
+    nu = (b.b.tau - 0.5) / 3.0
+    rate = -np.log(e2 / e1) / (t2 - t1)
+    expect = 2.0 * nu * 3.0 * (2 * np.pi / N) ** 2
+    assert abs(rate / expect - 1.0) < 2e-2  # O((k dx)^2) lattice error at N=32
+
+
 def test_guo_forcing_momentum_growth():
     F_ = (2e-5, -1e-5, 3e-6)
     fl = O.make_flow(nu=0.03, volumeForceIn=F_)
