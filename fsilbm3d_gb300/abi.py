@@ -58,7 +58,7 @@ SYMBOLS = [
     "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_block_timer",
     "fsi_block_set_kernel", "fsi_block_ib_step",
     "fsi_batch_create", "fsi_batch_destroy", "fsi_batch_ib_step", "fsi_batch_tune", "fsi_batch_set_threads",
-    "fsi_block_set_ib_mode",
+    "fsi_block_set_ib_mode", "fsi_block_pack_flow", "fsi_block_flux", "fsi_block_probes",
 ]
 IB_AUTO, IB_GRID, IB_CLUSTER = 0, 1, 2
 KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
@@ -99,6 +99,9 @@ def load_library():
     L.fsi_block_timer.argtypes = [VP, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_set_kernel.argtypes = [VP, C.c_int]
     L.fsi_block_set_ib_mode.argtypes = [VP, C.c_int]
+    L.fsi_block_pack_flow.argtypes = [VP, DP, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_float)]
+    L.fsi_block_flux.argtypes = [VP, DP, C.c_double, C.c_double, DP]
+    L.fsi_block_probes.argtypes = [VP, DP, C.c_int, DP, C.c_double, DP]
     L.fsi_batch_create.argtypes = [C.POINTER(VP), C.c_int, C.POINTER(VP)]
     L.fsi_batch_destroy.argtypes = [VP]
     L.fsi_batch_ib_step.argtypes = [VP, DP, DP, DP, DP, DP, DP, DP, C.c_int, C.c_double, DP, DP, IP, DP]
@@ -275,6 +278,32 @@ class Block:
     def set_kernel(self, kernel):
         """bulk step kernel of the offset forms: KERNEL_AUTO, _PAIRED, _PIPELINED"""
         _check(load_library().fsi_block_set_kernel(self.h, int(kernel)))
+
+    # -- outputs (main.f90:107-141), packed on the GPU --
+    def pack_flow(self, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, Uref=1.0, offset=0):
+        """write_flow_ fields: FP32 array (4, nx, ny, nz) of p, u, v, w"""
+        X, Y, Z = self.dims
+        nx, ny, nz = X - 2 * offset, Y - 2 * offset, Z - 2 * offset
+        out = np.empty((4, nx, ny, nz), dtype=np.float32)
+        vf = _vec3(volumeForce)
+        _check(load_library().fsi_block_pack_flow(self.h, _dp(vf), denIn, Uref, int(offset), _fp(out)))
+        return out
+
+    def flux(self, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, Uref=1.0):
+        """write_fluid_flux: (in, mid, out) normalised x-fluxes"""
+        f = np.empty(3)
+        vf = _vec3(volumeForce)
+        _check(load_library().fsi_block_flux(self.h, _dp(vf), denIn, Uref, _dp(f)))
+        return f
+
+    def probes(self, xyz, volumeForce=(0.0, 0.0, 0.0), Uref=1.0):
+        """fluid probes: (n, 3) velocities / Uref at the points xyz (n, 3)"""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        n = xyz.size // 3
+        uvw = np.empty(3 * max(n, 1))
+        vf = _vec3(volumeForce)
+        _check(load_library().fsi_block_probes(self.h, _dp(vf), n, _dp(xyz), Uref, _dp(uvw)))
+        return uvw[:3 * n].reshape(-1, 3)
 
     def set_ib_mode(self, mode):
         """IB stage of ib_step: IB_GRID (cooperative, then the step) or

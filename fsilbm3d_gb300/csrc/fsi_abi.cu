@@ -145,6 +145,8 @@ struct fsi_block {
     cudaEvent_t ev_fork = nullptr;
     double *h_ef = nullptr;  // pinned staging of the Lagrangian force (fsi_block_ib_step)
     int h_ef_cap = 0;
+    void *d_out = nullptr;   // output packing scratch
+    size_t out_cap = 0;
     // immersed boundary
     int nb = 0, Mtot = 0;
     std::vector<int> M, offs;
@@ -355,7 +357,7 @@ void free_block(fsi_block *h) {
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
                     h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
-                    h->d_feat};
+                    h->d_feat, h->d_out};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -535,6 +537,75 @@ int fsi_block_download_f(fsi_block_t h, double *fIn) {
         CK(launch_convert_from_store(h->fa, h->stage, h->N, h->prec, h->st));
         CK(cudaMemcpyAsync(fIn, h->stage, n * 8, cudaMemcpyDeviceToHost, h->st));
     }
+    return check_kerr(h);
+}
+
+// ---------------------------------------------------------------- outputs
+
+namespace {
+// den/u of the current state into the block's full-size arrays
+int macro_device(fsi_block *h, const double vf[3]) {
+    double z3[3] = {0, 0, 0};
+    const double *v = vf ? vf : z3;
+    if (h->prec == FSI_PREC_F64) CK(launch_macro_f64((const double *)h->fa, h->den, h->u, h->X, h->Y, h->Z, h->d.dh, v, h->st));
+    else CK(launch_macro_fast(h->fa, h->prec, h->den, h->u, h->X, h->Y, h->Z, h->d.dh, v, h->st));
+    return FSI_OK;
+}
+
+int out_scratch(fsi_block *h, size_t bytes) {
+    if (bytes <= h->out_cap) return FSI_OK;
+    CK(cudaStreamSynchronize(h->st));
+    if (h->d_out) cudaFree(h->d_out);
+    h->d_out = nullptr;
+    h->out_cap = 0;
+    CK(cudaMalloc(&h->d_out, bytes));
+    h->out_cap = bytes;
+    return FSI_OK;
+}
+}  // namespace
+
+int fsi_block_pack_flow(fsi_block_t h, const double vf[3], double denIn, double Uref, int offset, float *out) {
+    if (!h || !out) return fail(FSI_E_ARG, "null argument");
+    if (!(Uref != 0.0)) return fail(FSI_E_ARG, "Uref must be nonzero");
+    if (offset < 0 || 2 * offset >= h->X || 2 * offset >= h->Y || 2 * offset >= h->Z)
+        return fail(FSI_E_ARG, "offset %d leaves no output cells", offset);
+    const size_t n = (size_t)(h->X - 2 * offset) * (h->Y - 2 * offset) * (h->Z - 2 * offset);
+    if (int rc = macro_device(h, vf)) return rc;
+    if (int rc = out_scratch(h, sizeof(float) * 4 * n)) return rc;
+    CK(launch_pack_flow(h->den, h->u, h->X, h->Y, h->Z, offset, denIn, Uref, (float *)h->d_out, h->st));
+    CK(cudaMemcpyAsync(out, h->d_out, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, h->st));
+    return check_kerr(h);
+}
+
+int fsi_block_flux(fsi_block_t h, const double vf[3], double denIn, double Uref, double flux[3]) {
+    if (!h || !flux) return fail(FSI_E_ARG, "null argument");
+    if (int rc = macro_device(h, vf)) return rc;
+    if (int rc = out_scratch(h, sizeof(double) * 3)) return rc;
+    CK(launch_flux(h->den, h->u, h->X, h->Y, h->Z, h->d.dh, (double *)h->d_out, h->st));
+    double raw[3];
+    CK(cudaMemcpyAsync(raw, h->d_out, sizeof(double) * 3, cudaMemcpyDeviceToHost, h->st));
+    if (int rc = check_kerr(h)) return rc;
+    const double Yref = h->ymax - h->d.ymin, Zref = h->zmax - h->d.zmin;
+    for (int k = 0; k < 3; k++) flux[k] = raw[k] / (((denIn * Uref) * Zref) * Yref);
+    return FSI_OK;
+}
+
+int fsi_block_probes(fsi_block_t h, const double vf[3], int n, const double *xyz, double Uref, double *uvw) {
+    if (!h || n < 0 || (n > 0 && (!xyz || !uvw))) return fail(FSI_E_ARG, "invalid argument");
+    if (n == 0) return FSI_OK;
+    const double xmax = h->d.xmin + h->d.dh * (h->X - 1), ymax = h->d.ymin + h->d.dh * (h->Y - 1),
+                 zmax = h->d.zmin + h->d.dh * (h->Z - 1);
+    for (int i = 0; i < n; i++) {
+        const double *c = xyz + 3 * i;
+        if (c[0] < h->d.xmin || c[0] > xmax || c[1] < h->d.ymin || c[1] > ymax || c[2] < h->d.zmin || c[2] > zmax)
+            return fail(FSI_E_RANGE, "fluid probe %d is not in selected block", i + 1);  // FlowCondition.f90:205-210
+    }
+    if (int rc = macro_device(h, vf)) return rc;
+    if (int rc = out_scratch(h, sizeof(double) * 6 * n)) return rc;
+    double *d_xyz = (double *)h->d_out, *d_uvw = d_xyz + 3 * n;
+    CK(cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->st));
+    CK(launch_probes(h->u, h->X, h->Y, h->Z, h->d.dh, h->d.xmin, h->d.ymin, h->d.zmin, n, d_xyz, Uref, d_uvw, h->st));
+    CK(cudaMemcpyAsync(uvw, d_uvw, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
     return check_kerr(h);
 }
 

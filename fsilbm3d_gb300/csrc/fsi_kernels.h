@@ -73,6 +73,14 @@ cudaError_t launch_ib_coop(const IbCoop &a, int prec, int grid, cudaStream_t st)
 cudaError_t launch_ib_cluster(const IbCoop &a, int prec, cudaStream_t st);
 int ib_coop_grid(int prec);  // co-resident CTAs (256 threads) on this device, 0 on error
 
+// ---- output packing (k_f64_exact.cu, reference operation order) ----
+cudaError_t launch_pack_flow(const double *den, const double *u, int X, int Y, int Z, int off, double denIn,
+                             double Uref, float *out, cudaStream_t st);
+cudaError_t launch_flux(const double *den, const double *u, int X, int Y, int Z, double dh, double *flux,
+                        cudaStream_t st);
+cudaError_t launch_probes(const double *u, int X, int Y, int Z, double dh, double xmin, double ymin, double zmin, int n,
+                          const double *xyz, double Uref, double *out, cudaStream_t st);
+
 // ---- block refinement (k_f64_exact.cu) ----
 struct PairGeom {
     int sds[6], s[6], f[6], si[6], fi[6];

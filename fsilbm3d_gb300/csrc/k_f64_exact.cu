@@ -399,6 +399,78 @@ __global__ void k_ib_spread(const float *__restrict__ ew, const int *__restrict_
     wforce[wc + 2 * Nw] = a2 + vf2;
 }
 
+// ---------------------------------------------------------------- outputs
+// write_flow_ (FluidDomain.f90:1651-1663), outputtype 1: the FP32 output
+// fields over the block minus `off` cells on every side, (z,y,x,k) order:
+// p = Cs2 (den - denIn) and u/Uref, rounded from FP64 as the reference's
+// real(4) OUTtmp
+__global__ void k_pack_flow(const double *__restrict__ den, const double *__restrict__ u, long long N, int X, int Y,
+                            int Z, int off, double denIn, double invUref, float *out) {
+    const int nz = Z - 2 * off, ny = Y - 2 * off, nx = X - 2 * off;
+    const long long n = (long long)nz * ny * nx;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int zz = (int)(i % nz);
+    const long long t = i / nz;
+    const int yy = (int)(t % ny), xx = (int)(t / ny);
+    const long long c = cidx(zz + off, yy + off, xx + off, Z, Y);
+    const double Cs2 = 1.0 / 3.0;  // ConstParams.f90:39
+    out[i] = (float)(Cs2 * (den[c] - denIn));
+    out[i + n] = (float)(u[c] * invUref);
+    out[i + 2 * n] = (float)(u[c + N] * invUref);
+    out[i + 3 * n] = (float)(u[c + 2 * N] * invUref);
+}
+
+// write_fluid_flux (FluidDomain.f90:2019-2056): the x-flux through the
+// planes x = 1, (xDim+1)/2 and xDim (1-based), one thread per plane summing
+// in the reference's loop order (z outer, y inner) with its trapezoid weights
+__global__ void k_flux(const double *__restrict__ den, const double *__restrict__ u, long long N, int X, int Y, int Z,
+                       double dh, double *flux) {
+    const int p = threadIdx.x;
+    if (p >= 3) return;
+    const int x = p == 0 ? 0 : (p == 1 ? (X + 1) / 2 - 1 : X - 1);
+    double s = 0.0;
+    for (int k = 0; k < Z; k++) {
+        const double wz = (k == 0 || k == Z - 1) ? 0.5 : 1.0;
+        for (int j = 0; j < Y; j++) {
+            const double wy = (j == 0 || j == Y - 1) ? 0.5 : 1.0;
+            const long long c = cidx(k, j, x, Z, Y);
+            s = s + ((((u[c] * den[c]) * dh) * dh) * wy) * wz;
+        }
+    }
+    flux[p] = s;
+}
+
+// grid_value_interpolation (Util.f90:123-158): trilinear velocity at probe
+// points, one thread per probe and component; points on the last grid plane
+// take their upper neighbour as the same plane (its weight is zero)
+__global__ void k_probes(const double *__restrict__ u, long long N, int X, int Y, int Z, double dh, double xmin,
+                         double ymin, double zmin, int n, const double *__restrict__ xyz, double invUref, double *out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * n) return;
+    const int i = t / 3, comp = t % 3;
+    const double cx = xyz[3 * i], cy = xyz[3 * i + 1], cz = xyz[3 * i + 2];
+    int x1 = (int)floor((cx - xmin) / dh + 1.0), y1 = (int)floor((cy - ymin) / dh + 1.0),
+        z1 = (int)floor((cz - zmin) / dh + 1.0);
+    int x2 = x1 + 1, y2 = y1 + 1, z2 = z1 + 1;
+    const double dx1 = cx - (xmin + dh * (double)(x1 - 1));
+    const double dy1 = cy - (ymin + dh * (double)(y1 - 1));
+    const double dz1 = cz - (zmin + dh * (double)(z1 - 1));
+    const double dx2 = dh - dx1, dy2 = dh - dy1, dz2 = dh - dz1;
+    x2 = x2 > X ? X : x2;
+    y2 = y2 > Y ? Y : y2;
+    z2 = z2 > Z ? Z : z2;
+    const double coffe = 1.0 / ((dh * dh) * dh);
+    const double c1 = ((dx2 * dy2) * dz2) * coffe, c2 = ((dx2 * dy2) * dz1) * coffe, c3 = ((dx2 * dy1) * dz2) * coffe,
+                 c4 = ((dx1 * dy2) * dz2) * coffe, c5 = ((dx2 * dy1) * dz1) * coffe, c6 = ((dx1 * dy2) * dz1) * coffe,
+                 c7 = ((dx1 * dy1) * dz2) * coffe, c8 = ((dx1 * dy1) * dz1) * coffe;
+    const double *v = u + N * comp;
+    auto at = [&](int z, int y, int x) { return v[cidx(z - 1, y - 1, x - 1, Z, Y)]; };
+    const double val = ((((((c1 * at(z1, y1, x1) + c2 * at(z2, y1, x1)) + c3 * at(z1, y2, x1)) + c4 * at(z1, y1, x2)) +
+                          c5 * at(z2, y2, x1)) + c6 * at(z2, y1, x2)) + c7 * at(z1, y2, x2)) + c8 * at(z2, y2, x2);
+    out[t] = val * invUref;
+}
+
 // ------------------------------------------------------- block refinement
 // The face kernels check every global index against its buffer; the first
 // out-of-range access is recorded in err (code, index low, index high) and
@@ -680,6 +752,29 @@ cudaError_t launch_ib_spread(const float *ew, const int *start, const int *list,
     if (Nw <= 0) return cudaSuccess;
     k_ib_spread<<<(unsigned)((Nw + 127) / 128), 128, 0, st>>>(ew, start, list, Nw, eforce, invh3, vf[0], vf[1],
                                                                vf[2], wforce);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_flow(const double *den, const double *u, int X, int Y, int Z, int off, double denIn,
+                             double Uref, float *out, cudaStream_t st) {
+    const long long n = (long long)(Z - 2 * off) * (Y - 2 * off) * (X - 2 * off);
+    if (n <= 0) return cudaSuccess;
+    k_pack_flow<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(den, u, (long long)X * Y * Z, X, Y, Z, off, denIn,
+                                                             1.0 / Uref, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flux(const double *den, const double *u, int X, int Y, int Z, double dh, double *flux,
+                        cudaStream_t st) {
+    k_flux<<<1, 32, 0, st>>>(den, u, (long long)X * Y * Z, X, Y, Z, dh, flux);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probes(const double *u, int X, int Y, int Z, double dh, double xmin, double ymin, double zmin, int n,
+                          const double *xyz, double Uref, double *out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_probes<<<(3 * n + 127) / 128, 128, 0, st>>>(u, (long long)X * Y * Z, X, Y, Z, dh, xmin, ymin, zmin, n, xyz,
+                                                  1.0 / Uref, out);
     return cudaGetLastError();
 }
 

@@ -104,6 +104,22 @@ int fsi_block_set_boundary_conditions(fsi_block_t h, double blktime);
  * den (N) and uuu (3N) are written to the host if non-NULL */
 int fsi_block_macro(fsi_block_t h, const double vf[3], double *den, double *uuu);
 
+/* Output packing on the GPU (the outputs of main.f90:107-141), each from the
+ * macro quantities of the current state with volume force vf:
+ * write_flow_ (FluidDomain.f90:1628-1663, outputtype 1): out (z,y,x,k), the
+ * block minus `offset` cells (offsetOutput) on each side, k = p, u, v, w as
+ * FP32: p = (den - denIn)/3, u/Uref. */
+int fsi_block_pack_flow(fsi_block_t h, const double vf[3], double denIn, double Uref, int offset,
+                        float *out);
+/* write_fluid_flux (FluidDomain.f90:2019-2056): x-fluxes through the planes
+ * x = 1, (xDim+1)/2, xDim, divided by denIn*Uref*(zmax-zmin)*(ymax-ymin) */
+int fsi_block_flux(fsi_block_t h, const double vf[3], double denIn, double Uref, double flux[3]);
+/* write_fluid_information probes (FlowCondition.f90:195-223 with
+ * grid_value_interpolation, Util.f90:123-158): trilinear velocity / Uref at
+ * n points xyz (3,n) into uvw (3,n); a point outside the block returns
+ * FSI_E_RANGE (the reference stops) */
+int fsi_block_probes(fsi_block_t h, const double vf[3], int n, const double *xyz, double Uref, double *uvw);
+
 /* The fluid part of one time step, LBMBlockComm.f90:288-303:
  * add_volume_force_ (FluidDomain.f90:1182), collision_ (:1208),
  * halfwayBCset_ (:567), streaming_ (:1514), set_boundary_conditions_ (:616).

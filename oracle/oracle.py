@@ -280,3 +280,60 @@ def mrt_matrices(omega):
     mf = np.zeros(361)
     lib().or_mrt_matrices(omega, _dp(mc), _dp(mf))
     return mc.reshape(19, 19, order="F"), mf.reshape(19, 19, order="F")
+
+
+# ---------------------------------------------------------------- outputs
+# Restatements of the reference's output arithmetic on den/uuu (FP64, the
+# reference's operation order), for the checks of the packing kernels.
+
+def pack_flow(den, u, X, Y, Z, off, denIn, Uref):
+    """write_flow_, FluidDomain.f90:1651-1663: FP32 (4, nx, ny, nz) of
+    p = Cs2 (den - denIn), u/Uref over the block minus `off` cells per side"""
+    d = np.asarray(den).reshape(X, Y, Z)[off:X - off, off:Y - off, off:Z - off]
+    uu = np.asarray(u).reshape(3, X, Y, Z)[:, off:X - off, off:Y - off, off:Z - off]
+    inv = 1.0 / Uref
+    out = np.empty((4,) + d.shape, dtype=np.float32)
+    out[0] = ((1.0 / 3.0) * (d - denIn)).astype(np.float32)
+    for k in range(3):
+        out[1 + k] = (uu[k] * inv).astype(np.float32)
+    return out
+
+
+def flux(den, u, X, Y, Z, dh, denIn, Uref, Yref, Zref):
+    """write_fluid_flux, FluidDomain.f90:2019-2056 (serial sums, z outer)"""
+    d = np.asarray(den).reshape(X, Y, Z)
+    ux = np.asarray(u).reshape(3, X, Y, Z)[0]
+    res = []
+    for x in (0, (X + 1) // 2 - 1, X - 1):
+        s = 0.0
+        for k in range(Z):
+            wz = 0.5 if (k == 0 or k == Z - 1) else 1.0
+            for j in range(Y):
+                wy = 0.5 if (j == 0 or j == Y - 1) else 1.0
+                s = s + ((((float(ux[x, j, k]) * float(d[x, j, k])) * dh) * dh) * wy) * wz
+        res.append(s / (((denIn * Uref) * Zref) * Yref))
+    return np.array(res)
+
+
+def probe(u, X, Y, Z, dh, origin, point, Uref):
+    """grid_value_interpolation, Util.f90:123-158, for the three components"""
+    xmin, ymin, zmin = origin
+    uu = np.asarray(u).reshape(3, X, Y, Z)
+    cx, cy, cz = point
+    x1 = int(np.floor((cx - xmin) / dh + 1.0)); y1 = int(np.floor((cy - ymin) / dh + 1.0))
+    z1 = int(np.floor((cz - zmin) / dh + 1.0))
+    x2, y2, z2 = min(x1 + 1, X), min(y1 + 1, Y), min(z1 + 1, Z)
+    dx1 = cx - (xmin + dh * (x1 - 1)); dy1 = cy - (ymin + dh * (y1 - 1)); dz1 = cz - (zmin + dh * (z1 - 1))
+    dx2, dy2, dz2 = dh - dx1, dh - dy1, dh - dz1
+    co = 1.0 / ((dh * dh) * dh)
+    c = [((dx2 * dy2) * dz2) * co, ((dx2 * dy2) * dz1) * co, ((dx2 * dy1) * dz2) * co, ((dx1 * dy2) * dz2) * co,
+         ((dx2 * dy1) * dz1) * co, ((dx1 * dy2) * dz1) * co, ((dx1 * dy1) * dz2) * co, ((dx1 * dy1) * dz1) * co]
+    idx = [(z1, y1, x1), (z2, y1, x1), (z1, y2, x1), (z1, y1, x2), (z2, y2, x1), (z2, y1, x2), (z1, y2, x2),
+           (z2, y2, x2)]
+    out = []
+    for k in range(3):
+        v = 0.0
+        for ci, (z, y, x) in zip(c, idx):
+            v = v + ci * float(uu[k, x - 1, y - 1, z - 1])
+        out.append(v * (1.0 / Uref))
+    return np.array(out)
