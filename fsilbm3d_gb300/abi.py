@@ -42,6 +42,7 @@ class BlockDesc(C.Structure):
         ("uvwIn", C.c_double * 3),
         ("shearRateIn", C.c_double * 3),
         ("velocityKind", C.c_int),
+        ("params", C.c_double * 10),
     ]
 
 
@@ -59,6 +60,7 @@ SYMBOLS = [
     "fsi_block_set_kernel", "fsi_block_ib_step",
     "fsi_batch_create", "fsi_batch_destroy", "fsi_batch_ib_step", "fsi_batch_tune", "fsi_batch_set_threads",
     "fsi_block_set_ib_mode", "fsi_block_pack_flow", "fsi_block_flux", "fsi_block_probes",
+    "fsi_block_get_omega2", "fsi_block_get_tau_all",
 ]
 IB_AUTO, IB_GRID, IB_CLUSTER = 0, 1, 2
 KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
@@ -89,6 +91,8 @@ def load_library():
     L.fsi_block_create.argtypes = [C.POINTER(VP), C.POINTER(BlockDesc)]
     L.fsi_block_destroy.argtypes = [VP]
     L.fsi_block_get_params.argtypes = [VP, DP, DP, DP, DP]
+    L.fsi_block_get_omega2.argtypes = [VP, DP]
+    L.fsi_block_get_tau_all.argtypes = [VP, DP]
     L.fsi_block_upload_f.argtypes = [VP, DP]
     L.fsi_block_download_f.argtypes = [VP, DP]
     L.fsi_block_initialise.argtypes = [VP, C.c_double]
@@ -174,7 +178,7 @@ class Block:
 
     def __init__(self, xDim, yDim, zDim, dh=1.0, origin=(0.0, 0.0, 0.0), bndConds=(301,) * 6, iCollidModel=1,
                  nu=0.1 / 3.0, precision=PREC_F64, denIn=1.0, uvwIn=(0.0, 0.0, 0.0), shearRateIn=(0.0, 0.0, 0.0),
-                 velocityKind=0, m_collid=None, m_force=None):
+                 velocityKind=0, m_collid=None, m_force=None, params=None):
         L = load_library()
         d = BlockDesc()
         d.xDim, d.yDim, d.zDim = int(xDim), int(yDim), int(zDim)
@@ -193,6 +197,8 @@ class Block:
         d.uvwIn[:] = list(uvwIn)
         d.shearRateIn[:] = list(shearRateIn)
         d.velocityKind = int(velocityKind)
+        if params is not None:
+            d.params[:len(params)] = [float(v) for v in params]
         self.desc = d
         self.dims = (int(xDim), int(yDim), int(zDim))
         self.N = int(xDim) * int(yDim) * int(zDim)
@@ -225,6 +231,19 @@ class Block:
         mf = np.zeros(361)
         _check(load_library().fsi_block_get_params(self.h, C.byref(tau), C.byref(om), _dp(mc), _dp(mf)))
         return tau.value, om.value, mc.reshape(19, 19, order="F"), mf.reshape(19, 19, order="F")
+
+    def omega2(self):
+        """Omega2 of the TRT model (0 for the others)"""
+        v = C.c_double()
+        _check(load_library().fsi_block_get_omega2(self.h, C.byref(v)))
+        return v.value
+
+    def tau_all(self):
+        """tau_all(z,y,x) as an array of shape (xDim, yDim, zDim)"""
+        X, Y, Z = self.dims
+        out = np.empty((X, Y, Z))
+        _check(load_library().fsi_block_get_tau_all(self.h, _dp(out)))
+        return out
 
     # -- state transfer (write_continue_/read_continue_ layout) --
     def upload_f(self, f):

@@ -128,6 +128,9 @@ struct fsi_block {
     int X = 0, Y = 0, Z = 0;
     long long N = 0;
     double tau = 0, omega = 0, xmax = 0, ymax = 0, zmax = 0;
+    double omega2 = 0;          // TRT antisymmetric rate
+    double cles = 0;            // constant of the LES model (ConstParams.f90:40-45)
+    double *tau_all = nullptr;  // per-cell relaxation time of the LES models (N)
     int periodic[3] = {0, 0, 0};
     MrtMats mm{};
     int prec = 0;
@@ -301,6 +304,11 @@ void fill_step(fsi_block *h, const double vf[3], double blktime, bool use_window
     a.u = h->u;
     a.kerr = h->d_status + 4;
     a.variant = h->kernel;
+    a.omega2 = h->omega2;
+    a.tau = h->tau;
+    a.nu = h->d.nu;
+    a.cles = h->cles;
+    a.tau_all = h->tau_all;
     // z faces of code 101 with a face velocity uniform over the face: the
     // paired kernels write their equilibrium while streaming
     if (is_fast(h) && step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel)) {
@@ -334,8 +342,18 @@ int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_wind
     StepArgs a;
     fill_step(h, vf, blktime, use_window, a);
     a.join = (void *)join;
-    cudaError_t e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
-                               : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
+    cudaError_t e = cudaSuccess;
+    // only the paired kernels defer their IB-window work behind the join
+    // event; every other step waits for the IB stage before it starts
+    if (join && !(is_fast(h) && step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel))) {
+        e = cudaStreamWaitEvent(h->st, join, 0);
+        a.join = nullptr;
+    }
+    if (e == cudaSuccess && grad_model(h->d.iCollidModel))
+        e = is_fast(h) ? launch_step_macro_fast(a, h->prec, h->st) : launch_step_macro_f64(a, h->st);
+    if (e == cudaSuccess)
+        e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
+                       : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
     if (e != cudaSuccess) return fail(FSI_E_CUDA, "step kernel: %s", cudaGetErrorString(e));
     int rc = apply_bcs(h, h->fb, blktime, a.zeq);
     if (rc) return rc;
@@ -357,7 +375,7 @@ void free_block(fsi_block *h) {
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
                     h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
-                    h->d_feat, h->d_out};
+                    h->d_feat, h->d_out, h->tau_all};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -408,8 +426,18 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     if (d->xDim > 32767 || d->yDim > 32767 || d->zDim > 32767)
         return fail(FSI_E_ARG, "Grid number exceeds 32767, please try to reduced the grid size.");
     if (!(d->dh > 0.0)) return fail(FSI_E_ARG, "dh must be positive");
-    if (d->iCollidModel != 1 && d->iCollidModel != 3)
-        return fail(FSI_E_ARG, "iCollidModel %d not supported (1 SRT, 3 MRT)", d->iCollidModel);
+    if (d->iCollidModel == 12)
+        return fail(FSI_E_ARG, "iCollidModel 12 (RBGK) is not supported: the reference's branch relaxes with an "
+                               "uninitialised rate (FluidDomain.f90:1240-1243)");
+    if (d->iCollidModel == 13)
+        return fail(FSI_E_ARG, "iCollidModel 13 (ELBM) is not supported: the reference's branch sums an "
+                               "uninitialised array x3 (FluidDomain.f90:1296-1301)");
+    {
+        const int m = d->iCollidModel;
+        if (m != CM_SRT && m != CM_TRT && m != CM_MRT && !les_model(m))
+            return fail(FSI_E_ARG, "iCollidModel %d not supported (1 SRT, 2 TRT, 3 MRT, 11 Smagorinsky, 14 WALE, "
+                                   "15 Vreman)", m);
+    }
     if (d->precision < FSI_PREC_F64 || d->precision > FSI_PREC_BF16) return fail(FSI_E_ARG, "unknown precision");
     if (d->velocityKind != 0 && d->velocityKind != 2)
         return fail(FSI_E_ARG, "velocityKind %d not supported (0 shear, 2 oscillatory)", d->velocityKind);
@@ -438,6 +466,17 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     // calculate_SRT_params, FluidDomain.f90:450-456
     h->tau = d->nu / (d->dh * (1.0 / 3.0)) + 0.5;
     h->omega = 1.0 / h->tau;
+    // calculate_TRT_params, FluidDomain.f90:458-464
+    if (d->iCollidModel == CM_TRT) {
+        const double tmp = (d->params[0] * 4.0 - 1.0) * h->omega + 2.0;
+        h->omega2 = (2.0 * (2.0 - h->omega)) / tmp;
+        if (!std::isfinite(h->omega2)) return fail(FSI_E_ARG, "TRT: Lambda %g gives no finite Omega2", d->params[0]);
+    }
+    // CsmagConst, CWALEConst, CvremConst (ConstParams.f90:40-45), each
+    // product rounded in turn
+    if (d->iCollidModel == CM_SMAG) h->cles = ((2.0 * 0.17) * 0.17) * std::sqrt(2.0) * 9.0;
+    else if (d->iCollidModel == CM_WALE) h->cles = 0.5 * 0.5;
+    else if (d->iCollidModel == CM_VREM) h->cles = (2.5 * 0.17) * 0.17;
     if (d->m_collid && d->m_force) {
         memcpy(h->mm.mc, d->m_collid, sizeof(double) * 361);
         memcpy(h->mm.mf, d->m_force, sizeof(double) * 361);
@@ -465,6 +504,10 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     chk(cudaMalloc(&h->fb, fbytes));
     chk(cudaMalloc((void **)&h->den, sizeof(double) * h->N));
     chk(cudaMalloc((void **)&h->u, sizeof(double) * 3 * h->N));
+    if (les_model(d->iCollidModel)) {
+        chk(cudaMalloc((void **)&h->tau_all, sizeof(double) * h->N));
+        if (e == cudaSuccess) chk(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
+    }
     if (h->prec != FSI_PREC_F64 && h->prec != FSI_PREC_F64_FAST)
         chk(cudaMalloc((void **)&h->stage, sizeof(double) * 19 * (size_t)h->N));
     for (int k = 0; k < 6; k++) {
@@ -512,6 +555,23 @@ int fsi_block_get_params(fsi_block_t h, double *tau, double *omega, double *m_co
     if (omega) *omega = h->omega;
     if (m_collid) memcpy(m_collid, h->mm.mc, sizeof(double) * 361);
     if (m_force) memcpy(m_force, h->mm.mf, sizeof(double) * 361);
+    return FSI_OK;
+}
+
+int fsi_block_get_omega2(fsi_block_t h, double *omega2) {
+    if (!h || !omega2) return fail(FSI_E_ARG, "null argument");
+    *omega2 = h->omega2;
+    return FSI_OK;
+}
+
+int fsi_block_get_tau_all(fsi_block_t h, double *tau_all) {
+    if (!h || !tau_all) return fail(FSI_E_ARG, "null argument");
+    if (!h->tau_all) {
+        for (long long i = 0; i < h->N; i++) tau_all[i] = h->tau;
+        return FSI_OK;
+    }
+    CK(cudaMemcpyAsync(tau_all, h->tau_all, sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return FSI_OK;
 }
 
@@ -616,6 +676,8 @@ int fsi_block_initialise(fsi_block_t h, double time) {
     CK(launch_init_f64(dst, h->den, h->u, h->X, h->Y, h->Z, h->d.dh, h->d.xmin, h->d.ymin, h->d.zmin, h->d.denIn, v,
                        time, h->st));
     if (h->esz != 8) CK(launch_convert_to_store(h->stage, h->fa, h->N, h->prec, h->st));
+    // calculate_SRT_params (FluidDomain.f90:450-456) resets tau_all
+    if (h->tau_all) CK(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
     CK(cudaStreamSynchronize(h->st));
     return FSI_OK;
 }
@@ -1219,7 +1281,7 @@ int fsi_pair_extract(fsi_pair_t p, int time_level) {
     fsi_block *fa = p->fa;
     for (int k = 0; k < 6; k++) {
         if (p->so->d.bndConds[k] != BC_FLUID) continue;
-        CK(launch_pair_extract((const double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, p->p, k, p->buf[k][time_level - 1],
+        CK(launch_pair_extract((const double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, fa->tau_all, p->p, k, p->buf[k][time_level - 1],
                                p->buft[k][time_level - 1], p->d_err, fa->st));
         if (time_level == 2) {
             int ax = k >> 1;
@@ -1239,7 +1301,7 @@ int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]) {
     for (int k = 0; k < 6; k++) {
         if (p->p.sds[k] == 0) continue;
         int lvl = (n_timeStep == 0) ? 0 : 1;
-        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
+        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, so->tau_all, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
                            p->scheme, p->scr_f, p->scr_t, p->scr_cells, vf, fa->d.dh, p->d_err, so->st));
     }
     CK(cudaStreamSynchronize(so->st));
@@ -1253,8 +1315,8 @@ int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
     for (int k = 0; k < 6; k++) {
         int want = (k % 2 == 0) ? 1 : -1;
         if (p->p.sds[k] != want) continue;
-        CK(launch_pair_s2f((double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, (const double *)so->fa, so->X, so->Y, so->Z,
-                           so->tau, p->p, k, vf, so->d.dh, p->d_err, fa->st));
+        CK(launch_pair_s2f((double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, fa->tau_all, (const double *)so->fa, so->X,
+                           so->Y, so->Z, so->tau, so->tau_all, p->p, k, vf, so->d.dh, p->d_err, fa->st));
     }
     CK(cudaStreamSynchronize(fa->st));
     return pair_check(p);
@@ -1896,7 +1958,7 @@ extern "C" int fsi_pair_father_to_son_static(fsi_pair_t p, int n_timeStep, const
     for (int k = 0; k < 6; k++) {
         if (p->p.sds[k] == 0) continue;
         int lvl = (n_timeStep == 0) ? 0 : 1;
-        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
+        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, so->tau_all, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
                            p->scheme, scr_f, scr_t, FSI_STATIC_FACE_CELLS, vf, fa->d.dh, p->d_err, so->st));
     }
     CK(cudaStreamSynchronize(so->st));

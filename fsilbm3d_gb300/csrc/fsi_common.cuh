@@ -33,6 +33,18 @@ __host__ __device__ constexpr double wt_(int i) {
     return i == 0 ? 1.0 / 3.0 : (i <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
 }
 
+// representatives of the nine opposite pairs (positivedirs, ConstParams.f90:19);
+// opp_ of them gives negativedirs (ConstParams.f90:20) in the same order
+__host__ __device__ constexpr int pr_(int k) {
+    return k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 5 : k == 3 ? 7 : k == 4 ? 8 : k == 5 ? 11 : k == 6 ? 12 : k == 7 ? 15 : 16;
+}
+
+// collision models (iCollidModel, FluidDomain.f90:1225-1262)
+enum : int { CM_SRT = 1, CM_TRT = 2, CM_MRT = 3, CM_SMAG = 11, CM_WALE = 14, CM_VREM = 15 };
+__host__ __device__ constexpr bool les_model(int m) { return m == CM_SMAG || m == CM_WALE || m == CM_VREM; }
+// models that read the neighbours' velocity
+__host__ __device__ constexpr bool grad_model(int m) { return m == CM_WALE || m == CM_VREM; }
+
 // incoming population sets per face (x-, x+, y-, y+, z-, z+), FluidDomain.f90:645-1065
 __host__ __device__ constexpr int inc_(int k, int j) {
     return k == 0 ? (j == 0 ? 1 : j == 1 ? 7 : j == 2 ? 9 : j == 3 ? 11 : 13)
@@ -131,6 +143,13 @@ struct StepArgs {
     // host only: an event the window fix-up and face hooks wait for (the IB
     // stage running beside the bulk step on another stream), or null
     void *join;
+    // TRT (iCollidModel 2): the antisymmetric rate Omega2. The SRT collisions
+    // with a per-cell rate (11 Smagorinsky, 14 WALE, 15 Vreman): tau, flow%nu,
+    // the model constant and tau_all(z,y,x), which WALE also reads. WALE and
+    // Vreman read the velocity of each cell and its neighbours from u above,
+    // written for every cell by a macro pass before the step.
+    double omega2, tau, nu, cles;
+    double *tau_all;
 };
 
 struct BcArgs {

@@ -12,6 +12,11 @@ cudaError_t launch_init_f64(double *f, double *den, double *u, int X, int Y, int
 cudaError_t launch_macro_f64(const double *f, double *den, double *u, int X, int Y, int Z,
                              double dh, const double vf[3], cudaStream_t st);
 cudaError_t launch_step_f64_exact(const StepArgs &a, const MrtMats *mm, int model, cudaStream_t st);
+// den/u of every cell as the collision sees them (IB window cells from the IB
+// stage), written to a.den/a.u before the step of a model that reads its
+// neighbours' velocity (grad_model)
+cudaError_t launch_step_macro_f64(const StepArgs &a, cudaStream_t st);
+cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st);
 cudaError_t launch_bc_f64(const BcArgs &a, cudaStream_t st);
 cudaError_t launch_halfway_f64(const double *f, double *hw, int X, int Y, int Z, int face,
                                cudaStream_t st);
@@ -86,16 +91,19 @@ struct PairGeom {
     int sds[6], s[6], f[6], si[6], fi[6];
     int xDimS, xDimF, yDimS, yDimF, zDimS, zDimF;
 };
-cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f,
+// tau: the block's uniform tau, or per cell from tauA (tau_all) when non-null
+cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f,
                                 const PairGeom &p, int face, double *buf, double *buft, int *err,
                                 cudaStream_t st);
 cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaStream_t st);
-cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const PairGeom &p,
-                            int face, const double *buf, const double *buft, int scheme,
+cudaError_t launch_fill_f64(double *p, long long n, double v, cudaStream_t st);
+cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const double *tauA_s,
+                            const PairGeom &p, int face, const double *buf, const double *buft, int scheme,
                             double *scratch_f, double *scratch_t, long long scratch_cells,
                             const double vf[3], double dh, int *err, cudaStream_t st);
-cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *fs,
-                            int SX, int SY, int SZ, double tau_s, const PairGeom &p, int face,
+cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f,
+                            const double *fs, int SX, int SY, int SZ, double tau_s, const double *tauA_s,
+                            const PairGeom &p, int face,
                             const double vf[3], double dh, int *err, cudaStream_t st);
 
 // ---- fast kernels (k_fast.cu): FP64 regrouped, FP32/FP16/BF16 storage ----

@@ -42,6 +42,110 @@ __device__ __forceinline__ void macro_cell(const double f[Q], const double vf[3]
     u2 = (sz + (0.5 * vf[2]) * dh) / den;
 }
 
+// ------------------------------------------------- per-cell relaxation (LES)
+
+// the non-equilibrium stress sums of smag and WALE (FluidDomain.f90:1271-1276)
+// from fneq = -fEq
+__device__ __forceinline__ void neq_stress(const double fEq[Q], double q[6]) {
+    double fn[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) fn[i] = -fEq[i];
+    q[0] = fn[1] + fn[2] + fn[7] + fn[8] + fn[9] + fn[10] + fn[11] + fn[12] + fn[13] + fn[14];
+    q[1] = fn[3] + fn[4] + fn[7] + fn[8] + fn[9] + fn[10] + fn[15] + fn[16] + fn[17] + fn[18];
+    q[2] = fn[5] + fn[6] + fn[11] + fn[12] + fn[13] + fn[14] + fn[15] + fn[16] + fn[17] + fn[18];
+    q[3] = fn[7] - fn[8] - fn[9] + fn[10];
+    q[4] = fn[11] - fn[12] - fn[13] + fn[14];
+    q[5] = fn[15] - fn[16] - fn[17] + fn[18];
+}
+
+// center_diff / onesid_diff with the interior / first / last cell branches of
+// WALE and vrem (FluidDomain.f90:1343-1388, 1425-1491): the derivative of
+// velocity component k along axis d (0 x, 1 y, 2 z), times the reference's
+// invdh = dh
+__device__ __forceinline__ double les_diff(const StepArgs &a, int k, int d, int z, int y, int x, long long c) {
+    const double *__restrict__ u = a.u + a.N * k;
+    const int i = d == 0 ? x : (d == 1 ? y : z);
+    const int D = d == 0 ? a.X : (d == 1 ? a.Y : a.Z);
+    const long long s = d == 0 ? (long long)a.Z * a.Y : (d == 1 ? (long long)a.Z : 1LL);
+    if (i > 0 && i < D - 1) return (u[c + s] - u[c - s]) * a.dh;
+    if (i == 0) return ((-(3.0 * u[c]) + 4.0 * u[c + s]) - u[c + 2 * s]) * a.dh;
+    return ((-(3.0 * u[c]) + 4.0 * u[c - s]) - u[c - 2 * s]) * a.dh;
+}
+
+// smag, FluidDomain.f90:1265-1281
+__device__ __forceinline__ double les_smag(const StepArgs &a, const double fEq[Q], double rho, long long c) {
+    double q[6];
+    neq_stress(fEq, q);
+    const double QQ = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + 2.0 * (q[3] * q[3] + q[4] * q[4] + q[5] * q[5]);
+    const double tau_t = sqrt(a.tau * a.tau + a.cles * sqrt(QQ) / rho);
+    a.tau_all[c] = 0.5 * (a.tau + tau_t);
+    return 2.0 / (a.tau + tau_t);
+}
+
+// WALE, FluidDomain.f90:1304-1416 (the reference's 0.0d0 terms only change
+// the sign of a zero sum, which reaches no output)
+__device__ double les_wale(const StepArgs &a, const double fEq[Q], double rho, int z, int y, int x, long long c) {
+    double q[6];
+    neq_stress(fEq, q);
+    const double invdh = a.dh, tau_ = a.tau_all[c];
+    const double S11 = -(1.5 * invdh * q[0] / (rho * tau_));
+    const double S22 = -(1.5 * invdh * q[1] / (rho * tau_));
+    const double S33 = -(1.5 * invdh * q[2] / (rho * tau_));
+    const double S12 = -(1.5 * invdh * q[3] / (rho * tau_));
+    const double S13 = -(1.5 * invdh * q[4] / (rho * tau_));
+    const double S23 = -(1.5 * invdh * q[5] / (rho * tau_));
+    const double S = S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23);
+    double ox = les_diff(a, 2, 1, z, y, x, c);
+    ox = 0.5 * (ox - les_diff(a, 1, 2, z, y, x, c));
+    double oy = les_diff(a, 0, 2, z, y, x, c);
+    oy = 0.5 * (oy - les_diff(a, 2, 0, z, y, x, c));
+    double oz = les_diff(a, 1, 0, z, y, x, c);
+    oz = 0.5 * (oz - les_diff(a, 0, 1, z, y, x, c));
+    const double O12 = -(0.5 * oz), O13 = 0.5 * oy, O23 = -(0.5 * ox);
+    const double O = 2.0 * (O12 * O12 + O23 * O23 + O13 * O13);
+    const double SO11 = -(S11 * S11 * O12 * O12 + S11 * S11 * O13 * O13 + S12 * S12 * O12 * O12 +
+                          S12 * S12 * O13 * O13 + S13 * S13 * O12 * O12 + S13 * S13 * O13 * O13);
+    const double SO22 = -(S12 * S12 * O12 * O12 + S12 * S12 * O23 * O23 + S22 * S22 * O12 * O12 +
+                          S22 * S22 * O23 * O23 + S23 * S23 * O12 * O12 + S23 * S23 * O23 * O23);
+    const double SO33 = -(S13 * S13 * O13 * O13 + S13 * S13 * O23 * O23 + S23 * S23 * O13 * O13 +
+                          S23 * S23 * O23 * O23 + S33 * S33 * O13 * O13 + S33 * S33 * O23 * O23);
+    const double SO12 = -(S11 * S12 * O13 * O23 + S12 * S22 * O13 * O23 + S13 * S23 * O13 * O23);
+    const double SO13 = (S11 * S13 * O12 * O23 + S12 * S23 * O12 * O23 + S13 * S33 * O12 * O23);
+    const double SO23 = -(S12 * S13 * O12 * O13 + S22 * S23 * O12 * O13 + S23 * S33 * O12 * O13);
+    const double SO = SO11 + SO22 + SO33 + 2.0 * (SO12 + SO13 + SO23);
+    const double SdSd = (S * S + O * O) / 6.0 + 2.0 * S * O / 3.0 + 2.0 * SO;
+    double OP = pow(SdSd, 1.5) / (pow(S, 2.5) + pow(SdSd, 1.25));
+    if (!isfinite(OP) || OP < 0.0) OP = 0.0;
+    const double t = (a.nu + a.cles * OP * a.dh * a.dh) / (a.dh * (1.0 / 3.0)) + 0.5;
+    a.tau_all[c] = t;
+    return 1.0 / t;
+}
+
+// vrem, FluidDomain.f90:1428-1506; a[i][j] = half the derivative of
+// component i along axis j
+__device__ double les_vrem(const StepArgs &a, int z, int y, int x, long long c) {
+    double g[3][3], b[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) g[i][j] = 0.5 * les_diff(a, i, j, z, y, x, c);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) b[i][j] = g[i][j] * g[i][j];
+    const double aa = b[0][0] + b[0][1] + b[0][2] + b[1][0] + b[1][1] + b[1][2] + b[2][0] + b[2][1] + b[2][2];
+    const double r0 = b[0][0] + b[0][1] + b[0][2], r1 = b[1][0] + b[1][1] + b[1][2], r2 = b[2][0] + b[2][1] + b[2][2];
+    const double d01 = g[0][0] * g[1][0] + g[0][1] * g[1][1] + g[0][2] * g[1][2];
+    const double d02 = g[0][0] * g[2][0] + g[0][1] * g[2][1] + g[0][2] * g[2][2];
+    const double d12 = g[1][0] * g[2][0] + g[1][1] * g[2][1] + g[1][2] * g[2][2];
+    const double bb = r0 * r1 - d01 * d01 + r0 * r2 - d02 * d02 + r1 * r2 - d12 * d12;
+    double OP = sqrt(bb / aa);
+    if (!isfinite(OP)) OP = 0.0;
+    const double t = (a.nu + a.cles * OP * a.dh * a.dh) / (a.dh * (1.0 / 3.0)) + 0.5;
+    a.tau_all[c] = t;
+    return 1.0 / t;
+}
+
 // ---------------------------------------------------------------- init/macro
 
 __global__ void k_init(double *f, double *den, double *u, int X, int Y, int Z, double dh, double xmin,
@@ -75,6 +179,32 @@ __global__ void k_macro(const double *__restrict__ f, double *den, double *u, in
     u[c] = u0;
     u[c + N] = u1;
     u[c + 2 * N] = u2;
+}
+
+// den/uuu of every cell as the collision sees them (calculate_macro_quantities_,
+// then the IB stage's values inside its window), written before the step of a
+// model that reads its neighbours' velocity (WALE, Vreman)
+__global__ void k_step_macro(StepArgs a) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
+    if (z >= a.Z) return;
+    const long long c = cidx(z, y, x, a.Z, a.Y);
+    const Win &w = a.win;
+    double d, u0, u1, u2;
+    if (x >= w.x0 && x <= w.x1 && y >= w.y0 && y <= w.y1 && z >= w.z0 && z <= w.z1) {
+        long long wc = (long long)(z - w.z0) + (long long)w.WZ * ((long long)(y - w.y0) + (long long)w.WY * (x - w.x0));
+        d = w.den[wc];
+        u0 = w.u[wc]; u1 = w.u[wc + w.n]; u2 = w.u[wc + 2 * w.n];
+    } else {
+        const double *__restrict__ f = (const double *)a.src;
+        double fl[Q];
+#pragma unroll
+        for (int i = 0; i < Q; i++) fl[i] = f[c + a.N * i];
+        macro_cell(fl, a.vf, a.dh, d, u0, u1, u2);
+    }
+    a.den[c] = d;
+    a.u[c] = u0;
+    a.u[c + a.N] = u1;
+    a.u[c + 2 * a.N] = u2;
 }
 
 // ------------------------------------------------------------ collide+stream
@@ -111,9 +241,11 @@ __global__ void __launch_bounds__(TPB) k_step_exact(StepArgs a, MrtMats mm) {
         // ResetVolumeForce_ then add_volume_force_: 0 + vf
         F0 = 0.0 + a.vf[0]; F1 = 0.0 + a.vf[1]; F2 = 0.0 + a.vf[2];
     }
-    // den/uuu of layer 2 feed the non-equilibrium extrapolation (code 102)
-    if ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
-        (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2)) {
+    // den/uuu of layer 2 feed the non-equilibrium extrapolation (code 102);
+    // the models that read neighbour velocities had them written beforehand
+    if (!grad_model(MODEL) &&
+        ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
+         (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2))) {
         a.den[c] = den;
         a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
     }
@@ -121,7 +253,7 @@ __global__ void __launch_bounds__(TPB) k_step_exact(StepArgs a, MrtMats mm) {
     const double uSqr = (u0 * u0 + u1 * u1) + u2 * u2;
     const double dt3 = 3.0 * a.dh;
     double fo[Q];
-    if (MODEL == 1) {
+    if (MODEL == CM_SRT) {
         const double om = a.omega;
 #pragma unroll
         for (int i = 0; i < Q; i++) {
@@ -144,14 +276,35 @@ __global__ void __launch_bounds__(TPB) k_step_exact(StepArgs a, MrtMats mm) {
                                         (((ey - u1) + (3.0 * uxyz) * ey) * F1)) +
                                        (((ez - u2) + (3.0 * uxyz) * ez) * F2));
         }
+        if (MODEL == CM_MRT) {
 #pragma unroll
-        for (int i = 0; i < Q; i++) {
-            double s1 = 0.0, s2 = 0.0;
+            for (int i = 0; i < Q; i++) {
+                double s1 = 0.0, s2 = 0.0;
 #pragma unroll
-            for (int j = 0; j < Q; j++) s1 += mm.mc[i + Q * j] * fEq[j];
+                for (int j = 0; j < Q; j++) s1 += mm.mc[i + Q * j] * fEq[j];
 #pragma unroll
-            for (int j = 0; j < Q; j++) s2 += mm.mf[i + Q * j] * Flb[j];
-            fo[i] = (f[i] + s1) + s2;
+                for (int j = 0; j < Q; j++) s2 += mm.mf[i + Q * j] * Flb[j];
+                fo[i] = (f[i] + s1) + s2;
+            }
+        } else if (MODEL == CM_TRT) {
+            // TRT collision, FluidDomain.f90:1228-1235
+            const double om = a.omega, om2 = a.omega2;
+            fo[0] = f[0] + (om * fEq[0] + (1.0 - 0.5 * om) * Flb[0]);
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                const int p = pr_(k), m = opp_(p);
+                const double sp = 0.5 * om * (fEq[p] + fEq[m]) + (0.5 - 0.25 * om) * (Flb[p] + Flb[m]);
+                const double sm = 0.5 * om2 * (fEq[p] - fEq[m]) + (0.5 - 0.25 * om2) * (Flb[p] - Flb[m]);
+                fo[p] = f[p] + (sp + sm);
+                fo[m] = f[m] + (sp - sm);
+            }
+        } else {
+            // SRT with a per-cell rate, FluidDomain.f90:1239-1262
+            const double om = MODEL == CM_SMAG ? les_smag(a, fEq, den, c)
+                            : MODEL == CM_WALE ? les_wale(a, fEq, den, z, y, x, c)
+                                               : les_vrem(a, z, y, x, c);
+#pragma unroll
+            for (int i = 0; i < Q; i++) fo[i] = (f[i] + om * fEq[i]) + (1.0 - 0.5 * om) * Flb[i];
         }
     }
 
@@ -485,7 +638,8 @@ __device__ __forceinline__ void rec_err(int *err, int code, long long idx) {
 // extract_interpolate_layer for one son face (LBMBlockComm.f90:354-369):
 // buf(e, a, b) = father fIn on the face plane; buft = father tau
 __global__ void k_pair_extract(const double *__restrict__ ff, int FY, int FZ, long long NF, double tau_f,
-                               PairGeom p, int face, double *buf, double *buft, int A, int B, int *err) {
+                               const double *__restrict__ tauA_f, PairGeom p, int face, double *buf, double *buft,
+                               int A, int B, int *err) {
     int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (a >= A || b >= B) return;
     int ax = face >> 1, xF, yF, zF;
@@ -496,7 +650,12 @@ __global__ void k_pair_extract(const double *__restrict__ ff, int FY, int FZ, lo
     long long o = (long long)a + (long long)A * b;
     if (c < 0 || c >= NF) { rec_err(err, 4, c); return; }
     for (int e = 0; e < Q; e++) buf[e + Q * o] = ff[c + NF * e];
-    buft[o] = tau_f;
+    buft[o] = tauA_f ? tauA_f[c] : tau_f;
+}
+
+__global__ void k_fill(double *p, long long n, double v) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
 }
 
 __global__ void k_pair_average(double *b1, const double *b2, long long n) {
@@ -593,7 +752,8 @@ __global__ void k_pair_interp(int nq, int bF, const double *__restrict__ fFp, lo
 }
 
 // interpolation_father_to_son apply step (LBMBlockComm.f90:685-693)
-__global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, double tau_s, PairGeom p, int face,
+__global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, double tau_s,
+                                 const double *__restrict__ tauA_s, PairGeom p, int face,
                                  const double *tf, const double *tt, int AS, int BS, double vf0, double vf1,
                                  double vf2, double dh, int *err) {
     int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
@@ -605,7 +765,7 @@ __global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, doubl
     long long c = cidx(zS - 1, yS - 1, xS - 1, SZ, SY);
     long long o = (long long)a + (long long)AS * b;
     if (c < 0 || c >= NS) { rec_err(err, 3, c); return; }
-    double coeff = (tau_s / tt[o]) / 2.0;
+    double coeff = ((tauA_s ? tauA_s[c] : tau_s) / tt[o]) / 2.0;
     double fin[Q], vf[3] = {vf0, vf1, vf2};
     for (int e = 0; e < Q; e++) fin[e] = tf[Q * o + e];
     grid_transform(fin, coeff, vf, dh);
@@ -613,8 +773,9 @@ __global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, doubl
 }
 
 // deliver_son_to_father for one face (LBMBlockComm.f90:555-570 and siblings)
-__global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_f, const double *__restrict__ fs,
-                           int SY, int SZ, long long NS, double tau_s, PairGeom p, int face, int n1, int n2,
+__global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_f, const double *__restrict__ tauA_f,
+                           const double *__restrict__ fs, int SY, int SZ, long long NS, double tau_s,
+                           const double *__restrict__ tauA_s, PairGeom p, int face, int n1, int n2,
                            double vf0, double vf1, double vf2, double dh, int *err) {
     int i1 = blockIdx.x * blockDim.x + threadIdx.x, i2 = blockIdx.y;
     if (i1 >= n2 || i2 >= n1) return;
@@ -629,7 +790,7 @@ __global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_
     long long cf = cidx(F[2] - 1, F[1] - 1, F[0] - 1, FZ, FY);
     if (cs < 0 || cs >= NS) { rec_err(err, 5, cs); return; }
     if (cf < 0 || cf >= NF) { rec_err(err, 6, cf); return; }
-    double coeff = (tau_f / tau_s) * 2.0;
+    double coeff = ((tauA_f ? tauA_f[cf] : tau_f) / (tauA_s ? tauA_s[cs] : tau_s)) * 2.0;
     double t[Q], vf[3] = {vf0, vf1, vf2};
     for (int e = 0; e < Q; e++) t[e] = fs[cs + NS * e];
     grid_transform(t, coeff, vf, dh);
@@ -663,13 +824,26 @@ cudaError_t launch_macro_f64(const double *f, double *den, double *u, int X, int
     return cudaGetLastError();
 }
 
+cudaError_t launch_step_macro_f64(const StepArgs &a, cudaStream_t st) {
+    int bz;
+    dim3 g = zgrid(a.Z, a.Y, a.X, bz);
+    k_step_macro<<<g, bz, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_step_f64_exact(const StepArgs &a, const MrtMats *mm, int model, cudaStream_t st) {
     int bz = a.Z >= 128 ? 128 : ((a.Z + 31) / 32) * 32;
     int by = TPB / bz;
     if (by < 1) by = 1;
     dim3 blk(bz, by), grd((a.Z + bz - 1) / bz, (a.Y + by - 1) / by, a.X);
-    if (model == 3) k_step_exact<3><<<grd, blk, 0, st>>>(a, *mm);
-    else k_step_exact<1><<<grd, blk, 0, st>>>(a, MrtMats{});
+    switch (model) {
+    case CM_MRT: k_step_exact<CM_MRT><<<grd, blk, 0, st>>>(a, *mm); break;
+    case CM_TRT: k_step_exact<CM_TRT><<<grd, blk, 0, st>>>(a, MrtMats{}); break;
+    case CM_SMAG: k_step_exact<CM_SMAG><<<grd, blk, 0, st>>>(a, MrtMats{}); break;
+    case CM_WALE: k_step_exact<CM_WALE><<<grd, blk, 0, st>>>(a, MrtMats{}); break;
+    case CM_VREM: k_step_exact<CM_VREM><<<grd, blk, 0, st>>>(a, MrtMats{}); break;
+    default: k_step_exact<CM_SRT><<<grd, blk, 0, st>>>(a, MrtMats{}); break;
+    }
     return cudaGetLastError();
 }
 
@@ -778,14 +952,20 @@ cudaError_t launch_probes(const double *u, int X, int Y, int Z, double dh, doubl
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f, const PairGeom &p, int face,
-                                double *buf, double *buft, int *err, cudaStream_t st) {
+cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f,
+                                const PairGeom &p, int face, double *buf, double *buft, int *err, cudaStream_t st) {
     int ax = face >> 1, A, B;
     if (ax == 0) { A = p.zDimF; B = p.yDimF; }
     else if (ax == 1) { A = p.zDimF; B = p.xDimF; }
     else { A = p.yDimF; B = p.xDimF; }
-    k_pair_extract<<<dim3((A + 63) / 64, B), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, p, face, buf,
-                                                          buft, A, B, err);
+    k_pair_extract<<<dim3((A + 63) / 64, B), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, tauA_f, p, face,
+                                                          buf, buft, A, B, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_f64(double *p, long long n, double v, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_fill<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, n, v);
     return cudaGetLastError();
 }
 
@@ -794,7 +974,8 @@ cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaS
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const PairGeom &p, int face,
+cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const double *tauA_s, const PairGeom &p,
+                            int face,
                             const double *buf, const double *buft, int scheme, double *scratch_f, double *scratch_t,
                             long long scratch_cells, const double vf[3], double dh, int *err, cudaStream_t st) {
     int ax = face >> 1, AF, BF, AS, BS;
@@ -805,24 +986,25 @@ cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, co
     if ((long long)AS * BS > scratch_cells) return cudaErrorInvalidValue;
     k_pair_interp<<<1, 32, 0, st>>>(Q, AF, buf, Q * nF, AS, BS, scratch_f, Q * scratch_cells, scheme, err);
     k_pair_interp<<<1, 32, 0, st>>>(1, AF, buft, nF, AS, BS, scratch_t, scratch_cells, 1, err);
-    k_pair_f2s_apply<<<dim3((AS + 63) / 64, BS), 64, 0, st>>>(fs, SY, SZ, (long long)SX * SY * SZ, tau_s, p, face,
+    k_pair_f2s_apply<<<dim3((AS + 63) / 64, BS), 64, 0, st>>>(fs, SY, SZ, (long long)SX * SY * SZ, tau_s, tauA_s, p,
+                                                              face,
                                                               scratch_f, scratch_t, AS, BS, vf[0], vf[1], vf[2], dh,
                                                               err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *fs, int SX, int SY,
-                            int SZ, double tau_s, const PairGeom &p, int face, const double vf[3], double dh, int *err,
-                            cudaStream_t st) {
+cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f, const double *fs,
+                            int SX, int SY, int SZ, double tau_s, const double *tauA_s, const PairGeom &p, int face,
+                            const double vf[3], double dh, int *err, cudaStream_t st) {
     int ax = face >> 1;
     int o1 = (ax == 0) ? 1 : 0, o2 = (ax == 2) ? 1 : 2;
     // Fortran DO trip count of si(lo),si(hi),2: zero when hi < lo
     int n1 = (p.si[2 * o1 + 1] >= p.si[2 * o1]) ? (p.si[2 * o1 + 1] - p.si[2 * o1]) / 2 + 1 : 0;
     int n2 = (p.si[2 * o2 + 1] >= p.si[2 * o2]) ? (p.si[2 * o2 + 1] - p.si[2 * o2]) / 2 + 1 : 0;
     if (n1 <= 0 || n2 <= 0) return cudaSuccess;
-    k_pair_s2f<<<dim3((n2 + 63) / 64, n1), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, fs, SY, SZ,
-                                                         (long long)SX * SY * SZ, tau_s, p, face, n1, n2, vf[0], vf[1],
-                                                         vf[2], dh, err);
+    k_pair_s2f<<<dim3((n2 + 63) / 64, n1), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, tauA_f, fs, SY,
+                                                         SZ, (long long)SX * SY * SZ, tau_s, tauA_s, p, face, n1, n2,
+                                                         vf[0], vf[1], vf[2], dh, err);
     return cudaGetLastError();
 }
 

@@ -80,11 +80,6 @@ __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
 // +v, -v or the additive identity -0 for lattice component e
 template <typename C> __device__ __forceinline__ C sel(int e, C v) { return e > 0 ? v : (e < 0 ? -v : C(-0.0)); }
 
-// representatives of the nine opposite pairs (positivedirs, ConstParams.f90:19)
-__host__ __device__ constexpr int pr_(int k) {
-    return k == 0 ? 1 : k == 1 ? 3 : k == 2 ? 5 : k == 3 ? 7 : k == 4 ? 8 : k == 5 ? 11 : k == 6 ? 12 : k == 7 ? 15 : 16;
-}
-
 // offset equilibrium g_eq = w (rho - 1) + w rho (3 eu + 4.5 eu^2 - 1.5 u^2),
 // k15 = 1.5 u^2 (the face kernels and the fused z faces)
 __device__ __forceinline__ float geq_off(int q, float rho, float u0, float u1, float u2, float k15) {
@@ -246,7 +241,160 @@ __device__ __forceinline__ IT wrap_corr(int e, IT cp, IT cm) { return e > 0 ? cp
 // per-launch scalars in the arithmetic type, converted on the host: GB300
 // issues FP64 at a small fraction of the FP32 rate, so the FP32 kernels must
 // not convert double parameters per thread
-template <typename C> struct Scal { C om, dh, dh3, vf[3]; int forced; };
+template <typename C> struct Scal { C om, dh, dh3, vf[3]; int forced; C om2, tau, nu, cles; };
+
+// ---- TRT and the SRT collisions with a per-cell rate (LES) ----
+// The rates follow smag / WALE / vrem (FluidDomain.f90:1265-1506) in the
+// arithmetic type. WALE and Vreman scale their velocity-gradient tensors by
+// the largest entry g before the products (OP is homogeneous of degree 1 in
+// g), so that FP32 neither underflows nor overflows on quiet or violent
+// flow; the fractional powers are written with square roots.
+
+template <typename C>
+__device__ __forceinline__ void neq_stress_c(const C neq[Q], C q[6]) {
+    // fneq = -neq (FluidDomain.f90:1271-1276)
+    q[0] = -(neq[1] + neq[2] + neq[7] + neq[8] + neq[9] + neq[10] + neq[11] + neq[12] + neq[13] + neq[14]);
+    q[1] = -(neq[3] + neq[4] + neq[7] + neq[8] + neq[9] + neq[10] + neq[15] + neq[16] + neq[17] + neq[18]);
+    q[2] = -(neq[5] + neq[6] + neq[11] + neq[12] + neq[13] + neq[14] + neq[15] + neq[16] + neq[17] + neq[18]);
+    q[3] = -((neq[7] - neq[8]) - (neq[9] - neq[10]));
+    q[4] = -((neq[11] - neq[12]) - (neq[13] - neq[14]));
+    q[5] = -((neq[15] - neq[16]) - (neq[17] - neq[18]));
+}
+
+// center_diff / onesid_diff of velocity component k along axis d, times dh
+template <typename C>
+__device__ __forceinline__ C les_diff_c(const StepArgs &a, int k, int d, int z, int y, int x, long long c, C dh) {
+    const double *__restrict__ u = a.u + a.N * k;
+    const int i = d == 0 ? x : (d == 1 ? y : z);
+    const int D = d == 0 ? a.X : (d == 1 ? a.Y : a.Z);
+    const long long s = d == 0 ? (long long)a.Z * a.Y : (d == 1 ? (long long)a.Z : 1LL);
+    if (i > 0 && i < D - 1) return ((C)u[c + s] - (C)u[c - s]) * dh;
+    const long long s1 = i == 0 ? s : -s;
+    return ((C(4) * (C)u[c + s1] - C(3) * (C)u[c]) - (C)u[c + 2 * s1]) * dh;
+}
+
+template <typename C> __device__ __forceinline__ C pw15(C x) { return x * sqrt(x); }
+template <typename C> __device__ __forceinline__ C pw25(C x) { return (x * x) * sqrt(x); }
+template <typename C> __device__ __forceinline__ C pw125(C x) { return x * sqrt(sqrt(x)); }
+
+template <typename C, int MODEL>
+__device__ __forceinline__ C les_rate_c(const StepArgs &a, const Scal<C> &sc, const C neq[Q], C rho, int z, int y,
+                                        int x, long long c) {
+    C t;
+    if (MODEL == CM_SMAG) {
+        C q[6];
+        neq_stress_c(neq, q);
+        const C QQ = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + C(2) * (q[3] * q[3] + q[4] * q[4] + q[5] * q[5]);
+        const C tau_t = sqrt(sc.tau * sc.tau + sc.cles * sqrt(QQ) / rho);
+        a.tau_all[c] = (double)(C(0.5) * (sc.tau + tau_t));
+        return C(2) / (sc.tau + tau_t);
+    } else if (MODEL == CM_WALE) {
+        C q[6];
+        neq_stress_c(neq, q);
+        const C k = -(C(1.5) * sc.dh) / (rho * (C)a.tau_all[c]);
+        C S11 = k * q[0], S22 = k * q[1], S33 = k * q[2], S12 = k * q[3], S13 = k * q[4], S23 = k * q[5];
+        C ox = C(0.5) * (les_diff_c<C>(a, 2, 1, z, y, x, c, sc.dh) - les_diff_c<C>(a, 1, 2, z, y, x, c, sc.dh));
+        C oy = C(0.5) * (les_diff_c<C>(a, 0, 2, z, y, x, c, sc.dh) - les_diff_c<C>(a, 2, 0, z, y, x, c, sc.dh));
+        C oz = C(0.5) * (les_diff_c<C>(a, 1, 0, z, y, x, c, sc.dh) - les_diff_c<C>(a, 0, 1, z, y, x, c, sc.dh));
+        C O12 = C(-0.5) * oz, O13 = C(0.5) * oy, O23 = C(-0.5) * ox;
+        C g = fmax(fmax(fmax(fabs(S11), fabs(S22)), fmax(fabs(S33), fabs(S12))),
+                   fmax(fmax(fabs(S13), fabs(S23)), fmax(fmax(fabs(O12), fabs(O13)), fabs(O23))));
+        C OP = C(0);
+        if (g > C(0)) {
+            const C ig = C(1) / g;
+            S11 *= ig; S22 *= ig; S33 *= ig; S12 *= ig; S13 *= ig; S23 *= ig;
+            O12 *= ig; O13 *= ig; O23 *= ig;
+            const C S = S11 * S11 + S22 * S22 + S33 * S33 + C(2) * (S12 * S12 + S13 * S13 + S23 * S23);
+            const C O = C(2) * (O12 * O12 + O23 * O23 + O13 * O13);
+            const C a12 = O12 * O12, a13 = O13 * O13, a23 = O23 * O23;
+            const C SO11 = -((S11 * S11 + S12 * S12 + S13 * S13) * (a12 + a13));
+            const C SO22 = -((S12 * S12 + S22 * S22 + S23 * S23) * (a12 + a23));
+            const C SO33 = -((S13 * S13 + S23 * S23 + S33 * S33) * (a13 + a23));
+            const C SO12 = -((S11 * S12 + S12 * S22 + S13 * S23) * (O13 * O23));
+            const C SO13 = (S11 * S13 + S12 * S23 + S13 * S33) * (O12 * O23);
+            const C SO23 = -((S12 * S13 + S22 * S23 + S23 * S33) * (O12 * O13));
+            const C SO = SO11 + SO22 + SO33 + C(2) * (SO12 + SO13 + SO23);
+            const C SdSd = (S * S + O * O) * C(1.0 / 6.0) + C(2.0 / 3.0) * S * O + C(2) * SO;
+            OP = g * (pw15(SdSd) / (pw25(S) + pw125(SdSd)));
+            if (!(OP >= C(0)) || !isfinite(OP)) OP = C(0);
+        }
+        t = (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5);
+    } else {
+        C m[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) m[i][j] = C(0.5) * les_diff_c<C>(a, i, j, z, y, x, c, sc.dh);
+        C g = C(0);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) g = fmax(g, fabs(m[i][j]));
+        C OP = C(0);
+        if (g > C(0)) {
+            const C ig = C(1) / g;
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) m[i][j] *= ig;
+            const C r0 = m[0][0] * m[0][0] + m[0][1] * m[0][1] + m[0][2] * m[0][2];
+            const C r1 = m[1][0] * m[1][0] + m[1][1] * m[1][1] + m[1][2] * m[1][2];
+            const C r2 = m[2][0] * m[2][0] + m[2][1] * m[2][1] + m[2][2] * m[2][2];
+            const C d01 = m[0][0] * m[1][0] + m[0][1] * m[1][1] + m[0][2] * m[1][2];
+            const C d02 = m[0][0] * m[2][0] + m[0][1] * m[2][1] + m[0][2] * m[2][2];
+            const C d12 = m[1][0] * m[2][0] + m[1][1] * m[2][1] + m[1][2] * m[2][2];
+            const C bb = (r0 * r1 - d01 * d01) + (r0 * r2 - d02 * d02) + (r1 * r2 - d12 * d12);
+            OP = g * sqrt(bb / (r0 + r1 + r2));
+            if (!isfinite(OP)) OP = C(0);
+        }
+        t = (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5);
+    }
+    a.tau_all[c] = (double)t;
+    return C(1) / t;
+}
+
+// TRT (FluidDomain.f90:1228-1235) and the per-cell-rate SRT collisions
+// (:1239-1262) with Guo forcing on one cell
+template <int P, int MODEL>
+__device__ __forceinline__ void collide_rate(typename ST<P>::C g[Q], typename ST<P>::C rho, typename ST<P>::C drho,
+                                             typename ST<P>::C u0, typename ST<P>::C u1, typename ST<P>::C u2,
+                                             typename ST<P>::C F0, typename ST<P>::C F1, typename ST<P>::C F2,
+                                             const Scal<typename ST<P>::C> &sc, const StepArgs &a, int x, int y,
+                                             int z, long long c) {
+    using C = typename ST<P>::C;
+    constexpr bool OFF = ST<P>::OFF;
+    const C k15 = C(1.5) * (u0 * u0 + u1 * u1 + u2 * u2);
+    const C uF = u0 * F0 + u1 * F1 + u2 * F2;
+    C neq[Q], flb[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const C w = C(wt_(i));
+        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eq = OFF ? w * drho + (w * rho) * ((C(3) + C(4.5) * eu) * eu - k15)
+                         : (w * rho) * ((C(1) - k15) + (C(3) + C(4.5) * eu) * eu);
+        neq[i] = eq - g[i];
+        const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+        flb[i] = (sc.dh3 * w) * (eF - uF + C(3) * eu * eF);
+    }
+    if (MODEL == CM_TRT) {
+        const C om = sc.om, om2 = sc.om2;
+        const C hp = C(0.5) * om, hm = C(0.5) * om2, fp = C(0.5) - C(0.25) * om, fm = C(0.5) - C(0.25) * om2;
+        g[0] += om * neq[0] + (C(1) - C(0.5) * om) * flb[0];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int p = pr_(k), m = opp_(p);
+            const C sp = hp * (neq[p] + neq[m]) + fp * (flb[p] + flb[m]);
+            const C sm = hm * (neq[p] - neq[m]) + fm * (flb[p] - flb[m]);
+            g[p] += sp + sm;
+            g[m] += sp - sm;
+        }
+    } else {
+        const C om = les_rate_c<C, MODEL>(a, sc, neq, rho, z, y, x, c);
+        const C cf = C(1) - C(0.5) * om;
+#pragma unroll
+        for (int i = 0; i < Q; i++) g[i] += om * neq[i] + cf * flb[i];
+    }
+}
 
 template <int P, int MODEL, bool HOOKS, typename IT>
 __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST<P>::C> mm, Offs<IT> of,
@@ -283,17 +431,20 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
         F0 = sc.vf[0]; F1 = sc.vf[1]; F2 = sc.vf[2];
         forced = sc.forced != 0;
     }
-    if (HOOKS && ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
-                  (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2))) {
+    if (HOOKS && !grad_model(MODEL) &&
+        ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
+         (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2))) {
         a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
         a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
     }
     const C om = sc.om, dh3 = sc.dh3;
-    if (MODEL == 1) {
+    if (MODEL == CM_SRT) {
         if (forced) collide_srt<P, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, om, dh3);
         else collide_srt_free<P>(g, rho, drho, u0, u1, u2, om);
-    } else {
+    } else if (MODEL == CM_MRT) {
         collide_mrt<P>(g, rho, drho, u0, u1, u2, F0, F1, F2, forced, dh3, mm);
+    } else {
+        collide_rate<P, MODEL>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, a, x, y, z, (long long)c);
     }
 
     if (HOOKS) {
@@ -1209,6 +1360,38 @@ __global__ void k_macro_fast(const void *__restrict__ fs, double *den, double *u
     u[c] = u0; u[c + N] = u1; u[c + 2 * N] = u2;
 }
 
+// den/uuu of every cell as the collision sees them (IB window cells from the
+// IB stage), before the step of a model that reads neighbour velocities
+template <int P>
+__global__ void k_step_macro_fast(StepArgs a) {
+    using T = ST<P>;
+    using C = typename T::C;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
+    if (z >= a.Z) return;
+    const long long c = cidx(z, y, x, a.Z, a.Y), N = a.N;
+    const Win &w = a.win;
+    if (x >= w.x0 && x <= w.x1 && y >= w.y0 && y <= w.y1 && z >= w.z0 && z <= w.z1) {
+        long long wc = (long long)(z - w.z0) + (long long)w.WZ * ((long long)(y - w.y0) + (long long)w.WY * (x - w.x0));
+        const double d = w.den[wc];
+        // the values the step kernel converts them to
+        C rho, drho;
+        if (T::OFF) { drho = (C)(d - 1.0); rho = C(1) + drho; }
+        else { rho = (C)d; drho = rho - C(1); }
+        a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
+        a.u[c] = (C)w.u[wc]; a.u[c + N] = (C)w.u[wc + w.n]; a.u[c + 2 * N] = (C)w.u[wc + 2 * w.n];
+        return;
+    }
+    const typename T::S *src = (const typename T::S *)a.src;
+    C g[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) g[i] = T::dec(src[c + N * i]);
+    const C vf[3] = {(C)a.vf[0], (C)a.vf[1], (C)a.vf[2]};
+    C rho, drho, u0, u1, u2;
+    macro_fast<P>(g, vf, (C)a.dh, rho, drho, u0, u1, u2);
+    a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
+    a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
+}
+
 template <int P>
 __global__ void k_win_macro_fast(const void *__restrict__ fs, double *wden, double *wu, IbGeom g, long long N,
                                  long long Nw, double vf0, double vf1, double vf2) {
@@ -1547,6 +1730,10 @@ cudaError_t step_launch(const StepArgs &a, const MatsT<typename ST<P>::C> &m, cu
     sc.dh3 = (C)3 * (C)a.dh;
     for (int k = 0; k < 3; k++) sc.vf[k] = (C)a.vf[k];
     sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
+    sc.om2 = (C)a.omega2;
+    sc.tau = (C)a.tau;
+    sc.nu = (C)a.nu;
+    sc.cles = (C)a.cles;
     k_step_fast<P, MODEL, HOOKS, IT><<<grd, blk, 0, st>>>(a, m, of, sc);
     return cudaGetLastError();
 }
@@ -1822,12 +2009,25 @@ cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
 
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
-    return prec != FSI_PREC_F64_FAST && (model == 1 || mm->diag) && small && a.Z % 2 == 0 && a.Z <= 512;
+    return prec != FSI_PREC_F64_FAST && (model == CM_SRT || (model == CM_MRT && mm->diag)) && small &&
+           a.Z % 2 == 0 && a.Z <= 512;
 }
 
 cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st) {
-    if (model == 3) { FSI_DISPATCH(prec, return (step_inst<PP, 3>(a, mm, st))) }
-    FSI_DISPATCH(prec, return (step_inst<PP, 1>(a, mm, st)))
+    switch (model) {
+    case CM_MRT: { FSI_DISPATCH(prec, return (step_inst<PP, CM_MRT>(a, mm, st))) }
+    case CM_TRT: { FSI_DISPATCH(prec, return (step_inst<PP, CM_TRT>(a, mm, st))) }
+    case CM_SMAG: { FSI_DISPATCH(prec, return (step_inst<PP, CM_SMAG>(a, mm, st))) }
+    case CM_WALE: { FSI_DISPATCH(prec, return (step_inst<PP, CM_WALE>(a, mm, st))) }
+    case CM_VREM: { FSI_DISPATCH(prec, return (step_inst<PP, CM_VREM>(a, mm, st))) }
+    default: { FSI_DISPATCH(prec, return (step_inst<PP, CM_SRT>(a, mm, st))) }
+    }
+}
+
+cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st) {
+    int bz = a.Z >= 256 ? 256 : ((a.Z + 31) / 32) * 32;
+    dim3 g((a.Z + bz - 1) / bz, a.Y, a.X);
+    FSI_DISPATCH(prec, k_step_macro_fast<PP><<<g, bz, 0, st>>>(a); return cudaGetLastError())
 }
 
 cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {

@@ -62,7 +62,10 @@ typedef struct {
     int    xDim, yDim, zDim;
     double dh, xmin, ymin, zmin;
     int    bndConds[6];      /* x-, x+, y-, y+, z-, z+ codes (ConstParams.f90:31-34) */
-    int    iCollidModel;     /* 1 SRT/BGK, 3 MRT */
+    int    iCollidModel;     /* 1 SRT/BGK, 2 TRT, 3 MRT, 11 SRT + Smagorinsky,
+                                14 SRT + WALE, 15 SRT + Vreman (FluidDomain.f90:1225-1262);
+                                12 (RBGK) and 13 (ELBM) are refused: the reference
+                                reads an uninitialised rate / array there */
     double nu;               /* flow%nu; tau = nu/(dh/3) + 1/2 (FluidDomain.f90:452) */
     const double *m_collid;  /* optional 19x19 column-major M_COLLID (NULL: built here) */
     const double *m_force;   /* optional 19x19 column-major M_FORCE  (NULL: built here) */
@@ -71,6 +74,9 @@ typedef struct {
     double uvwIn[3];
     double shearRateIn[3];
     int    velocityKind;     /* 0 shear profile, 2 oscillatory (FluidDomain.f90:1791-1824) */
+    double params[10];       /* params(1:10) of the block line (FluidDomain.f90:84);
+                                params[0] = the TRT magic parameter Lambda of
+                                calculate_TRT_params (FluidDomain.f90:458-464) */
 } fsi_block_desc;
 
 /* message of the last error on this thread ("" if none); returns its length */
@@ -86,6 +92,14 @@ int fsi_block_destroy(fsi_block_t h);
 /* tau, Omega and the MRT matrices in use (FluidDomain.f90:450-522) */
 int fsi_block_get_params(fsi_block_t h, double *tau, double *omega,
                          double *m_collid, double *m_force);
+
+/* Omega2 of the TRT model (FluidDomain.f90:458-464; 0 for other models) */
+int fsi_block_get_omega2(fsi_block_t h, double *omega2);
+
+/* tau_all(z,y,x) (FluidDomain.f90:35): the per-cell relaxation time that the
+ * Smagorinsky, WALE and Vreman collisions write every step (and WALE reads);
+ * tau everywhere for the other models. N doubles in (z,y,x) order. */
+int fsi_block_get_tau_all(fsi_block_t h, double *tau_all);
 
 /* copy fIn(z,y,x,0:18) between host and device (write_continue_/read_continue_,
  * FluidDomain.f90:1770-1789, keep this exact layout) */

@@ -149,6 +149,13 @@ void or_block_setup(or_block *b, const or_flow *fl) {
         for (size_t i = 0; i < n; i++) b->tau_all[i] = b->tau;
     }
     if (b->model == 3) or_mrt_matrices(b->omega, b->mc, b->mf);
+    /* calculate_TRT_params, FluidDomain.f90:458-464 */
+    b->omega2 = 0.0;
+    if (b->model == 2) {
+        double tmp = (b->params[0] * 4.0 - 1.0) * b->omega + 2.0;
+        b->omega2 = (2.0 * (2.0 - b->omega)) / tmp;
+    }
+    b->nu = fl->nu;
     for (int k = 0; k < 6; k++) b->hw_ready[k] = 0;
 }
 
@@ -236,7 +243,123 @@ void or_add_force(or_block *b) {
     }
 }
 
-/* collision_ (SRT and MRT branches), FluidDomain.f90:1208-1238 */
+/* ConstParams.f90:19-20: the TRT population pairs */
+static const int POSD[9] = {1, 3, 5, 7, 8, 11, 12, 15, 16};
+static const int NEGD[9] = {2, 4, 6, 10, 9, 14, 13, 18, 17};
+
+/* ConstParams.f90:40-45, each product rounded in turn as the parameter
+ * expressions are evaluated */
+static double les_const(int model) {
+    const double Csmag = 0.17, CWALE = 0.50;
+    if (model == 11) return ((2.0 * Csmag) * Csmag) * sqrt(2.0) * 9.0;
+    if (model == 14) return CWALE * CWALE;
+    return (2.5 * Csmag) * Csmag;
+}
+
+/* the non-equilibrium stress sums of smag/WALE (FluidDomain.f90:1271-1276) */
+static void neq_stress(const double fn[Q], double q[6]) {
+    q[0] = fn[1] + fn[2] + fn[7] + fn[8] + fn[9] + fn[10] + fn[11] + fn[12] + fn[13] + fn[14];
+    q[1] = fn[3] + fn[4] + fn[7] + fn[8] + fn[9] + fn[10] + fn[15] + fn[16] + fn[17] + fn[18];
+    q[2] = fn[5] + fn[6] + fn[11] + fn[12] + fn[13] + fn[14] + fn[15] + fn[16] + fn[17] + fn[18];
+    q[3] = fn[7] - fn[8] - fn[9] + fn[10];
+    q[4] = fn[11] - fn[12] - fn[13] + fn[14];
+    q[5] = fn[15] - fn[16] - fn[17] + fn[18];
+}
+
+/* smag, FluidDomain.f90:1265-1281 */
+static double les_smag(const or_block *b, const double fEq[Q], double rho, size_t c) {
+    double fn[Q], q[6];
+    for (int i = 0; i < Q; i++) fn[i] = -fEq[i];
+    neq_stress(fn, q);
+    double QQ = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + 2.0 * (q[3] * q[3] + q[4] * q[4] + q[5] * q[5]);
+    double tau_t = sqrt(b->tau * b->tau + les_const(11) * sqrt(QQ) / rho);
+    b->tau_all[c] = 0.5 * (b->tau + tau_t);
+    return 2.0 / (b->tau + tau_t);
+}
+
+/* center_diff / onesid_diff and the interior / first / last branch of
+ * WALE and vrem (FluidDomain.f90:1343-1388, 1425-1471, 1482-1491):
+ * derivative of velocity component k along axis d at cell (z,y,x). The
+ * reference multiplies by its invdh = dh. */
+static double les_diff(const or_block *b, int k, int d, int z, int y, int x) {
+    size_t n = ncell(b);
+    const double *u = b->u + n * k;
+    int p[3] = {x, y, z}, D[3] = {b->X, b->Y, b->Z};
+    int i = p[d];
+    size_t s = (d == 0) ? (size_t)b->Z * b->Y : (d == 1 ? (size_t)b->Z : 1);
+    size_t c = cidx(b, z, y, x);
+    double inv = b->dh;
+    if (i > 0 && i < D[d] - 1) return (u[c + s] - u[c - s]) * inv;
+    if (i == 0) return ((-(3.0 * u[c]) + 4.0 * u[c + s]) - u[c + 2 * s]) * inv;
+    return ((-(3.0 * u[c]) + 4.0 * u[c - s]) - u[c - 2 * s]) * inv;
+}
+
+/* WALE, FluidDomain.f90:1304-1416 */
+static double les_wale(const or_block *b, const double fEq[Q], double rho, int z, int y, int x, size_t c) {
+    double fn[Q], q[6];
+    for (int i = 0; i < Q; i++) fn[i] = -fEq[i];
+    neq_stress(fn, q);
+    double invdh = b->dh, tau_ = b->tau_all[c];
+    double S11 = -(1.5 * invdh * q[0] / (rho * tau_));
+    double S22 = -(1.5 * invdh * q[1] / (rho * tau_));
+    double S33 = -(1.5 * invdh * q[2] / (rho * tau_));
+    double S12 = -(1.5 * invdh * q[3] / (rho * tau_));
+    double S13 = -(1.5 * invdh * q[4] / (rho * tau_));
+    double S23 = -(1.5 * invdh * q[5] / (rho * tau_));
+    double S = S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23);
+    double ox = les_diff(b, 2, 1, z, y, x);
+    ox = 0.5 * (ox - les_diff(b, 1, 2, z, y, x));
+    double oy = les_diff(b, 0, 2, z, y, x);
+    oy = 0.5 * (oy - les_diff(b, 2, 0, z, y, x));
+    double oz = les_diff(b, 1, 0, z, y, x);
+    oz = 0.5 * (oz - les_diff(b, 0, 1, z, y, x));
+    double O12 = -(0.5 * oz), O13 = 0.5 * oy, O23 = -(0.5 * ox);
+    double O = 2.0 * (O12 * O12 + O23 * O23 + O13 * O13);
+    /* the reference's 0.0d0 terms change nothing but the sign of a zero sum,
+     * which reaches no output (a zero SdSd gives OP = 0 either way) */
+    double SO11 = -(S11 * S11 * O12 * O12 + S11 * S11 * O13 * O13 + S12 * S12 * O12 * O12 +
+                    S12 * S12 * O13 * O13 + S13 * S13 * O12 * O12 + S13 * S13 * O13 * O13);
+    double SO22 = -(S12 * S12 * O12 * O12 + S12 * S12 * O23 * O23 + S22 * S22 * O12 * O12 +
+                    S22 * S22 * O23 * O23 + S23 * S23 * O12 * O12 + S23 * S23 * O23 * O23);
+    double SO33 = -(S13 * S13 * O13 * O13 + S13 * S13 * O23 * O23 + S23 * S23 * O13 * O13 +
+                    S23 * S23 * O23 * O23 + S33 * S33 * O13 * O13 + S33 * S33 * O23 * O23);
+    double SO12 = -(S11 * S12 * O13 * O23 + S12 * S22 * O13 * O23 + S13 * S23 * O13 * O23);
+    double SO13 = (S11 * S13 * O12 * O23 + S12 * S23 * O12 * O23 + S13 * S33 * O12 * O23);
+    double SO23 = -(S12 * S13 * O12 * O13 + S22 * S23 * O12 * O13 + S23 * S33 * O12 * O13);
+    double SO = SO11 + SO22 + SO33 + 2.0 * (SO12 + SO13 + SO23);
+    double SdSd = (S * S + O * O) / 6.0 + 2.0 * S * O / 3.0 + 2.0 * SO;
+    double OP = pow(SdSd, 1.5) / (pow(S, 2.5) + pow(SdSd, 1.25));
+    if (!isfinite(OP) || OP < 0.0) OP = 0.0;
+    double t = (b->nu + les_const(14) * OP * b->dh * b->dh) / (b->dh * CS2) + 0.5;
+    b->tau_all[c] = t;
+    return 1.0 / t;
+}
+
+/* vrem, FluidDomain.f90:1428-1506 */
+static double les_vrem(const or_block *b, int z, int y, int x, size_t c) {
+    double a[3][3];  /* a[i][j]: derivative of component i along axis j, halved */
+    for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) a[i][j] = 0.5 * les_diff(b, i, j, z, y, x);
+    double bq[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) bq[i][j] = a[i][j] * a[i][j];
+    double aa = bq[0][0] + bq[0][1] + bq[0][2] + bq[1][0] + bq[1][1] + bq[1][2] + bq[2][0] + bq[2][1] + bq[2][2];
+    double r0 = bq[0][0] + bq[0][1] + bq[0][2], r1 = bq[1][0] + bq[1][1] + bq[1][2], r2 = bq[2][0] + bq[2][1] + bq[2][2];
+    double d01 = a[0][0] * a[1][0] + a[0][1] * a[1][1] + a[0][2] * a[1][2];
+    double d02 = a[0][0] * a[2][0] + a[0][1] * a[2][1] + a[0][2] * a[2][2];
+    double d12 = a[1][0] * a[2][0] + a[1][1] * a[2][1] + a[1][2] * a[2][2];
+    double bb = r0 * r1 - d01 * d01 + r0 * r2 - d02 * d02 + r1 * r2 - d12 * d12;
+    double OP = sqrt(bb / aa);
+    if (!isfinite(OP)) OP = 0.0;
+    double t = (b->nu + les_const(15) * OP * b->dh * b->dh) / (b->dh * CS2) + 0.5;
+    b->tau_all[c] = t;
+    return 1.0 / t;
+}
+
+/* collision_, FluidDomain.f90:1208-1262: SRT (1), TRT (2), MRT (3) and the
+ * SRT collisions with a per-cell rate: Smagorinsky (11), WALE (14), Vreman
+ * (15). RBGK (12) reads an uninitialised rate and ELBM (13) an uninitialised
+ * array (x3), so neither has a defined result to restate. */
 void or_collide(or_block *b) {
     size_t n = ncell(b);
     double dt3 = 3.0 * b->dh;
@@ -268,6 +391,24 @@ void or_collide(or_block *b) {
                         for (int j = 0; j < Q; j++) bb += b->mf[i + Q * j] * Flb[j];
                         b->f[c + n * i] = (b->f[c + n * i] + a) + bb;
                     }
+                } else if (b->model == 2) {
+                    const double om = b->omega, om2 = b->omega2;
+                    double d[Q];
+                    d[0] = om * fEq[0] + (1.0 - 0.5 * om) * Flb[0];
+                    for (int k = 0; k < 9; k++) {
+                        int p = POSD[k], m = NEGD[k];
+                        double sp = 0.5 * om * (fEq[p] + fEq[m]) + (0.5 - 0.25 * om) * (Flb[p] + Flb[m]);
+                        double sm = 0.5 * om2 * (fEq[p] - fEq[m]) + (0.5 - 0.25 * om2) * (Flb[p] - Flb[m]);
+                        d[p] = sp + sm;
+                        d[m] = sp - sm;
+                    }
+                    for (int i = 0; i < Q; i++) b->f[c + n * i] = b->f[c + n * i] + d[i];
+                } else if (b->model == 11 || b->model == 14 || b->model == 15) {
+                    double om = (b->model == 11) ? les_smag(b, fEq, den, c)
+                              : (b->model == 14) ? les_wale(b, fEq, den, z, y, x, c)
+                              : les_vrem(b, z, y, x, c);
+                    for (int i = 0; i < Q; i++)
+                        b->f[c + n * i] = (b->f[c + n * i] + om * fEq[i]) + (1.0 - 0.5 * om) * Flb[i];
                 }
             }
 }

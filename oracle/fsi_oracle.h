@@ -46,7 +46,8 @@ typedef struct {
     double dh, xmin, ymin, zmin, xmax, ymax, zmax;
     int    bnd[6];
     int    periodic[3];
-    int    model;                 /* iCollidModel: 1 SRT, 3 MRT */
+    int    model;                 /* iCollidModel: 1 SRT, 2 TRT, 3 MRT, 11 SRT+Smagorinsky,
+                                     14 SRT+WALE, 15 SRT+Vreman (12, 13 not restated) */
     double tau, omega;
     double mc[361], mf[361];      /* M_COLLID, M_FORCE, column-major (i + 19*j) */
     double volumeForce[3];
@@ -55,9 +56,13 @@ typedef struct {
     double *u;                    /* 3*N   uuu(z,y,x,1:3) */
     double *den;                  /* N */
     double *force;                /* 3*N */
-    double *tau_all;              /* N   (may be NULL: constant tau) */
+    double *tau_all;              /* N   (may be NULL: constant tau; required by 11, 14, 15) */
     double *hw[6];                /* half-way face copies, 19*face each (may be NULL) */
     int    hw_ready[6];           /* 0 until the first set_boundary_conditions call */
+    double params[10];            /* params(1:10) of the block (FluidDomain.f90:84);
+                                     params[0] = TRT magic parameter Lambda */
+    double omega2;                /* TRT antisymmetric rate (FluidDomain.f90:458-464) */
+    double nu;                    /* flow%nu, read by the WALE and Vreman models */
 } or_block;
 
 /* One immersed body (Solidbody.f90:25-68), markers stored as (3,M). */

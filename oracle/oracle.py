@@ -49,6 +49,9 @@ class OrBlock(C.Structure):
         ("f", DP), ("u", DP), ("den", DP), ("force", DP), ("tau_all", DP),
         ("hw", DP * 6),
         ("hw_ready", C.c_int * 6),
+        ("params", C.c_double * 10),
+        ("omega2", C.c_double),
+        ("nu", C.c_double),
     ]
 
 
@@ -134,7 +137,7 @@ class Block:
     """One oracle block; numpy arrays in the reference's (z,y,x,q) order,
     exposed with shape (q, x, y, z) in C order (same memory)."""
 
-    def __init__(self, X, Y, Z, dh, origin, bnd, model, flow, with_tau=True):
+    def __init__(self, X, Y, Z, dh, origin, bnd, model, flow, with_tau=True, params=None):
         self.b = OrBlock()
         b = self.b
         b.X, b.Y, b.Z = X, Y, Z
@@ -142,6 +145,8 @@ class Block:
         b.xmin, b.ymin, b.zmin = origin
         b.bnd[:] = list(bnd)
         b.model = model
+        if params is not None:
+            b.params[:len(params)] = list(params)
         n = X * Y * Z
         self.n = n
         self.f = np.zeros(Q * n)
@@ -179,6 +184,10 @@ class Block:
 
     def macro(self):
         lib().or_macro(C.byref(self.b))
+
+    def collide(self):
+        """collision_ alone on the current f, den, u and force"""
+        lib().or_collide(C.byref(self.b))
 
     def step(self, bodies=(), Uref=1.0, ntol=0, dtol=0.0):
         arr = (OrBody * max(1, len(bodies)))()

@@ -4,7 +4,7 @@ Each case stores its inputs (initial distributions from a seeded uniform
 generator pushed through the equilibrium, marker arrays) and the oracle's
 outputs after every step. Inputs use no transcendental functions, so the
 vectors do not depend on the platform's libm. Regenerate with
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 and commit the .npz files together with any intended oracle change.
 """
 import os
@@ -30,7 +30,20 @@ CASES = {
                     uvw=(0.04, 0.01, 0.0), shear=(0.001, 0.0, 0.0)),
     "ib_plate": dict(dims=(18, 12, 10), bnd=(101, 104, 101, 101, 101, 101), model=1, nu=0.02,
                      uvw=(0.05, 0.0, 0.0), shear=(0, 0, 0), plate=True),
+    # TRT (params(1) = Lambda) and the SRT collisions with a per-cell rate
+    "trt_faces": dict(dims=(9, 8, 7), bnd=(101, 104, 201, 202, 302, 103), model=2, nu=0.01,
+                      uvw=(0.05, 0.0, 0.0), shear=(0.0, 0.002, 0.001), params=(3.0 / 16.0,)),
+    "les_smag": dict(dims=(10, 8, 6), bnd=(102, 103, 203, 204, 301, 301), model=11, nu=0.002,
+                     uvw=(0.04, 0.01, 0.0), shear=(0.001, 0.0, 0.0)),
+    "les_wale": dict(dims=(9, 8, 7), bnd=(101, 104, 201, 202, 302, 103), model=14, nu=0.002,
+                     uvw=(0.05, 0.0, 0.0), shear=(0.0, 0.002, 0.001)),
+    "les_vrem": dict(dims=(18, 12, 10), bnd=(101, 104, 101, 101, 101, 101), model=15, nu=0.002,
+                     uvw=(0.05, 0.0, 0.0), shear=(0, 0, 0), plate=True),
 }
+# WALE's fractional powers come from the platform's pow(): its vectors pin
+# the oracle on the machine that made them, and the GPU meets them to a
+# tolerance instead of bitwise
+POW_CASES = ("les_wale",)
 STEPS = 3
 
 
@@ -66,7 +79,8 @@ def digest(a):
 
 def run_case(name, spec):
     fl = O.make_flow(uvwIn=spec["uvw"], shearRateIn=spec["shear"], nu=spec["nu"])
-    b = O.Block(*spec["dims"], 1.0, (0.0, 0.0, 0.0), list(spec["bnd"]), spec["model"], fl)
+    b = O.Block(*spec["dims"], 1.0, (0.0, 0.0, 0.0), list(spec["bnd"]), spec["model"], fl,
+                params=spec.get("params"))
     f0 = initial_f(spec["dims"], seed=sum(map(ord, name)))
     b.fview()[...] = f0
     # main.f90:63: the initial boundary call (half-way faces only marked)
@@ -83,6 +97,8 @@ def run_case(name, spec):
         out["sha_%d" % (s + 1)] = np.array(digest(b.fview()))
         if s + 1 == STEPS:
             out["f_final"] = b.fview().copy()
+            if spec["model"] in (11, 14, 15):
+                out["tau_final"] = b.tau_all.reshape(spec["dims"]).copy()
         if bodies:
             out["eforce_%d" % (s + 1)] = bodies[0].eforce.reshape(-1, 3).copy()
             out["ei"] = bodies[0].ei.reshape(-1, 12).copy()
@@ -93,12 +109,14 @@ def run_case(name, spec):
     return out
 
 
-def main():
+def main(names=None):
     for name, spec in CASES.items():
+        if names and name not in names:
+            continue
         out = run_case(name, spec)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, sorted(out))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -11,19 +11,19 @@ class Case:
     def __init__(self, dims, bnd=(301,) * 6, model=1, nu=0.1 / 3.0, dh=1.0, origin=(0.0, 0.0, 0.0),
                  denIn=1.0, uvwIn=(0.0, 0.0, 0.0), shearRateIn=(0.0, 0.0, 0.0), velocityKind=0,
                  volumeForceIn=(0.0, 0.0, 0.0), volumeForceAmp=0.0, volumeForceFreq=0.0, volumeForcePhi=0.0,
-                 precision=F.PREC_F64, plates=(), ntol=3, dtol=1e-9, Uref=None):
+                 precision=F.PREC_F64, plates=(), ntol=3, dtol=1e-9, Uref=None, params=None):
         X, Y, Z = dims
         self.fl = O.make_flow(denIn=denIn, uvwIn=uvwIn, shearRateIn=shearRateIn, velocityKind=velocityKind,
                               volumeForceIn=volumeForceIn, volumeForceAmp=volumeForceAmp,
                               volumeForceFreq=volumeForceFreq, volumeForcePhi=volumeForcePhi, nu=nu)
-        self.ob = O.Block(X, Y, Z, dh, origin, bnd, model, self.fl)
+        self.ob = O.Block(X, Y, Z, dh, origin, bnd, model, self.fl, params=params)
         # the host builds M_COLLID/M_FORCE (FluidDomain.f90:466-522) and hands
         # them to the device, as the Fortran host does through the ABI
         mc = np.array(self.ob.b.mc[:]).reshape(19, 19, order="F") if model == 3 else None
         mf = np.array(self.ob.b.mf[:]).reshape(19, 19, order="F") if model == 3 else None
         self.gb = F.Block(X, Y, Z, dh=dh, origin=origin, bndConds=bnd, iCollidModel=model, nu=nu,
                           precision=precision, denIn=denIn, uvwIn=uvwIn, shearRateIn=shearRateIn,
-                          velocityKind=velocityKind, m_collid=mc, m_force=mf)
+                          velocityKind=velocityKind, m_collid=mc, m_force=mf, params=params)
         self.dh = dh
         self.denIn = denIn
         self.time = 0.0

@@ -41,3 +41,12 @@ def test_no_cpu_fallback_without_library(tmp_path, monkeypatch):
     monkeypatch.setattr(A, "library_path", lambda: str(tmp_path / "absent.so"))
     with pytest.raises(A.FsiError):
         A.load_library()
+
+
+def test_unsupported_collision_models_are_refused(gpu_lib):
+    # argument checks come before any device call, so this runs without a GPU
+    import fsilbm3d_gb300 as F
+    for m, what in ((12, "RBGK"), (13, "ELBM"), (4, "not supported"), (0, "not supported")):
+        with pytest.raises(F.FsiError) as e:
+            F.Block(8, 8, 8, iCollidModel=m)
+        assert e.value.code == F.FSI_E_ARG and what in str(e.value)

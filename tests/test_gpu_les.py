@@ -1,0 +1,129 @@
+"""TRT (iCollidModel 2) and the SRT collisions with a per-cell relaxation time
+(11 Smagorinsky, 14 WALE, 15 Vreman; FluidDomain.f90:1225-1506) against the
+oracle: bitwise on the exact FP64 form (WALE to rounding, its fractional
+powers come from pow()), to the storage form's rounding on the fast forms,
+through the captured step graph, and through the block-refinement exchange,
+which carries tau_all."""
+import numpy as np
+import pytest
+
+import fsilbm3d_gb300 as F
+from paired import Case, plate_in
+
+pytestmark = pytest.mark.gpu
+
+LAMBDA = 3.0 / 16.0
+MODELS = [2, 11, 14, 15]
+
+
+def _params(model):
+    return (LAMBDA,) if model == 2 else None
+
+
+def _same(a, b):
+    return a.shape == b.shape and np.ascontiguousarray(a).tobytes() == np.ascontiguousarray(b).tobytes()
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_exact_tgv_forced(gpu_lib, model):
+    c = Case((16, 12, 10), model=model, nu=0.004, params=_params(model), volumeForceIn=(2e-5, -1e-5, 0.0))
+    c.init_tgv(0.06)
+    for s in range(5):
+        c.step()
+        fo, fg = c.f_pair()
+        if model == 14:
+            assert _rel(fg, fo) < 1e-13, s
+        else:
+            assert _same(fo, fg), ("step", s)
+    if model in (11, 14, 15):
+        to = c.ob.tau_all.reshape(c.gb.dims)
+        tg = c.gb.tau_all()
+        if model == 14:
+            assert np.max(np.abs(tg - to)) < 1e-13
+        else:
+            assert _same(to, tg)
+    if model == 2:
+        assert c.gb.omega2() == c.ob.b.omega2
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_exact_walls_and_plate(gpu_lib, model):
+    # one-sided velocity differences at every face, IB window values in the
+    # gradients
+    dims = (20, 14, 12)
+    c = Case(dims, model=model, nu=0.003, params=_params(model), bnd=(101, 104, 201, 202, 203, 204),
+             uvwIn=(0.05, 0.0, 0.0), shearRateIn=(0.0, 0.001, 0.0), plates=[plate_in(dims, n=5, heave=1.0, freq=0.02)],
+             ntol=3, dtol=1e-12, Uref=0.05)
+    c.init_equilibrium()
+    for s in range(4):
+        r = c.step()
+        fo, fg = c.f_pair()
+        if model == 14:
+            assert _rel(fg, fo) < 1e-12, s
+        else:
+            assert _same(fo, fg), ("step", s)
+            assert r["ef_g"].tobytes() == r["ef_o"].tobytes()
+
+
+@pytest.mark.parametrize("model", [11, 15])
+def test_graph_run_matches_steps(gpu_lib, model):
+    kw = dict(bndConds=(101, 104, 201, 202, 302, 302), nu=0.003, uvwIn=(0.05, 0, 0), iCollidModel=model)
+    a, b = F.Block(16, 12, 10, **kw), F.Block(16, 12, 10, **kw)
+    for blk in (a, b):
+        blk.initialise(0.0)
+        blk.set_boundary_conditions(0.0)
+    for s in range(6):
+        a.step(blktime=(s + 1) * 1.0)
+    b.run(6, blktime0=1.0)
+    assert _same(a.download_f(), b.download_f())
+    assert _same(a.tau_all(), b.tau_all())
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("prec,tol", [(F.PREC_F64_FAST, 1e-11), (F.PREC_F32, 5e-5), (F.PREC_F16, 5e-3),
+                                      (F.PREC_BF16, 5e-2)])
+def test_fast_forms(gpu_lib, model, prec, tol):
+    dims = (18, 14, 12)
+    c = Case(dims, model=model, nu=0.003, params=_params(model), precision=prec, bnd=(101, 104, 201, 202, 302, 302),
+             uvwIn=(0.05, 0.0, 0.0), volumeForceIn=(1e-5, 0.0, 0.0))
+    c.init_tgv(0.05)
+    for s in range(8):
+        c.step()
+    c.ob.b.volumeForce[:] = list(c.vf(c.time))
+    c.ob.macro()
+    den, uuu = c.gb.calculate_macro_quantities(c.vf(c.time))
+    assert _rel(uuu, c.ob.u.reshape(uuu.shape)) < tol
+    if model in (11, 14, 15):
+        to = c.ob.tau_all.reshape(dims)
+        tg = c.gb.tau_all()
+        # the eddy part tau_all - tau, relative to its peak
+        ed = to - c.ob.b.tau
+        assert np.max(np.abs(tg - to)) < 10 * tol * max(np.max(np.abs(ed)), 1e-6)
+
+
+@pytest.mark.parametrize("model", [11, 15])
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F16])
+def test_fast_ib_step(gpu_lib, model, prec):
+    # fsi_block_ib_step: the IB stage, then the step that reads its window
+    dims = (24, 16, 14)
+    c = Case(dims, model=model, nu=0.003, precision=prec, bnd=(101, 104, 101, 101, 101, 101),
+             uvwIn=(0.05, 0.0, 0.0), plates=[plate_in(dims, n=5, heave=1.0, freq=0.02)], ntol=4, dtol=1e-12,
+             Uref=0.05)
+    c.init_equilibrium()
+    other = F.Block(*dims, bndConds=(101, 104, 101, 101, 101, 101), iCollidModel=model, nu=0.003, precision=prec,
+                    uvwIn=(0.05, 0.0, 0.0))
+    other.initialise(0.0)
+    other.set_boundary_conditions(0.0)
+    other.ib_set_bodies([c.plates[0].M], bc=[101, 104, 101, 101, 101, 101])
+    for s in range(3):
+        t = c.time
+        xyz, vel, area = c.plates[0].markers(t)
+        ef1, it1, _ = other.ib_step(xyz, vel, area, Uref=0.05, ntol=4, dtol=1e-12, blktime=t + 1.0)
+        c.step()
+        assert np.max(np.abs(ef1 - c.last["ef_g"])) <= 1e-6 * np.max(np.abs(c.last["ef_g"]))
+    assert np.array_equal(other.download_f().view(np.uint64), c.gb.download_f().view(np.uint64))
+

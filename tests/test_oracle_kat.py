@@ -194,3 +194,77 @@ def test_refined_uniform_flow_stays_uniform(scheme):
         tl.step()
     assert np.max(np.abs(tl.ofa.fview() - f0)) < 1e-15
     assert np.max(np.abs(tl.oso.fview() - s0)) < 1e-15
+
+
+def test_trt_with_equal_rates_is_srt():
+    # Lambda = (1/omega - 1/2)^2 gives Omega2 = Omega: TRT is then SRT up to
+    # the order of the sums
+    fl = O.make_flow(nu=0.02, volumeForceIn=(1e-5, -2e-5, 0.0))
+    a = O.Block(8, 7, 6, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    lam = (1.0 / a.b.omega - 0.5) ** 2
+    b = O.Block(8, 7, 6, 1.0, (0, 0, 0), [301] * 6, 2, fl, params=[lam])
+    assert abs(b.b.omega2 - b.b.omega) < 1e-14
+    a.init_tgv(0.05)
+    b.init_tgv(0.05)
+    for _ in range(5):
+        a.step()
+        b.step()
+    assert np.max(np.abs(a.f - b.f)) < 1e-14
+
+
+def test_trt_conserves_mass_and_momentum():
+    fl = O.make_flow(nu=0.02)
+    b = O.Block(12, 10, 8, 1.0, (0, 0, 0), [301] * 6, 2, fl, params=[3.0 / 16.0])
+    b.init_tgv(0.05)
+    m0, p0 = b.f.sum(), total_momentum(b)
+    for _ in range(10):
+        b.step()
+    assert abs(b.f.sum() - m0) / m0 < 1e-13
+    assert np.max(np.abs(total_momentum(b) - p0)) < 1e-13
+
+
+def test_smagorinsky_at_rest_is_srt():
+    # no non-equilibrium stress: tau_t = tau, omega = 1/tau bitwise
+    fl = O.make_flow(nu=0.02)
+    a = O.Block(8, 6, 5, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    b = O.Block(8, 6, 5, 1.0, (0, 0, 0), [301] * 6, 11, fl)
+    for blk in (a, b):
+        blk.initialise(0.0)
+        for _ in range(3):
+            blk.step()
+    assert np.array_equal(a.f, b.f)
+    assert np.all(b.tau_all == b.b.tau)
+
+
+@pytest.mark.parametrize("model", [11, 14, 15])
+def test_les_raises_relaxation_time_in_shear(model):
+    # the eddy viscosity is non-negative: tau_all >= tau, above it somewhere
+    fl = O.make_flow(nu=0.005)
+    b = O.Block(16, 16, 16, 1.0, (0, 0, 0), [301] * 6, model, fl)
+    b.init_tgv(0.08)
+    for _ in range(4):
+        b.step()
+    assert b.tau_all.min() >= b.b.tau - 1e-15
+    assert b.tau_all.max() > b.b.tau * (1.0 + 1e-4)
+
+
+def test_vreman_vanishes_in_plane_shear():
+    # u = (g y, 0, 0): Vreman's B_beta is zero, so tau_all = tau exactly
+    fl = O.make_flow(nu=0.01)
+    X, Y, Z = 6, 9, 5
+    b = O.Block(X, Y, Z, 1.0, (0, 0, 0), [301] * 6, 15, fl)
+    n = X * Y * Z
+    u = b.u.reshape(3, X, Y, Z)
+    u[...] = 0.0
+    u[0] = (0.002 * np.arange(Y))[None, :, None]
+    b.den[:] = 1.0
+    f = b.fview()
+    for x in range(X):
+        for y in range(Y):
+            for z in range(Z):
+                f[:, x, y, z] = O.feq(1.0, u[:, x, y, z])
+    b.force[:] = 0.0
+    b.tau_all[:] = 0.0
+    b.collide()
+    assert np.all(b.tau_all == b.b.tau)
+    assert n == b.tau_all.size
