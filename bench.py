@@ -66,12 +66,14 @@ def parse():
     p.add_argument("--no-extra", action="store_true", help="skip the TGV forms and the 160x96x96 case")
     p.add_argument("--f64-steps", type=int, default=24, help="steps of the FP64 plain comparison")
     p.add_argument("--grid", default="384x256x256", help="headline grid (profiling runs use a smaller one)")
-    p.add_argument("--only", default="all", choices=["all", "tgv256", "ib160", "batched_sweep", "warm_start"],
+    p.add_argument("--only", default="all", choices=["all", "tgv256", "models", "ib160", "batched_sweep",
+                                                     "warm_start"],
                    help="run one side section alone and print its result (profiling runs)")
     p.add_argument("--tgv-grid", type=int, default=256, help="edge of the periodic TGV cube")
     p.add_argument("--ib160-steps", type=int, default=2000, help="steps of the 160x96x96 plate case")
     p.add_argument("--tgv-forms", default="f64,f64_fast,f32,f16,bf16", help="TGV storage forms")
     p.add_argument("--tgv-models", default="1,3", help="TGV collision models (1 SRT, 3 MRT)")
+    p.add_argument("--les-models", default="2,11,14,15", help="TRT and LES models of the models section")
     a = p.parse_args()
     global FSI_GRID, TGV_GRID
     FSI_GRID = tuple(int(v) for v in a.grid.split("x"))
@@ -281,27 +283,45 @@ def tgv_f64(grid):
     return f
 
 
+MODEL_NAMES = {1: "srt", 2: "trt", 3: "mrt", 11: "smag", 14: "wale", 15: "vrem"}
+TRT_LAMBDA = 3.0 / 16.0
+
+
+def model_bytes(model, s):
+    """algorithmic HBM bytes per cell update: the populations read and
+    written once, plus tau_all (Smagorinsky writes it, WALE reads and writes
+    it) and, for WALE and Vreman, the macro pass (populations read, den and u
+    written) and the step's read of the velocity field"""
+    B = 2 * 19 * s
+    if model == 11:
+        B += 8
+    elif model in (14, 15):
+        B += 19 * s + 32 + 24 + (16 if model == 14 else 8)
+    return B
+
+
 def tgv_forms(F, steps, pk, forms=("f64", "f64_fast", "f32", "f16", "bf16"), models=(1, 3)):
     X, Y, Z = TGV_GRID
     N = X * Y * Z
     nu = (TAU - 0.5) / 3.0
     f0 = tgv_f64(TGV_GRID)
     out = {}
-    for model, mname in ((1, "srt"), (3, "mrt")):
+    for model, mname in sorted(MODEL_NAMES.items()):
         if model not in models:
             continue
         ref_u, ref_n = None, None
+        prm = (TRT_LAMBDA,) if model == 2 else None
         for name in forms:
-            b = F.Block(X, Y, Z, nu=nu, precision=F.PRECISIONS[name], iCollidModel=model)
+            b = F.Block(X, Y, Z, nu=nu, precision=F.PRECISIONS[name], iCollidModel=model, params=prm)
             b.upload_f(f0)
             b.run(3)
             b.upload_f(f0)
             n = steps if name != "f64" else max(4, steps // 4)
             ms = b.run(n)
             den, uuu = b.calculate_macro_quantities()
-            B = 2 * 19 * b.store_bytes
+            B = model_bytes(model, b.store_bytes)
             mlups = N * n / (ms * 1e-3) / 1e6
-            r = {"mlups": round(mlups, 1), "ms_per_step": ms / n, "steps": n,
+            r = {"mlups": round(mlups, 1), "ms_per_step": ms / n, "steps": n, "bytes_per_cell": B,
                  "algorithmic_gbs": round(mlups * B / 1e3, 1), "hbm_frac": round(mlups * B / 1e3 / pk, 4)}
             if name == "f64":
                 ref_u, ref_n = uuu, n
@@ -316,7 +336,7 @@ def tgv_forms(F, steps, pk, forms=("f64", "f64_fast", "f32", "f16", "bf16"), mod
             key = "%s_%s" % (name, mname)
             if "u_max_rel_err_vs_f64" in out[key]:
                 continue
-            b = F.Block(X, Y, Z, nu=nu, precision=F.PRECISIONS[name], iCollidModel=model)
+            b = F.Block(X, Y, Z, nu=nu, precision=F.PRECISIONS[name], iCollidModel=model, params=prm)
             b.upload_f(f0)
             b.run(ref_n)
             den, uuu = b.calculate_macro_quantities()
@@ -324,6 +344,8 @@ def tgv_forms(F, steps, pk, forms=("f64", "f64_fast", "f32", "f16", "bf16"), mod
             out[key]["err_after_steps"] = ref_n
             b.close()
     out["workload"] = "taylor-green vortex %d^3 periodic, tau=0.6, u0=0.05, inputs larger than L2" % X
+    if 2 in models:
+        out["trt_lambda"] = TRT_LAMBDA
     return out
 
 
@@ -576,6 +598,8 @@ def main():
         steps = max(10, min(a.steps, 100))
         if a.only == "tgv256":
             r = tgv_forms(F, steps, pk, forms=a.tgv_forms.split(","), models=[int(m) for m in a.tgv_models.split(",")])
+        elif a.only == "models":
+            r = tgv_forms(F, steps, pk, forms=a.tgv_forms.split(","), models=[int(m) for m in a.les_models.split(",")])
         elif a.only == "ib160":
             r = ib160_case(F, a.ib160_steps)
         elif a.only == "batched_sweep":
@@ -669,6 +693,8 @@ def main():
     extra = {}
     if not a.no_extra and rank == 0:
         extra["tgv256"] = tgv_forms(F, max(20, min(a.steps, 100)), pk)
+        extra["tgv256_models"] = tgv_forms(F, max(20, min(a.steps, 100)), pk, forms=("f64", "f32", "f16"),
+                                           models=tuple(int(m) for m in a.les_models.split(",")))
         extra["ib160"] = ib160_case(F, a.ib160_steps)
         extra["batched_sweep"] = batched_sweep(F, max(10, min(a.steps, 50)))
         extra["warm_start"] = warm_start_case(F)

@@ -60,7 +60,7 @@ SYMBOLS = [
     "fsi_block_set_kernel", "fsi_block_ib_step",
     "fsi_batch_create", "fsi_batch_destroy", "fsi_batch_ib_step", "fsi_batch_tune", "fsi_batch_set_threads",
     "fsi_block_set_ib_mode", "fsi_block_pack_flow", "fsi_block_flux", "fsi_block_probes",
-    "fsi_block_get_omega2", "fsi_block_get_tau_all",
+    "fsi_block_get_omega2", "fsi_block_get_tau_all", "fsi_continue_write", "fsi_continue_read",
 ]
 IB_AUTO, IB_GRID, IB_CLUSTER = 0, 1, 2
 KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
@@ -92,6 +92,8 @@ def load_library():
     L.fsi_block_destroy.argtypes = [VP]
     L.fsi_block_get_params.argtypes = [VP, DP, DP, DP, DP]
     L.fsi_block_get_omega2.argtypes = [VP, DP]
+    L.fsi_continue_write.argtypes = [C.c_char_p, C.POINTER(VP), C.c_int, C.c_int, C.c_double]
+    L.fsi_continue_read.argtypes = [C.c_char_p, C.POINTER(VP), C.c_int, C.POINTER(C.c_int), DP]
     L.fsi_block_get_tau_all.argtypes = [VP, DP]
     L.fsi_block_upload_f.argtypes = [VP, DP]
     L.fsi_block_download_f.argtypes = [VP, DP]
@@ -622,3 +624,20 @@ class Batch:
 
     def set_threads(self, threads):
         _check(load_library().fsi_batch_set_threads(self.h, int(threads)))
+
+
+def continue_write(path, blocks, step, time):
+    """write_continue_blocks (FluidDomain.f90:266-281): the continue file of
+    the blocks' current fIn"""
+    arr = (C.c_void_p * len(blocks))(*[b.h.value for b in blocks])
+    _check(load_library().fsi_continue_write(os.fsencode(path), arr, len(blocks), int(step), float(time)))
+
+
+def continue_read(path, blocks):
+    """check_is_continue (FluidDomain.f90:127-236): re-grid the blocks' fIn
+    from a continue file on the GPU; returns the file's (step, time)"""
+    arr = (C.c_void_p * len(blocks))(*[b.h.value for b in blocks])
+    step = C.c_int(0)
+    t = C.c_double(0.0)
+    _check(load_library().fsi_continue_read(os.fsencode(path), arr, len(blocks), C.byref(step), C.byref(t)))
+    return step.value, t.value

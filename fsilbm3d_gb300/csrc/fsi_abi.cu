@@ -600,6 +600,143 @@ int fsi_block_download_f(fsi_block_t h, double *fIn) {
     return check_kerr(h);
 }
 
+// ---------------------------------------------------------------- restart
+
+int fsi_continue_write(const char *path, const fsi_block_t *blocks, int n, int step, double time) {
+    if (!path || !blocks || n <= 0) return fail(FSI_E_ARG, "invalid argument");
+    for (int i = 0; i < n; i++)
+        if (!blocks[i]) return fail(FSI_E_ARG, "null block %d", i);
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return fail(FSI_E_ARG, "cannot open %s for writing", path);
+    bool ok = true;
+    const int32_t head[2] = {(int32_t)n, (int32_t)step};
+    ok = ok && fwrite(head, sizeof(int32_t), 2, fp) == 2;
+    ok = ok && fwrite(&time, sizeof(double), 1, fp) == 1;
+    std::vector<double> f;
+    int rc = FSI_OK;
+    for (int i = 0; i < n && ok && rc == FSI_OK; i++) {
+        fsi_block *h = blocks[i];
+        const double g[4] = {h->d.xmin, h->d.ymin, h->d.zmin, h->d.dh};
+        const int32_t dims[3] = {(int32_t)h->X, (int32_t)h->Y, (int32_t)h->Z};
+        f.resize(19 * (size_t)h->N);
+        rc = fsi_block_download_f(h, f.data());
+        if (rc) break;
+        ok = ok && fwrite(g, sizeof(double), 4, fp) == 4;
+        ok = ok && fwrite(dims, sizeof(int32_t), 3, fp) == 3;
+        ok = ok && fwrite(f.data(), sizeof(double), f.size(), fp) == f.size();
+    }
+    if (fclose(fp) != 0) ok = false;
+    if (rc) return rc;
+    if (!ok) return fail(FSI_E_ARG, "short write to %s", path);
+    return FSI_OK;
+}
+
+int fsi_continue_read(const char *path, const fsi_block_t *blocks, int n, int *step, double *time) {
+    if (!path || !blocks || n <= 0) return fail(FSI_E_ARG, "invalid argument");
+    for (int i = 0; i < n; i++)
+        if (!blocks[i]) return fail(FSI_E_ARG, "null block %d", i);
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(FSI_E_ARG, "cannot open %s", path);
+    fseek(fp, 0, SEEK_END);
+    const long long fsize = ftell(fp);
+    fseek(fp, 0, SEEK_SET);
+    int32_t head[2];
+    double t0 = 0.0;
+    if (fread(head, sizeof(int32_t), 2, fp) != 2 || fread(&t0, sizeof(double), 1, fp) != 1 || head[0] <= 0) {
+        fclose(fp);
+        return fail(FSI_E_ARG, "%s: not a continue file", path);
+    }
+    const int nold = head[0];
+    long long pos = 16;
+    std::vector<RegridSrc> src(nold);
+    std::vector<double *> dev(nold, nullptr);
+    std::vector<double> host;
+    auto cleanup = [&]() {
+        for (double *p : dev)
+            if (p) cudaFree(p);
+    };
+    cudaStream_t st = blocks[0]->st;
+    for (int k = 0; k < nold; k++) {
+        double g[4];
+        int32_t dims[3];
+        if (fread(g, sizeof(double), 4, fp) != 4 || fread(dims, sizeof(int32_t), 3, fp) != 3 || dims[0] < 2 ||
+            dims[1] < 2 || dims[2] < 2 || !(g[3] > 0.0)) {
+            fclose(fp);
+            cleanup();
+            return fail(FSI_E_ARG, "%s: bad header of block %d", path, k);
+        }
+        pos += 44;
+        const long long cells = (long long)dims[0] * dims[1] * dims[2];
+        if (pos + 19 * 8 * cells > fsize) {
+            fclose(fp);
+            cleanup();
+            return fail(FSI_E_ARG, "%s: block %d is truncated", path, k);
+        }
+        host.resize(19 * (size_t)cells);
+        if (fread(host.data(), sizeof(double), host.size(), fp) != host.size()) {
+            fclose(fp);
+            cleanup();
+            return fail(FSI_E_ARG, "%s: short read in block %d", path, k);
+        }
+        pos += 19 * 8 * cells;
+        RegridSrc &r = src[k];
+        r.xmin = g[0]; r.ymin = g[1]; r.zmin = g[2]; r.dh = g[3];
+        r.X = dims[0]; r.Y = dims[1]; r.Z = dims[2];
+        // coor_max, FluidDomain.f90:165-169
+        r.xmx = r.xmin + (double)(r.X - 1) * r.dh;
+        r.ymx = r.ymin + (double)(r.Y - 1) * r.dh;
+        r.zmx = r.zmin + (double)(r.Z - 1) * r.dh;
+        cudaError_t e = cudaMalloc((void **)&dev[k], sizeof(double) * host.size());
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dev[k], host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            fclose(fp);
+            cleanup();
+            return fail(FSI_E_CUDA, "continue upload: %s", cudaGetErrorString(e));
+        }
+        r.f = dev[k];
+    }
+    fclose(fp);
+    // the search order: the exchange sort of FluidDomain.f90:151-163, which
+    // compares dh at the original positions while it permutes the indices
+    std::vector<int> order(nold);
+    for (int i = 0; i < nold; i++) order[i] = i;
+    for (int i = 0; i < nold - 1; i++)
+        for (int j = i + 1; j < nold; j++)
+            if (src[i].dh > src[j].dh) std::swap(order[i], order[j]);
+    std::vector<RegridSrc> sorted(nold);
+    for (int i = 0; i < nold; i++) sorted[i] = src[order[i]];
+    RegridSrc *d_src = nullptr;
+    int *d_err = nullptr;
+    cudaError_t e = cudaMalloc((void **)&d_src, sizeof(RegridSrc) * nold);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_err, sizeof(int) * 4);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_src, sorted.data(), sizeof(RegridSrc) * nold, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_err, 0, sizeof(int) * 4, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    int herr[3] = {0, 0, 0};
+    for (int i = 0; i < n && e == cudaSuccess; i++) {
+        fsi_block *h = blocks[i];
+        double *dst = (h->esz == 8) ? (double *)h->fa : h->stage;
+        if (h->esz != 8) e = launch_convert_from_store(h->fa, h->stage, h->N, h->prec, h->st);
+        if (e == cudaSuccess)
+            e = launch_regrid_f64(dst, h->X, h->Y, h->Z, h->d.dh, h->d.xmin, h->d.ymin, h->d.zmin, d_src, nold, d_err,
+                                  h->st);
+        if (e == cudaSuccess && h->esz != 8) e = launch_convert_to_store(h->stage, h->fa, h->N, h->prec, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(herr, d_err, sizeof(int) * 3, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (d_src) cudaFree(d_src);
+    if (d_err) cudaFree(d_err);
+    cleanup();
+    if (e != cudaSuccess) return fail(FSI_E_CUDA, "continue re-grid: %s", cudaGetErrorString(e));
+    if (herr[0]) return fail(FSI_E_RANGE, "continue re-grid: stencil outside a file block at cell %lld",
+                             (long long)(unsigned)herr[1] | ((long long)herr[2] << 32));
+    if (step) *step = head[1];
+    if (time) *time = t0;
+    return FSI_OK;
+}
+
 // ---------------------------------------------------------------- outputs
 
 namespace {

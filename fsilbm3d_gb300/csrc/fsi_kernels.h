@@ -86,6 +86,18 @@ cudaError_t launch_flux(const double *den, const double *u, int X, int Y, int Z,
 cudaError_t launch_probes(const double *u, int X, int Y, int Z, double dh, double xmin, double ymin, double zmin, int n,
                           const double *xyz, double Uref, double *out, cudaStream_t st);
 
+// ---- continue-file re-grid (k_f64_exact.cu, check_is_continue,
+// FluidDomain.f90:170-226): one file block, its upper corner precomputed ----
+struct RegridSrc {
+    double xmin, ymin, zmin, dh, xmx, ymx, zmx;
+    int X, Y, Z;
+    const double *f;  // fIn(z,y,x,0:18) on the device
+};
+// fIn (FP64, N = X*Y*Z cells) of a block at (xmin, ymin, zmin) with spacing dh
+// from the file blocks src[0..nsrc) in search order; err: first bad index
+cudaError_t launch_regrid_f64(double *f, int X, int Y, int Z, double dh, double xmin, double ymin, double zmin,
+                              const RegridSrc *src, int nsrc, int *err, cudaStream_t st);
+
 // ---- block refinement (k_f64_exact.cu) ----
 struct PairGeom {
     int sds[6], s[6], f[6], si[6], fi[6];

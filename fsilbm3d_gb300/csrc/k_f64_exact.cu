@@ -797,6 +797,47 @@ __global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_
     for (int e = 0; e < Q; e++) ff[cf + NF * e] = t[e];
 }
 
+// check_is_continue's trilinear re-grid (FluidDomain.f90:170-226): each
+// cell takes the first file block (in search order) that contains it and
+// blends its 8 surrounding nodes in the reference's order; cells outside
+// every file block keep their values
+__global__ void k_regrid(double *__restrict__ f, int X, int Y, int Z, double dh, double xmin, double ymin,
+                         double zmin, const RegridSrc *__restrict__ src, int nsrc, int *err) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
+    if (z >= Z) return;
+    const double xc = xmin + (double)x * dh, yc = ymin + (double)y * dh, zc = zmin + (double)z * dh;
+    const long long N = (long long)X * Y * Z, c = cidx(z, y, x, Z, Y);
+    for (int j = 0; j < nsrc; j++) {
+        const RegridSrc o = src[j];
+        if (!(zc >= o.zmin && zc <= o.zmx && yc >= o.ymin && yc <= o.ymx && xc >= o.xmin && xc <= o.xmx)) continue;
+        double c1 = (xc - o.xmin) / o.dh, c2 = (yc - o.ymin) / o.dh, c3 = (zc - o.zmin) / o.dh;
+        int i1 = (int)floor(c1), i3 = (int)floor(c2), i5 = (int)floor(c3);
+        if (i1 == o.X - 1) i1 = i1 - 1;
+        if (i3 == o.Y - 1) i3 = i3 - 1;
+        if (i5 == o.Z - 1) i5 = i5 - 1;
+        if (i1 < 0 || i1 + 1 >= o.X || i3 < 0 || i3 + 1 >= o.Y || i5 < 0 || i5 + 1 >= o.Z) {
+            rec_err(err, 7, c);
+            return;
+        }
+        c1 = c1 - (double)i1;
+        c2 = c2 - (double)i3;
+        c3 = c3 - (double)i5;
+        const long long no = (long long)o.X * o.Y * o.Z;
+        const long long a000 = cidx(i5, i3, i1, o.Z, o.Y), a001 = cidx(i5, i3, i1 + 1, o.Z, o.Y);
+        const long long a010 = cidx(i5, i3 + 1, i1, o.Z, o.Y), a011 = cidx(i5, i3 + 1, i1 + 1, o.Z, o.Y);
+        const long long a100 = cidx(i5 + 1, i3, i1, o.Z, o.Y), a101 = cidx(i5 + 1, i3, i1 + 1, o.Z, o.Y);
+        const long long a110 = cidx(i5 + 1, i3 + 1, i1, o.Z, o.Y), a111 = cidx(i5 + 1, i3 + 1, i1 + 1, o.Z, o.Y);
+        for (int q = 0; q < Q; q++) {
+            const double *__restrict__ g = o.f + no * q;
+            f[c + N * q] = g[a000] * (1.0 - c3) * (1.0 - c2) * (1.0 - c1) + g[a001] * (1.0 - c3) * (1.0 - c2) * c1 +
+                           g[a010] * (1.0 - c3) * c2 * (1.0 - c1) + g[a011] * (1.0 - c3) * c2 * c1 +
+                           g[a100] * c3 * (1.0 - c2) * (1.0 - c1) + g[a101] * c3 * (1.0 - c2) * c1 +
+                           g[a110] * c3 * c2 * (1.0 - c1) + g[a111] * c3 * c2 * c1;
+        }
+        return;
+    }
+}
+
 inline dim3 zgrid(int Z, int Y, int X, int &bz) {
     bz = Z >= 256 ? 256 : ((Z + 31) / 32) * 32;
     return dim3((Z + bz - 1) / bz, Y, X);
@@ -960,6 +1001,14 @@ cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double
     else { A = p.yDimF; B = p.xDimF; }
     k_pair_extract<<<dim3((A + 63) / 64, B), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, tauA_f, p, face,
                                                           buf, buft, A, B, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_regrid_f64(double *f, int X, int Y, int Z, double dh, double xmin, double ymin, double zmin,
+                              const RegridSrc *src, int nsrc, int *err, cudaStream_t st) {
+    int bz;
+    dim3 g = zgrid(Z, Y, X, bz);
+    k_regrid<<<g, bz, 0, st>>>(f, X, Y, Z, dh, xmin, ymin, zmin, src, nsrc, err);
     return cudaGetLastError();
 }
 

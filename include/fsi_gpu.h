@@ -106,6 +106,19 @@ int fsi_block_get_tau_all(fsi_block_t h, double *tau_all);
 int fsi_block_upload_f(fsi_block_t h, const double *fIn);
 int fsi_block_download_f(fsi_block_t h, double *fIn);
 
+/* Continue files (restart). fsi_continue_write: write_continue_blocks and
+ * write_continue_ (FluidDomain.f90:266-281, 1770-1777): int32 n, int32 step,
+ * real8 time, then per block real8 xmin, ymin, zmin, dh, int32 xDim, yDim,
+ * zDim and real8 fIn(z,y,x,0:18), stream access in native byte order (the
+ * reference's ./DatContinue/continue<time> file). fsi_continue_read:
+ * check_is_continue (FluidDomain.f90:127-236): the fIn of each of the n
+ * blocks is re-gridded on the GPU from the file's blocks by trilinear
+ * interpolation, each cell from the first file block containing it in the
+ * reference's dh order; cells outside every file block keep their values.
+ * step and time receive the file's. FSI_E_ARG for a short or malformed file. */
+int fsi_continue_write(const char *path, const fsi_block_t *blocks, int n, int step, double time);
+int fsi_continue_read(const char *path, const fsi_block_t *blocks, int n, int *step, double *time);
+
 /* initialise_flow: den = denIn, uuu = inflow profile, fIn = feq (FluidDomain.f90:524-544) */
 int fsi_block_initialise(fsi_block_t h, double time);
 

@@ -987,3 +987,66 @@ void or_deliver_s2f(or_block *fa, const or_block *so, const or_pair *p) {
             }
     }
 }
+
+/* check_is_continue's sort of the file's blocks by dh (FluidDomain.f90:151-163):
+ * the exchange sort compares the dh at the original positions i and j while
+ * it permutes the index list, as the reference does */
+void or_continue_order(int nold, const double *dh, int *order) {
+    for (int i = 0; i < nold; i++) order[i] = i;
+    for (int i = 0; i < nold - 1; i++)
+        for (int j = i + 1; j < nold; j++)
+            if (dh[i] > dh[j]) {
+                int t = order[i];
+                order[i] = order[j];
+                order[j] = t;
+            }
+}
+
+/* check_is_continue's trilinear re-grid, FluidDomain.f90:170-226 */
+void or_continue_regrid(or_block *b, int nold, const or_block *old, const int *order) {
+    size_t n = ncell(b);
+    #pragma omp parallel for schedule(static)
+    for (int x = 0; x < b->X; x++) {
+        double xc = b->xmin + (double)x * b->dh;
+        for (int y = 0; y < b->Y; y++) {
+            double yc = b->ymin + (double)y * b->dh;
+            for (int z = 0; z < b->Z; z++) {
+                double zc = b->zmin + (double)z * b->dh;
+                for (int jj = 0; jj < nold; jj++) {
+                    const or_block *o = &old[order[jj]];
+                    double xmx = o->xmin + (double)(o->X - 1) * o->dh;
+                    double ymx = o->ymin + (double)(o->Y - 1) * o->dh;
+                    double zmx = o->zmin + (double)(o->Z - 1) * o->dh;
+                    if (!(zc >= o->zmin && zc <= zmx && yc >= o->ymin && yc <= ymx && xc >= o->xmin && xc <= xmx))
+                        continue;
+                    double c1 = (xc - o->xmin) / o->dh, c2 = (yc - o->ymin) / o->dh, c3 = (zc - o->zmin) / o->dh;
+                    int i1 = (int)floor(c1), i3 = (int)floor(c2), i5 = (int)floor(c3);
+                    if (i1 == o->X - 1) i1 = i1 - 1;
+                    if (i3 == o->Y - 1) i3 = i3 - 1;
+                    if (i5 == o->Z - 1) i5 = i5 - 1;
+                    c1 = c1 - (double)i1;
+                    c2 = c2 - (double)i3;
+                    c3 = c3 - (double)i5;
+                    size_t no = (size_t)o->X * o->Y * o->Z;
+                    size_t a000 = cidx(o, i5, i3, i1), a001 = cidx(o, i5, i3, i1 + 1);
+                    size_t a010 = cidx(o, i5, i3 + 1, i1), a011 = cidx(o, i5, i3 + 1, i1 + 1);
+                    size_t a100 = cidx(o, i5 + 1, i3, i1), a101 = cidx(o, i5 + 1, i3, i1 + 1);
+                    size_t a110 = cidx(o, i5 + 1, i3 + 1, i1), a111 = cidx(o, i5 + 1, i3 + 1, i1 + 1);
+                    size_t c = cidx(b, z, y, x);
+                    for (int q = 0; q < Q; q++) {
+                        const double *f = o->f + no * q;
+                        b->f[c + n * q] = f[a000] * (1.0 - c3) * (1.0 - c2) * (1.0 - c1) +
+                                          f[a001] * (1.0 - c3) * (1.0 - c2) * c1 +
+                                          f[a010] * (1.0 - c3) * c2 * (1.0 - c1) +
+                                          f[a011] * (1.0 - c3) * c2 * c1 +
+                                          f[a100] * c3 * (1.0 - c2) * (1.0 - c1) +
+                                          f[a101] * c3 * (1.0 - c2) * c1 +
+                                          f[a110] * c3 * c2 * (1.0 - c1) +
+                                          f[a111] * c3 * c2 * c1;
+                    }
+                    break;
+                }
+            }
+        }
+    }
+}

@@ -104,6 +104,13 @@ void   or_ib_spread(or_body *bd, int nb, or_block *b);
 int    or_step(or_block *b, const or_flow *fl, or_body *bd, int nb, double Uref,
                int ntol, double dtol, double *tmp, int *iters, double *residual);
 
+/* continue-file re-grid (check_is_continue, FluidDomain.f90:127-236): the
+ * reference's order of the file's blocks (sortdh, 0-based), and the fIn of
+ * block b from the file's blocks old[0..nold) (X, Y, Z, dh, xmin, ymin, zmin
+ * and f used); cells outside every file block keep their values */
+void   or_continue_order(int nold, const double *dh, int *order);
+void   or_continue_regrid(or_block *b, int nold, const or_block *old, const int *order);
+
 /* field statistics (FluidDomain.f90:1739-1768) */
 void   or_field_stat(const or_block *b, double Uref, double l2[3], double linf[3]);
 

@@ -108,6 +108,8 @@ def lib():
         L.or_extract_layer.argtypes = [BP, BP, C.POINTER(OrPair), C.c_int, BUF, BUF]
         L.or_interp_f2s.argtypes = [BP, BP, C.POINTER(OrPair), C.c_int, BUF, BUF, C.c_int]
         L.or_deliver_s2f.argtypes = [BP, BP, C.POINTER(OrPair)]
+        L.or_continue_order.argtypes = [C.c_int, DP, C.POINTER(C.c_int)]
+        L.or_continue_regrid.argtypes = [BP, C.c_int, BP, C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -346,3 +348,55 @@ def probe(u, X, Y, Z, dh, origin, point, Uref):
             v = v + ci * float(uu[k, x - 1, y - 1, z - 1])
         out.append(v * (1.0 / Uref))
     return np.array(out)
+
+
+# ---- continue files (write_continue_blocks / write_continue_ /
+# read_continue_, FluidDomain.f90:266-281, 1770-1789): stream access, native
+# byte order: int32 nblocks, int32 step, real8 time; per block real8 xmin,
+# ymin, zmin, dh, int32 xDim, yDim, zDim, real8 fIn(z,y,x,0:18)
+
+def write_continue(path, step, time, blocks):
+    """blocks: (xmin, ymin, zmin, dh, f) with f of shape (19, X, Y, Z)"""
+    with open(path, "wb") as fh:
+        fh.write(np.array([len(blocks), step], dtype="<i4").tobytes())
+        fh.write(np.array([time], dtype="<f8").tobytes())
+        for xmin, ymin, zmin, dh, f in blocks:
+            fh.write(np.array([xmin, ymin, zmin, dh], dtype="<f8").tobytes())
+            fh.write(np.array(f.shape[1:], dtype="<i4").tobytes())
+            fh.write(np.ascontiguousarray(f, dtype="<f8").tobytes())
+
+
+def read_continue(path):
+    """(step, time, [(xmin, ymin, zmin, dh, f (19, X, Y, Z))])"""
+    raw = open(path, "rb").read()
+    n, step = np.frombuffer(raw, "<i4", 2, 0)
+    time = float(np.frombuffer(raw, "<f8", 1, 8)[0])
+    off = 16
+    out = []
+    for _ in range(int(n)):
+        xmin, ymin, zmin, dh = np.frombuffer(raw, "<f8", 4, off)
+        X, Y, Z = (int(v) for v in np.frombuffer(raw, "<i4", 3, off + 32))
+        off += 44
+        f = np.frombuffer(raw, "<f8", 19 * X * Y * Z, off).reshape(19, X, Y, Z).copy()
+        off += 8 * f.size
+        out.append((float(xmin), float(ymin), float(zmin), float(dh), f))
+    return int(step), time, out
+
+
+def continue_regrid(block, olds):
+    """check_is_continue's re-grid of block.f from olds = [(xmin, ymin, zmin,
+    dh, f)] (cells outside every old block keep their values)"""
+    keep = []
+    arr = (OrBlock * max(1, len(olds)))()
+    for k, (xmin, ymin, zmin, dh, f) in enumerate(olds):
+        fc = np.ascontiguousarray(f, dtype=np.float64)
+        keep.append(fc)
+        o = arr[k]
+        o.X, o.Y, o.Z = fc.shape[1:]
+        o.dh, o.xmin, o.ymin, o.zmin = dh, xmin, ymin, zmin
+        o.f = _dp(fc)
+    dhs = np.array([o[3] for o in olds], dtype=np.float64)
+    order = (C.c_int * max(1, len(olds)))()
+    lib().or_continue_order(len(olds), _dp(dhs), order)
+    lib().or_continue_regrid(C.byref(block.b), len(olds), arr, order)
+    return list(order)[:len(olds)]

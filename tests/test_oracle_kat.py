@@ -268,3 +268,36 @@ def test_vreman_vanishes_in_plane_shear():
     b.collide()
     assert np.all(b.tau_all == b.b.tau)
     assert n == b.tau_all.size
+
+
+def test_continue_file_round_trip_and_identity_regrid(tmp_path):
+    # same grid: the trilinear re-grid returns the file's values exactly
+    fl = O.make_flow(nu=0.02)
+    a = O.Block(7, 6, 5, 0.5, (1.0, 2.0, 3.0), [301] * 6, 1, fl)
+    a.init_tgv(0.05)
+    p = str(tmp_path / "continue")
+    O.write_continue(p, 5, 2.5, [(1.0, 2.0, 3.0, 0.5, a.fview())])
+    step, time, blocks = O.read_continue(p)
+    assert (step, time) == (5, 2.5) and blocks[0][4].tobytes() == a.fview().tobytes()
+    b = O.Block(7, 6, 5, 0.5, (1.0, 2.0, 3.0), [301] * 6, 1, fl)
+    O.continue_regrid(b, blocks)
+    assert b.f.tobytes() == a.f.tobytes()
+
+
+def test_continue_regrid_is_linear_exact():
+    # a field linear in x, y, z is reproduced exactly (to rounding) at any
+    # target spacing inside the file block
+    fl = O.make_flow(nu=0.02)
+    dims = (9, 8, 7)
+    f = np.empty((19,) + dims)
+    x, y, z = np.meshgrid(*(np.arange(n, dtype=float) for n in dims), indexing="ij")
+    for q in range(19):
+        f[q] = 0.1 + 0.01 * q + 0.003 * x - 0.002 * y + 0.001 * z
+    b = O.Block(10, 9, 8, 0.7, (0.3, 0.2, 0.1), [301] * 6, 1, fl)
+    O.continue_regrid(b, [(0.0, 0.0, 0.0, 1.0, f)])
+    xb, yb, zb = np.meshgrid(*(0.3 * (k == 0) + 0.2 * (k == 1) + 0.1 * (k == 2) + 0.7 * np.arange(n)
+                               for k, n in enumerate((10, 9, 8))), indexing="ij")
+    inside = (xb <= 8) & (yb <= 7) & (zb <= 6)
+    for q in range(19):
+        want = 0.1 + 0.01 * q + 0.003 * xb - 0.002 * yb + 0.001 * zb
+        assert np.max(np.abs(b.fview()[q][inside] - want[inside])) < 1e-15
