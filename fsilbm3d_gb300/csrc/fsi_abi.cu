@@ -130,7 +130,9 @@ struct fsi_block {
     double tau = 0, omega = 0, xmax = 0, ymax = 0, zmax = 0;
     double omega2 = 0;          // TRT antisymmetric rate
     double cles = 0;            // constant of the LES model (ConstParams.f90:40-45)
-    double *tau_all = nullptr;  // per-cell relaxation time of the LES models (N)
+    double *tau_all = nullptr;  // per-cell relaxation time of the LES models (N), FP64 forms
+    float *tauf = nullptr;      // the same in FP32 for the offset storage forms
+    float *uf = nullptr;        // FP32 velocity field of WALE / Vreman, offset storage forms (3N)
     int periodic[3] = {0, 0, 0};
     MrtMats mm{};
     int prec = 0;
@@ -309,6 +311,8 @@ void fill_step(fsi_block *h, const double vf[3], double blktime, bool use_window
     a.nu = h->d.nu;
     a.cles = h->cles;
     a.tau_all = h->tau_all;
+    a.tauf = h->tauf;
+    a.uf = h->uf;
     // z faces of code 101 with a face velocity uniform over the face: the
     // paired kernels write their equilibrium while streaming
     if (is_fast(h) && step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel)) {
@@ -375,7 +379,7 @@ void free_block(fsi_block *h) {
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
                     h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
-                    h->d_feat, h->d_out, h->tau_all};
+                    h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -504,9 +508,16 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     chk(cudaMalloc(&h->fb, fbytes));
     chk(cudaMalloc((void **)&h->den, sizeof(double) * h->N));
     chk(cudaMalloc((void **)&h->u, sizeof(double) * 3 * h->N));
-    if (les_model(d->iCollidModel)) {
-        chk(cudaMalloc((void **)&h->tau_all, sizeof(double) * h->N));
-        if (e == cudaSuccess) chk(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
+    {
+        const bool off = h->prec == FSI_PREC_F32 || h->prec == FSI_PREC_F16 || h->prec == FSI_PREC_BF16;
+        if (les_model(d->iCollidModel) && off) {
+            chk(cudaMalloc((void **)&h->tauf, sizeof(float) * h->N));
+            if (e == cudaSuccess) chk(launch_fill_f32(h->tauf, h->N, (float)h->tau, h->st));
+        } else if (les_model(d->iCollidModel)) {
+            chk(cudaMalloc((void **)&h->tau_all, sizeof(double) * h->N));
+            if (e == cudaSuccess) chk(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
+        }
+        if (grad_model(d->iCollidModel) && off) chk(cudaMalloc((void **)&h->uf, sizeof(float) * 3 * h->N));
     }
     if (h->prec != FSI_PREC_F64 && h->prec != FSI_PREC_F64_FAST)
         chk(cudaMalloc((void **)&h->stage, sizeof(double) * 19 * (size_t)h->N));
@@ -566,6 +577,13 @@ int fsi_block_get_omega2(fsi_block_t h, double *omega2) {
 
 int fsi_block_get_tau_all(fsi_block_t h, double *tau_all) {
     if (!h || !tau_all) return fail(FSI_E_ARG, "null argument");
+    if (h->tauf) {
+        std::vector<float> t((size_t)h->N);
+        CK(cudaMemcpyAsync(t.data(), h->tauf, sizeof(float) * h->N, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        for (long long i = 0; i < h->N; i++) tau_all[i] = (double)t[(size_t)i];
+        return FSI_OK;
+    }
     if (!h->tau_all) {
         for (long long i = 0; i < h->N; i++) tau_all[i] = h->tau;
         return FSI_OK;
@@ -815,6 +833,7 @@ int fsi_block_initialise(fsi_block_t h, double time) {
     if (h->esz != 8) CK(launch_convert_to_store(h->stage, h->fa, h->N, h->prec, h->st));
     // calculate_SRT_params (FluidDomain.f90:450-456) resets tau_all
     if (h->tau_all) CK(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
+    if (h->tauf) CK(launch_fill_f32(h->tauf, h->N, (float)h->tau, h->st));
     CK(cudaStreamSynchronize(h->st));
     return FSI_OK;
 }
@@ -1817,6 +1836,8 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
             return fail(FSI_E_ARG, "block %d: batches take the offset storage forms (F32, F16, BF16)", c);
         if (h->prec != blocks[0]->prec || h->d.iCollidModel != blocks[0]->d.iCollidModel)
             return fail(FSI_E_ARG, "block %d: all blocks of a batch share the storage form and collision model", c);
+        if (h->d.iCollidModel != CM_SRT && h->d.iCollidModel != CM_MRT)
+            return fail(FSI_E_ARG, "block %d: batches run SRT or MRT", c);
         StepArgs a;
         double z3[3] = {0, 0, 0};
         fill_step(h, z3, 0.0, false, a);

@@ -150,6 +150,9 @@ struct StepArgs {
     // written for every cell by a macro pass before the step.
     double omega2, tau, nu, cles;
     double *tau_all;
+    // the offset storage forms keep that velocity field and tau_all in FP32
+    // (uf: 3N, tauf: N) and use them instead of u and tau_all
+    float *uf, *tauf;
 };
 
 struct BcArgs {

@@ -109,6 +109,7 @@ cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double
                                 cudaStream_t st);
 cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaStream_t st);
 cudaError_t launch_fill_f64(double *p, long long n, double v, cudaStream_t st);
+cudaError_t launch_fill_f32(float *p, long long n, float v, cudaStream_t st);
 cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const double *tauA_s,
                             const PairGeom &p, int face, const double *buf, const double *buft, int scheme,
                             double *scratch_f, double *scratch_t, long long scratch_cells,

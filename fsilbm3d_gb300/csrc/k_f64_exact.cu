@@ -653,7 +653,8 @@ __global__ void k_pair_extract(const double *__restrict__ ff, int FY, int FZ, lo
     buft[o] = tauA_f ? tauA_f[c] : tau_f;
 }
 
-__global__ void k_fill(double *p, long long n, double v) {
+template <typename T>
+__global__ void k_fill(T *p, long long n, T v) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) p[i] = v;
 }
@@ -1014,7 +1015,13 @@ cudaError_t launch_regrid_f64(double *f, int X, int Y, int Z, double dh, double 
 
 cudaError_t launch_fill_f64(double *p, long long n, double v, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_fill<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, n, v);
+    k_fill<double><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, n, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_f32(float *p, long long n, float v, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_fill<float><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, n, v);
     return cudaGetLastError();
 }
 

@@ -261,41 +261,61 @@ __device__ __forceinline__ void neq_stress_c(const C neq[Q], C q[6]) {
     q[5] = -((neq[15] - neq[16]) - (neq[17] - neq[18]));
 }
 
+// the velocity field and tau_all of the per-cell-rate models in the
+// arithmetic type: FP32 arrays for the offset forms (GB300 converts between
+// FP64 and FP32 on its FP64 pipe), FP64 arrays for FSI_PREC_F64_FAST
+template <int P> __device__ __forceinline__ typename ST<P>::C uval(const StepArgs &a, long long i) {
+    if (ST<P>::OFF) return a.uf[i];
+    else return (typename ST<P>::C)a.u[i];
+}
+template <int P> __device__ __forceinline__ typename ST<P>::C tau_get(const StepArgs &a, long long c) {
+    if (ST<P>::OFF) return a.tauf[c];
+    else return (typename ST<P>::C)a.tau_all[c];
+}
+template <int P> __device__ __forceinline__ void tau_put(const StepArgs &a, long long c, typename ST<P>::C v) {
+    if (ST<P>::OFF) a.tauf[c] = (float)v;
+    else a.tau_all[c] = (double)v;
+}
+
 // center_diff / onesid_diff of velocity component k along axis d, times dh
-template <typename C>
-__device__ __forceinline__ C les_diff_c(const StepArgs &a, int k, int d, int z, int y, int x, long long c, C dh) {
-    const double *__restrict__ u = a.u + a.N * k;
+template <int P>
+__device__ __forceinline__ typename ST<P>::C les_diff_c(const StepArgs &a, int k, int d, int z, int y, int x,
+                                                        long long c, typename ST<P>::C dh) {
+    using C = typename ST<P>::C;
+    const long long b = a.N * k + c;
     const int i = d == 0 ? x : (d == 1 ? y : z);
     const int D = d == 0 ? a.X : (d == 1 ? a.Y : a.Z);
     const long long s = d == 0 ? (long long)a.Z * a.Y : (d == 1 ? (long long)a.Z : 1LL);
-    if (i > 0 && i < D - 1) return ((C)u[c + s] - (C)u[c - s]) * dh;
+    if (i > 0 && i < D - 1) return (uval<P>(a, b + s) - uval<P>(a, b - s)) * dh;
     const long long s1 = i == 0 ? s : -s;
-    return ((C(4) * (C)u[c + s1] - C(3) * (C)u[c]) - (C)u[c + 2 * s1]) * dh;
+    return ((C(4) * uval<P>(a, b + s1) - C(3) * uval<P>(a, b)) - uval<P>(a, b + 2 * s1)) * dh;
 }
 
 template <typename C> __device__ __forceinline__ C pw15(C x) { return x * sqrt(x); }
 template <typename C> __device__ __forceinline__ C pw25(C x) { return (x * x) * sqrt(x); }
 template <typename C> __device__ __forceinline__ C pw125(C x) { return x * sqrt(sqrt(x)); }
 
-template <typename C, int MODEL>
-__device__ __forceinline__ C les_rate_c(const StepArgs &a, const Scal<C> &sc, const C neq[Q], C rho, int z, int y,
-                                        int x, long long c) {
+template <int P, int MODEL>
+__device__ __forceinline__ typename ST<P>::C les_rate_c(const StepArgs &a, const Scal<typename ST<P>::C> &sc,
+                                                        const typename ST<P>::C neq[Q], typename ST<P>::C rho, int z,
+                                                        int y, int x, long long c) {
+    using C = typename ST<P>::C;
     C t;
     if (MODEL == CM_SMAG) {
         C q[6];
         neq_stress_c(neq, q);
         const C QQ = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + C(2) * (q[3] * q[3] + q[4] * q[4] + q[5] * q[5]);
         const C tau_t = sqrt(sc.tau * sc.tau + sc.cles * sqrt(QQ) / rho);
-        a.tau_all[c] = (double)(C(0.5) * (sc.tau + tau_t));
+        tau_put<P>(a, c, C(0.5) * (sc.tau + tau_t));
         return C(2) / (sc.tau + tau_t);
     } else if (MODEL == CM_WALE) {
         C q[6];
         neq_stress_c(neq, q);
-        const C k = -(C(1.5) * sc.dh) / (rho * (C)a.tau_all[c]);
+        const C k = -(C(1.5) * sc.dh) / (rho * tau_get<P>(a, c));
         C S11 = k * q[0], S22 = k * q[1], S33 = k * q[2], S12 = k * q[3], S13 = k * q[4], S23 = k * q[5];
-        C ox = C(0.5) * (les_diff_c<C>(a, 2, 1, z, y, x, c, sc.dh) - les_diff_c<C>(a, 1, 2, z, y, x, c, sc.dh));
-        C oy = C(0.5) * (les_diff_c<C>(a, 0, 2, z, y, x, c, sc.dh) - les_diff_c<C>(a, 2, 0, z, y, x, c, sc.dh));
-        C oz = C(0.5) * (les_diff_c<C>(a, 1, 0, z, y, x, c, sc.dh) - les_diff_c<C>(a, 0, 1, z, y, x, c, sc.dh));
+        C ox = C(0.5) * (les_diff_c<P>(a, 2, 1, z, y, x, c, sc.dh) - les_diff_c<P>(a, 1, 2, z, y, x, c, sc.dh));
+        C oy = C(0.5) * (les_diff_c<P>(a, 0, 2, z, y, x, c, sc.dh) - les_diff_c<P>(a, 2, 0, z, y, x, c, sc.dh));
+        C oz = C(0.5) * (les_diff_c<P>(a, 1, 0, z, y, x, c, sc.dh) - les_diff_c<P>(a, 0, 1, z, y, x, c, sc.dh));
         C O12 = C(-0.5) * oz, O13 = C(0.5) * oy, O23 = C(-0.5) * ox;
         C g = fmax(fmax(fmax(fabs(S11), fabs(S22)), fmax(fabs(S33), fabs(S12))),
                    fmax(fmax(fabs(S13), fabs(S23)), fmax(fmax(fabs(O12), fabs(O13)), fabs(O23))));
@@ -324,7 +344,7 @@ __device__ __forceinline__ C les_rate_c(const StepArgs &a, const Scal<C> &sc, co
 #pragma unroll
         for (int j = 0; j < 3; j++)
 #pragma unroll
-            for (int i = 0; i < 3; i++) m[i][j] = C(0.5) * les_diff_c<C>(a, i, j, z, y, x, c, sc.dh);
+            for (int i = 0; i < 3; i++) m[i][j] = C(0.5) * les_diff_c<P>(a, i, j, z, y, x, c, sc.dh);
         C g = C(0);
 #pragma unroll
         for (int i = 0; i < 3; i++)
@@ -349,7 +369,7 @@ __device__ __forceinline__ C les_rate_c(const StepArgs &a, const Scal<C> &sc, co
         }
         t = (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5);
     }
-    a.tau_all[c] = (double)t;
+    tau_put<P>(a, c, t);
     return C(1) / t;
 }
 
@@ -389,7 +409,7 @@ __device__ __forceinline__ void collide_rate(typename ST<P>::C g[Q], typename ST
             g[m] += sp - sm;
         }
     } else {
-        const C om = les_rate_c<C, MODEL>(a, sc, neq, rho, z, y, x, c);
+        const C om = les_rate_c<P, MODEL>(a, sc, neq, rho, z, y, x, c);
         const C cf = C(1) - C(0.5) * om;
 #pragma unroll
         for (int i = 0; i < Q; i++) g[i] += om * neq[i] + cf * flb[i];
@@ -431,7 +451,7 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
         F0 = sc.vf[0]; F1 = sc.vf[1]; F2 = sc.vf[2];
         forced = sc.forced != 0;
     }
-    if (HOOKS && !grad_model(MODEL) &&
+    if (HOOKS && !(grad_model(MODEL) && !T::OFF) &&
         ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
          (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2))) {
         a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
@@ -696,21 +716,97 @@ __device__ __forceinline__ void mrt_backward(const float2 t[Q], float2 &E0, floa
 template <int MODEL, bool FORCED, bool KEEPG, class EMIT>
 __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1,
                                              float2 u2, float2 F0, float2 F1, float2 F2, const Scal<float> &sc,
-                                             const MrtS &ms, EMIT &&emit) {
+                                             const MrtS &ms, EMIT &&emit, float2 *tau_rel = nullptr) {
     const float om = sc.om;
     const float2 k15 = mul2(f2(1.5f), fma2(u0, u0, fma2(u1, u1, mul2(u2, u2))));
     float2 uF = f2(0.f);
     if (FORCED) uF = fma2(u0, F0, fma2(u1, F1, mul2(u2, F2)));
     const float w0 = (float)wt_(0), w1 = (float)wt_(1), w2 = (float)wt_(7);
-    if (MODEL == 1) {
-        const float2 omc = f2(1.0f - om);
+    // per pair: fsum = feq_i + feq_o, fdif = feq_i - feq_o,
+    // FS = (Flb_i + Flb_o)/2, FA = (Flb_i - Flb_o)/2
+    auto pair_terms = [&](int i, float2 &fsum, float2 &fdif, float2 &FS, float2 &FA) {
+        const float w = (float)wt_(i);
+        const float2 eu = edot(i, u0, u1, u2);
+        const float2 wr = mul2(f2(w), rho);
+        fsum = mul2(f2(2.0f), fma2(f2(w), drho, mul2(wr, fma2(f2(4.5f), mul2(eu, eu), neg2(k15)))));
+        fdif = mul2(mul2(f2(6.0f), wr), eu);
+        if (FORCED) {
+            const float2 eF = edot(i, F0, F1, F2);
+            FS = mul2(f2(sc.dh3 * w), sub2(mul2(f2(3.0f), mul2(eu, eF)), uF));
+            FA = mul2(f2(sc.dh3 * w), eF);
+        } else {
+            FS = f2(0.f);
+            FA = f2(0.f);
+        }
+    };
+    if (MODEL == CM_SMAG) {
+        // SRT with the Smagorinsky rate (FluidDomain.f90:1239-1242, smag
+        // :1265-1281). The stress sums Q_ab = sum e_a e_b fneq_i take the
+        // pair sums s = neq_i + neq_o only (fneq = -neq).
+        float2 q11 = f2(0.f), q22 = f2(0.f), q33 = f2(0.f), q12 = f2(0.f), q13 = f2(0.f), q23 = f2(0.f);
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int i = pr_(k), o = opp_(i);
+            float2 fsum, fdif, FS, FA;
+            pair_terms(i, fsum, fdif, FS, FA);
+            const float2 sv = sub2(add2(g[i], g[o]), fsum);  // fneq_i + fneq_o
+            if (ex_(i)) q11 = add2(q11, sv);
+            if (ey_(i)) q22 = add2(q22, sv);
+            if (ez_(i)) q33 = add2(q33, sv);
+            if (ex_(i) && ey_(i)) q12 = ex_(i) * ey_(i) > 0 ? add2(q12, sv) : sub2(q12, sv);
+            if (ex_(i) && ez_(i)) q13 = ex_(i) * ez_(i) > 0 ? add2(q13, sv) : sub2(q13, sv);
+            if (ey_(i) && ez_(i)) q23 = ey_(i) * ez_(i) > 0 ? add2(q23, sv) : sub2(q23, sv);
+        }
+        const float2 qq = fma2(q11, q11, fma2(q22, q22, fma2(q33, q33, mul2(f2(2.0f), fma2(q12, q12, fma2(q13, q13,
+                                                                                                   mul2(q23, q23)))))));
+        float2 omv, cfv;
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            const float tau_t = sqrtf(sc.tau * sc.tau + sc.cles * sqrtf(getl(qq, l)) / getl(rho, l));
+            setl(omv, l, 2.0f / (sc.tau + tau_t));
+            setl(cfv, l, 1.0f - 0.5f * getl(omv, l));
+            if (tau_rel) setl(*tau_rel, l, 0.5f * (sc.tau + tau_t));
+        }
+        const float2 feq0 = mul2(f2(w0), sub2(drho, mul2(rho, k15)));
+        float2 n0 = fma2(omv, sub2(feq0, g[0]), g[0]);
+        if (FORCED) n0 = sub2(n0, mul2(mul2(cfv, f2(sc.dh3 * w0)), uF));
+        emit(0, n0);
+        const float2 hov = mul2(f2(-0.5f), omv);
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int i = pr_(k), o = opp_(i);
+            float2 fsum, fdif, FS, FA;
+            pair_terms(i, fsum, fdif, FS, FA);
+            // neq_i,o = (-s_k +- d)/2, d = fdif - (g_i - g_o)
+            const float2 dv = sub2(fdif, sub2(g[i], g[o]));
+            float2 A = mul2(hov, sub2(add2(g[i], g[o]), fsum));  // Om (neq_i + neq_o)/2
+            float2 B = mul2(mul2(f2(-1.0f), hov), dv);  // Om (neq_i - neq_o)/2
+            if (FORCED) {
+                A = fma2(cfv, FS, A);
+                B = fma2(cfv, FA, B);
+            }
+            emit(i, add2(g[i], add2(A, B)));
+            emit(o, add2(g[o], sub2(A, B)));
+        }
+    } else if (MODEL == CM_SRT || MODEL == CM_TRT) {
+        // SRT, and TRT (FluidDomain.f90:1228-1235) in the same form: per pair
+        //   g'_i = al g_i + be g_o + S + A,  g'_o = al g_o + be g_i + S - A,
+        //   S = Om/2 (feq_i + feq_o), A = Om2/2 (feq_i - feq_o),
+        //   al = 1 - (Om + Om2)/2, be = (Om2 - Om)/2  (SRT: Om2 = Om),
+        // forcing (1 - Om/2)(Flb_i + Flb_o)/2 +- (1 - Om2/2)(Flb_i - Flb_o)/2
+        constexpr bool TRT = MODEL == CM_TRT;
+        const float oa = TRT ? sc.om2 : om;
+        const float2 omc = f2(TRT ? 1.0f - 0.5f * (om + oa) : 1.0f - om);
+        const float bet = TRT ? 0.5f * (oa - om) : 0.0f;
         const float2 base = sub2(drho, mul2(rho, k15));
         const float2 orho = mul2(f2(om), rho);
+        const float2 arho = TRT ? mul2(f2(oa), rho) : orho;
         const float2 ac0 = mul2(f2(om * w0), base);
-        const float2 ac1 = mul2(f2(om * w1), base), bc1 = mul2(f2(4.5f * w1), orho), cc1 = mul2(f2(3.0f * w1), orho);
-        const float2 ac2 = mul2(f2(om * w2), base), bc2 = mul2(f2(4.5f * w2), orho), cc2 = mul2(f2(3.0f * w2), orho);
+        const float2 ac1 = mul2(f2(om * w1), base), bc1 = mul2(f2(4.5f * w1), orho), cc1 = mul2(f2(3.0f * w1), arho);
+        const float2 ac2 = mul2(f2(om * w2), base), bc2 = mul2(f2(4.5f * w2), orho), cc2 = mul2(f2(3.0f * w2), arho);
         const float cf = (1.0f - 0.5f * om) * sc.dh3;
-        float2 n0 = fma2(omc, g[0], ac0);
+        const float cfa = TRT ? (1.0f - 0.5f * oa) * sc.dh3 : cf;
+        float2 n0 = fma2(TRT ? f2(1.0f - om) : omc, g[0], ac0);
         if (FORCED) n0 = sub2(n0, mul2(f2(cf * w0), uF));
         emit(0, n0);
 #pragma unroll
@@ -722,10 +818,15 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
             const float2 Am = mul2(cls1 ? cc1 : cc2, eu);
             float2 ni = fma2(omc, g[i], add2(Sm, Am));
             float2 no = fma2(omc, g[o], sub2(Sm, Am));
+            if (TRT) {
+                ni = fma2(f2(bet), g[o], ni);
+                no = fma2(f2(bet), g[i], no);
+            }
             if (FORCED) {
                 const float2 eF = edot(i, F0, F1, F2);
-                const float cw = cf * (cls1 ? w1 : w2);
-                const float2 Fs = mul2(f2(cw), sub2(mul2(f2(3.0f), mul2(eF, eu)), uF)), Fa = mul2(f2(cw), eF);
+                const float wc = cls1 ? w1 : w2;
+                const float2 Fs = mul2(f2(cf * wc), sub2(mul2(f2(3.0f), mul2(eF, eu)), uF));
+                const float2 Fa = mul2(f2(cfa * wc), eF);
                 ni = add2(ni, add2(Fs, Fa));
                 no = add2(no, sub2(Fs, Fa));
             }
@@ -734,23 +835,6 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
         }
     } else {
         const float dh3 = sc.dh3;
-        // per pair: fsum = feq_i + feq_o, fdif = feq_i - feq_o,
-        // FS = (Flb_i + Flb_o)/2, FA = (Flb_i - Flb_o)/2
-        auto pair_terms = [&](int i, float2 &fsum, float2 &fdif, float2 &FS, float2 &FA) {
-            const float w = (float)wt_(i);
-            const float2 eu = edot(i, u0, u1, u2);
-            const float2 wr = mul2(f2(w), rho);
-            fsum = mul2(f2(2.0f), fma2(f2(w), drho, mul2(wr, fma2(f2(4.5f), mul2(eu, eu), neg2(k15)))));
-            fdif = mul2(mul2(f2(6.0f), wr), eu);
-            if (FORCED) {
-                const float2 eF = edot(i, F0, F1, F2);
-                FS = mul2(f2(dh3 * w), sub2(mul2(f2(3.0f), mul2(eu, eF)), uF));
-                FA = mul2(f2(dh3 * w), eF);
-            } else {
-                FS = f2(0.f);
-                FA = f2(0.f);
-            }
-        };
         const float2 feq0 = mul2(f2(w0), sub2(drho, mul2(rho, k15)));
         const float2 hf0 = FORCED ? mul2(f2(0.5f * dh3 * w0), uF) : f2(0.f);  // -Flb_0/2
         // r = feq - g - Flb/2: rest r0, pair sums rs = r_i + r_o, differences rd = r_i - r_o
@@ -819,10 +903,11 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
 // collide_emit with the results written back into g
 template <int MODEL, bool FORCED>
 __device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1, float2 u2,
-                                         float2 F0, float2 F1, float2 F2, const Scal<float> &sc, const MrtS &ms) {
+                                         float2 F0, float2 F1, float2 F2, const Scal<float> &sc, const MrtS &ms,
+                                         float2 *tau_rel = nullptr) {
     float2 out[Q];
     collide_emit<MODEL, FORCED, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms,
-                                      [&](int i, float2 v) { out[i] = v; });
+                                      [&](int i, float2 v) { out[i] = v; }, tau_rel);
 #pragma unroll
     for (int i = 0; i < Q; i++) g[i] = out[i];
 }
@@ -841,8 +926,9 @@ __device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, f
 #endif
 template <int P, int MODEL, bool FORCED>
 constexpr int pair_minb() {
-    return MODEL == 1 ? FSI_PAIR_MINB_SRT
-                      : ((FORCED || P == FSI_PREC_F32) ? FSI_PAIR_MINB_MRT_FORCED : FSI_PAIR_MINB_MRT);
+    return (MODEL == CM_SRT || MODEL == CM_TRT)
+               ? FSI_PAIR_MINB_SRT
+               : ((FORCED || P == FSI_PREC_F32) ? FSI_PAIR_MINB_MRT_FORCED : FSI_PAIR_MINB_MRT);
 }
 
 // The bulk step: every cell takes den/u from its own distributions and the
@@ -902,9 +988,14 @@ __device__ __forceinline__ void pair_body(const StepArgs &a, const Offs<int> &of
             *(S2 *)(sm + (zslot_(i) * R + ty) * Z + z0) = V::enc(v);
         }
     };
-    if (MODEL == 1) {
-        // SRT: stored pair by pair, so that the 64-register budget holds
+    if (MODEL == CM_SRT || MODEL == CM_TRT) {
+        // SRT, TRT: stored pair by pair, so that the 64-register budget holds
         collide_emit<MODEL, FORCED, false>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit);
+    } else if (MODEL == CM_SMAG) {
+        // tau_all(z0, z0+1) with the populations (c is even: an aligned pair)
+        float2 tr;
+        collide_emit<MODEL, FORCED, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit, &tr);
+        if (active) *(float2 *)(a.tauf + c) = tr;
     } else {
         // MRT: all 19 collided first, then stored under one branch
         collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
@@ -1207,9 +1298,17 @@ __device__ __forceinline__ void win_fix_body(const StepArgs &a, const Scal<float
         setl(F1, l, (float)w.force[wc + w.n]);
         setl(F2, l, (float)w.force[wc + 2 * w.n]);
     }
-    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
+    float2 tr;
+    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, &tr);
     push_cell<P>(a, x[0], y[0], z[0], g, 0);
     if (two) push_cell<P>(a, x[1], y[1], z[1], g, 1);
+    if (MODEL == CM_SMAG) {
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            if (l == 1 && !two) break;
+            a.tauf[(long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l])] = getl(tr, l);
+        }
+    }
 }
 
 template <int P, int MODEL>
@@ -1302,6 +1401,10 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
     sc.dh3 = 3.0f * (float)a.dh;
     for (int k = 0; k < 3; k++) sc.vf[k] = (float)a.vf[k];
     sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
+    sc.om2 = (float)a.omega2;
+    sc.tau = (float)a.tau;
+    sc.nu = (float)a.nu;
+    sc.cles = (float)a.cles;
     MrtS ms{};
     if (MODEL == 3)
         for (int k = 0; k < Q; k++) ms.sd[k] = (float)mm->sd[k];
@@ -1309,13 +1412,15 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
     const int R = std::max(1, 256 / tpr);
     dim3 blk(tpr, R), grd(1, (a.Y + R - 1) / R, a.X);
     size_t smem = (size_t)10 * R * a.Z * sizeof(typename V2<P>::S);
-    // the pipelined persistent form (on request; it needs 16-byte aligned
-    // population rows) or the paired form
-    const bool pipe = a.variant == 2 && a.Z % 8 == 0;
+    // the pipelined persistent form (on request, SRT and MRT; it needs
+    // 16-byte aligned population rows) or the paired form
+    const bool pipe = a.variant == 2 && a.Z % 8 == 0 && (MODEL == CM_SRT || MODEL == CM_MRT);
     if (pipe) {
-        cudaError_t e = sc.forced ? pipe_run<P, MODEL, true>(a, of, sc, ms, tpr, R, st)
-                                  : pipe_run<P, MODEL, false>(a, of, sc, ms, tpr, R, st);
-        if (e != cudaSuccess) return e;
+        if constexpr (MODEL == CM_SRT || MODEL == CM_MRT) {
+            cudaError_t e = sc.forced ? pipe_run<P, MODEL, true>(a, of, sc, ms, tpr, R, st)
+                                      : pipe_run<P, MODEL, false>(a, of, sc, ms, tpr, R, st);
+            if (e != cudaSuccess) return e;
+        }
     } else if (sc.forced) {
         k_step_pair<P, MODEL, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
     } else {
@@ -1363,7 +1468,7 @@ __global__ void k_macro_fast(const void *__restrict__ fs, double *den, double *u
 // den/uuu of every cell as the collision sees them (IB window cells from the
 // IB stage), before the step of a model that reads neighbour velocities
 template <int P>
-__global__ void k_step_macro_fast(StepArgs a) {
+__global__ void k_step_macro_fast(StepArgs a, Scal<typename ST<P>::C> sc) {
     using T = ST<P>;
     using C = typename T::C;
     const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
@@ -1377,19 +1482,27 @@ __global__ void k_step_macro_fast(StepArgs a) {
         C rho, drho;
         if (T::OFF) { drho = (C)(d - 1.0); rho = C(1) + drho; }
         else { rho = (C)d; drho = rho - C(1); }
-        a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
-        a.u[c] = (C)w.u[wc]; a.u[c + N] = (C)w.u[wc + w.n]; a.u[c + 2 * N] = (C)w.u[wc + 2 * w.n];
+        if (T::OFF) {
+            a.uf[c] = (C)w.u[wc]; a.uf[c + N] = (C)w.u[wc + w.n]; a.uf[c + 2 * N] = (C)w.u[wc + 2 * w.n];
+        } else {
+            a.den[c] = (double)rho;
+            a.u[c] = (C)w.u[wc]; a.u[c + N] = (C)w.u[wc + w.n]; a.u[c + 2 * N] = (C)w.u[wc + 2 * w.n];
+        }
+        (void)drho;
         return;
     }
     const typename T::S *src = (const typename T::S *)a.src;
     C g[Q];
 #pragma unroll
     for (int i = 0; i < Q; i++) g[i] = T::dec(src[c + N * i]);
-    const C vf[3] = {(C)a.vf[0], (C)a.vf[1], (C)a.vf[2]};
     C rho, drho, u0, u1, u2;
-    macro_fast<P>(g, vf, (C)a.dh, rho, drho, u0, u1, u2);
-    a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
-    a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
+    macro_fast<P>(g, sc.vf, sc.dh, rho, drho, u0, u1, u2);
+    if (T::OFF) {
+        a.uf[c] = u0; a.uf[c + N] = u1; a.uf[c + 2 * N] = u2;
+    } else {
+        a.den[c] = (double)rho;
+        a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
+    }
 }
 
 template <int P>
@@ -2009,7 +2122,8 @@ cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
 
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
-    return prec != FSI_PREC_F64_FAST && (model == CM_SRT || (model == CM_MRT && mm->diag)) && small &&
+    return prec != FSI_PREC_F64_FAST &&
+           (model == CM_SRT || model == CM_TRT || model == CM_SMAG || (model == CM_MRT && mm->diag)) && small &&
            a.Z % 2 == 0 && a.Z <= 512;
 }
 
@@ -2027,7 +2141,14 @@ cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int
 cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st) {
     int bz = a.Z >= 256 ? 256 : ((a.Z + 31) / 32) * 32;
     dim3 g((a.Z + bz - 1) / bz, a.Y, a.X);
-    FSI_DISPATCH(prec, k_step_macro_fast<PP><<<g, bz, 0, st>>>(a); return cudaGetLastError())
+    FSI_DISPATCH(prec, {
+        using CC = typename ST<PP>::C;
+        Scal<CC> sc{};
+        sc.dh = (CC)a.dh;
+        for (int k = 0; k < 3; k++) sc.vf[k] = (CC)a.vf[k];
+        k_step_macro_fast<PP><<<g, bz, 0, st>>>(a, sc);
+        return cudaGetLastError();
+    })
 }
 
 cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
