@@ -882,7 +882,7 @@ int fsi_block_set_kernel(fsi_block_t h, int kernel) {
 
 int fsi_block_set_ib_mode(fsi_block_t h, int mode) {
     if (!h) return fail(FSI_E_ARG, "null handle");
-    if (mode < FSI_IB_AUTO || mode > FSI_IB_CLUSTER) return fail(FSI_E_ARG, "unknown IB mode %d", mode);
+    if (mode < FSI_IB_AUTO || mode > FSI_IB_OVERLAP) return fail(FSI_E_ARG, "unknown IB mode %d", mode);
     h->ib_mode = mode;
     return FSI_OK;
 }
@@ -1110,7 +1110,17 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     a.aux = wm.aux ? h->d_aux : nullptr;
     a.feat = wm.features ? h->d_feat : nullptr;
     a.Uref = Uref;
-    if (wm.step && h->ib_mode == FSI_IB_CLUSTER && !wm.mlp && !wm.features && h->prec != FSI_PREC_F64_FAST) {
+    // the IB stage beside the bulk step: on request, and by default for the
+    // offset forms when the paired kernels run the step (their window fix-up
+    // and face hooks wait for it)
+    int mode = h->ib_mode;
+    if (mode == FSI_IB_AUTO && wm.step && h->prec != FSI_PREC_F64_FAST) {
+        StepArgs t;
+        fill_step(h, wm.step_vf, wm.step_time, true, t);
+        mode = step_fast_paired(t, &h->mm, h->prec, h->d.iCollidModel) ? FSI_IB_OVERLAP : FSI_IB_GRID;
+    }
+    if (wm.step && (mode == FSI_IB_CLUSTER || mode == FSI_IB_OVERLAP) && !wm.mlp && !wm.features &&
+        h->prec != FSI_PREC_F64_FAST) {
         // the IB stage on one cluster on the second stream, beside the bulk
         // step (both only read the state); the window fix-up and the face
         // hooks wait for it
@@ -1123,7 +1133,13 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         }
         CK(cudaEventRecord(h->ev_fork, h->st));
         CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
-        CK(launch_ib_cluster(a, h->prec, h->st2));
+        if (mode == FSI_IB_OVERLAP) {
+            long long need = std::max<long long>((h->Mtot + 7) / 8, (h->Nw + 255) / 256);
+            CK(launch_ib_coop(a, h->prec, (int)std::max<long long>(1, std::min<long long>(need, h->coop_grid)),
+                              h->st2));
+        } else {
+            CK(launch_ib_cluster(a, h->prec, h->st2));
+        }
         CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st2));
         CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st2));
         CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st2));

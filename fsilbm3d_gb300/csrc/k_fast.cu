@@ -1288,15 +1288,15 @@ __device__ __forceinline__ void win_fix_body(const StepArgs &a, const Scal<float
         const long long wc = (l == 1 && !two) ? w0 : w0 + l;
         win_cell(w, wc, x[l], y[l], z[l]);
         load_cell<P>(a, x[l], y[l], z[l], g, l);
-        const float d = (float)(w.den[wc] - 1.0);
+        const float d = (float)(__ldcg(w.den + wc) - 1.0);
         setl(drho, l, d);
         setl(rho, l, 1.0f + d);
-        setl(u0, l, (float)w.u[wc]);
-        setl(u1, l, (float)w.u[wc + w.n]);
-        setl(u2, l, (float)w.u[wc + 2 * w.n]);
-        setl(F0, l, (float)w.force[wc]);
-        setl(F1, l, (float)w.force[wc + w.n]);
-        setl(F2, l, (float)w.force[wc + 2 * w.n]);
+        setl(u0, l, (float)__ldcg(w.u + wc));
+        setl(u1, l, (float)__ldcg(w.u + wc + w.n));
+        setl(u2, l, (float)__ldcg(w.u + wc + 2 * w.n));
+        setl(F0, l, (float)__ldcg(w.force + wc));
+        setl(F1, l, (float)__ldcg(w.force + wc + w.n));
+        setl(F2, l, (float)__ldcg(w.force + wc + 2 * w.n));
     }
     float2 tr;
     collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, &tr);
@@ -1352,15 +1352,15 @@ __global__ void __launch_bounds__(128) k_face_hook(StepArgs a, Scal<float> sc, M
         if (x[l] >= w.x0 && x[l] <= w.x1 && y[l] >= w.y0 && y[l] <= w.y1 && z[l] >= w.z0 && z[l] <= w.z1) {
             const long long wc = (long long)(z[l] - w.z0) +
                                  (long long)w.WZ * ((long long)(y[l] - w.y0) + (long long)w.WY * (x[l] - w.x0));
-            const float d = (float)(w.den[wc] - 1.0);
+            const float d = (float)(__ldcg(w.den + wc) - 1.0);
             setl(drho, l, d);
             setl(rho, l, 1.0f + d);
-            setl(u0, l, (float)w.u[wc]);
-            setl(u1, l, (float)w.u[wc + w.n]);
-            setl(u2, l, (float)w.u[wc + 2 * w.n]);
-            setl(F0, l, (float)w.force[wc]);
-            setl(F1, l, (float)w.force[wc + w.n]);
-            setl(F2, l, (float)w.force[wc + 2 * w.n]);
+            setl(u0, l, (float)__ldcg(w.u + wc));
+            setl(u1, l, (float)__ldcg(w.u + wc + w.n));
+            setl(u2, l, (float)__ldcg(w.u + wc + 2 * w.n));
+            setl(F0, l, (float)__ldcg(w.force + wc));
+            setl(F1, l, (float)__ldcg(w.force + wc + w.n));
+            setl(F2, l, (float)__ldcg(w.force + wc + 2 * w.n));
         }
     }
     if (!hw) {

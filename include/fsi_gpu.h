@@ -174,14 +174,17 @@ int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps
 int fsi_block_set_kernel(fsi_block_t h, int kernel);
 
 /* No counterpart in the reference: how fsi_block_ib_step runs the IB stage
- * of the offset forms. FSI_IB_GRID (and FSI_IB_AUTO): one cooperative launch
- * over the GPU, then the fluid step. FSI_IB_CLUSTER: one thread-block cluster
- * on a second stream beside the bulk step (both only read the state), the
- * IB-window fix-up after both; pays off when the bulk step outlasts the IB
- * stage. Same stopping rule and results to rounding. */
+ * of the fast forms. FSI_IB_GRID: one cooperative launch over the GPU, then
+ * the fluid step. FSI_IB_OVERLAP: the same cooperative launch on a second,
+ * high-priority stream beside the bulk step (both only read the state), the
+ * IB-window fix-up and face hooks after both. FSI_IB_CLUSTER: as OVERLAP with
+ * the IB stage on one thread-block cluster. FSI_IB_AUTO: OVERLAP for the
+ * offset forms when the paired kernels run the step, else GRID. Same
+ * stopping rule and results to rounding. */
 #define FSI_IB_AUTO    0
 #define FSI_IB_GRID    1
 #define FSI_IB_CLUSTER 2
+#define FSI_IB_OVERLAP 3
 int fsi_block_set_ib_mode(fsi_block_t h, int mode);
 
 /* No counterpart in the reference: device time of the work a host loop
