@@ -219,6 +219,9 @@ namespace {
 
 bool is_fast(const fsi_block *h) { return h->prec != FSI_PREC_F64; }
 
+// tau_all of a block for the refinement exchange
+TauSrc tau_src(const fsi_block *h) { return TauSrc{h->tau, h->tau_all, h->tauf}; }
+
 Vel make_vel(const fsi_block *h, double blktime) {
     Vel v{};
     v.kind = h->d.velocityKind;
@@ -1355,8 +1358,7 @@ int fsi_ib_get_window(fsi_block_t h, int box[6]) {
 int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme) {
     if (!out || !fa || !so) return fail(FSI_E_ARG, "null argument");
     *out = nullptr;
-    if (fa->prec != FSI_PREC_F64 || so->prec != FSI_PREC_F64)
-        return fail(FSI_E_ARG, "block refinement is built for the FP64 form");
+    if (fa->prec != so->prec) return fail(FSI_E_ARG, "father and son share one storage form");
     fsi_pair *p = new fsi_pair();
     p->fa = fa;
     p->so = so;
@@ -1453,7 +1455,7 @@ int fsi_pair_extract(fsi_pair_t p, int time_level) {
     fsi_block *fa = p->fa;
     for (int k = 0; k < 6; k++) {
         if (p->so->d.bndConds[k] != BC_FLUID) continue;
-        CK(launch_pair_extract((const double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, fa->tau_all, p->p, k, p->buf[k][time_level - 1],
+        CK(launch_pair_extract(fa->fa, fa->prec, fa->X, fa->Y, fa->Z, tau_src(fa), p->p, k, p->buf[k][time_level - 1],
                                p->buft[k][time_level - 1], p->d_err, fa->st));
         if (time_level == 2) {
             int ax = k >> 1;
@@ -1473,7 +1475,7 @@ int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]) {
     for (int k = 0; k < 6; k++) {
         if (p->p.sds[k] == 0) continue;
         int lvl = (n_timeStep == 0) ? 0 : 1;
-        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, so->tau_all, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
+        CK(launch_pair_f2s(so->fa, so->prec, so->X, so->Y, so->Z, tau_src(so), p->p, k, p->buf[k][lvl], p->buft[k][lvl],
                            p->scheme, p->scr_f, p->scr_t, p->scr_cells, vf, fa->d.dh, p->d_err, so->st));
     }
     CK(cudaStreamSynchronize(so->st));
@@ -1487,8 +1489,8 @@ int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
     for (int k = 0; k < 6; k++) {
         int want = (k % 2 == 0) ? 1 : -1;
         if (p->p.sds[k] != want) continue;
-        CK(launch_pair_s2f((double *)fa->fa, fa->X, fa->Y, fa->Z, fa->tau, fa->tau_all, (const double *)so->fa, so->X,
-                           so->Y, so->Z, so->tau, so->tau_all, p->p, k, vf, so->d.dh, p->d_err, fa->st));
+        CK(launch_pair_s2f(fa->fa, fa->prec, fa->X, fa->Y, fa->Z, tau_src(fa), so->fa, so->X, so->Y, so->Z, tau_src(so),
+                           p->p, k, vf, so->d.dh, p->d_err, fa->st));
     }
     CK(cudaStreamSynchronize(fa->st));
     return pair_check(p);
@@ -1852,8 +1854,9 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
             return fail(FSI_E_ARG, "block %d: batches take the offset storage forms (F32, F16, BF16)", c);
         if (h->prec != blocks[0]->prec || h->d.iCollidModel != blocks[0]->d.iCollidModel)
             return fail(FSI_E_ARG, "block %d: all blocks of a batch share the storage form and collision model", c);
-        if (h->d.iCollidModel != CM_SRT && h->d.iCollidModel != CM_MRT)
-            return fail(FSI_E_ARG, "block %d: batches run SRT or MRT", c);
+        if (h->d.iCollidModel != CM_SRT && h->d.iCollidModel != CM_MRT && h->d.iCollidModel != CM_TRT &&
+            h->d.iCollidModel != CM_SMAG)
+            return fail(FSI_E_ARG, "block %d: batches run SRT, TRT, MRT or Smagorinsky", c);
         StepArgs a;
         double z3[3] = {0, 0, 0};
         fill_step(h, z3, 0.0, false, a);
@@ -2132,7 +2135,7 @@ extern "C" int fsi_pair_father_to_son_static(fsi_pair_t p, int n_timeStep, const
     for (int k = 0; k < 6; k++) {
         if (p->p.sds[k] == 0) continue;
         int lvl = (n_timeStep == 0) ? 0 : 1;
-        CK(launch_pair_f2s((double *)so->fa, so->X, so->Y, so->Z, so->tau, so->tau_all, p->p, k, p->buf[k][lvl], p->buft[k][lvl],
+        CK(launch_pair_f2s(so->fa, so->prec, so->X, so->Y, so->Z, tau_src(so), p->p, k, p->buf[k][lvl], p->buft[k][lvl],
                            p->scheme, scr_f, scr_t, FSI_STATIC_FACE_CELLS, vf, fa->d.dh, p->d_err, so->st));
     }
     CK(cudaStreamSynchronize(so->st));

@@ -2,6 +2,7 @@
 // Each launcher enqueues on `st` and returns the launch status.
 #pragma once
 #include "fsi_common.cuh"
+#include "store_acc.cuh"
 
 namespace fsi {
 
@@ -103,21 +104,19 @@ struct PairGeom {
     int sds[6], s[6], f[6], si[6], fi[6];
     int xDimS, xDimF, yDimS, yDimF, zDimS, zDimF;
 };
-// tau: the block's uniform tau, or per cell from tauA (tau_all) when non-null
-cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f,
-                                const PairGeom &p, int face, double *buf, double *buft, int *err,
-                                cudaStream_t st);
+// the face exchange of block refinement on any storage form `prec` (father
+// and son alike); tau per cell from TauSrc (store_acc.cuh)
+cudaError_t launch_pair_extract(const void *ff, int prec, int FX, int FY, int FZ, TauSrc tf, const PairGeom &p,
+                                int face, double *buf, double *buft, int *err, cudaStream_t st);
 cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaStream_t st);
 cudaError_t launch_fill_f64(double *p, long long n, double v, cudaStream_t st);
 cudaError_t launch_fill_f32(float *p, long long n, float v, cudaStream_t st);
-cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const double *tauA_s,
-                            const PairGeom &p, int face, const double *buf, const double *buft, int scheme,
-                            double *scratch_f, double *scratch_t, long long scratch_cells,
-                            const double vf[3], double dh, int *err, cudaStream_t st);
-cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f,
-                            const double *fs, int SX, int SY, int SZ, double tau_s, const double *tauA_s,
-                            const PairGeom &p, int face,
-                            const double vf[3], double dh, int *err, cudaStream_t st);
+cudaError_t launch_pair_f2s(void *fs, int prec, int SX, int SY, int SZ, TauSrc ts, const PairGeom &p, int face,
+                            const double *buf, const double *buft, int scheme, double *scratch_f, double *scratch_t,
+                            long long scratch_cells, const double vf[3], double dh, int *err, cudaStream_t st);
+cudaError_t launch_pair_s2f(void *ff, int prec, int FX, int FY, int FZ, TauSrc tf, const void *fs, int SX, int SY,
+                            int SZ, TauSrc ts, const PairGeom &p, int face, const double vf[3], double dh, int *err,
+                            cudaStream_t st);
 
 // ---- fast kernels (k_fast.cu): FP64 regrouped, FP32/FP16/BF16 storage ----
 cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st);

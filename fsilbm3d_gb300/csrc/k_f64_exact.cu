@@ -11,6 +11,7 @@
 #include "fsi_kernels.h"
 #include "bc_impl.cuh"
 #include "ib_impl.cuh"
+#include "store_acc.cuh"
 
 #include <math.h>
 
@@ -637,9 +638,9 @@ __device__ __forceinline__ void rec_err(int *err, int code, long long idx) {
 
 // extract_interpolate_layer for one son face (LBMBlockComm.f90:354-369):
 // buf(e, a, b) = father fIn on the face plane; buft = father tau
-__global__ void k_pair_extract(const double *__restrict__ ff, int FY, int FZ, long long NF, double tau_f,
-                               const double *__restrict__ tauA_f, PairGeom p, int face, double *buf, double *buft,
-                               int A, int B, int *err) {
+template <int P>
+__global__ void k_pair_extract(const void *__restrict__ ff, int FY, int FZ, long long NF, TauSrc tf, PairGeom p,
+                               int face, double *buf, double *buft, int A, int B, int *err) {
     int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (a >= A || b >= B) return;
     int ax = face >> 1, xF, yF, zF;
@@ -649,8 +650,8 @@ __global__ void k_pair_extract(const double *__restrict__ ff, int FY, int FZ, lo
     long long c = cidx(zF - 1, yF - 1, xF - 1, FZ, FY);
     long long o = (long long)a + (long long)A * b;
     if (c < 0 || c >= NF) { rec_err(err, 4, c); return; }
-    for (int e = 0; e < Q; e++) buf[e + Q * o] = ff[c + NF * e];
-    buft[o] = tauA_f ? tauA_f[c] : tau_f;
+    for (int e = 0; e < Q; e++) buf[e + Q * o] = FAcc<P>::load(ff, c + NF * e, e);
+    buft[o] = tf.at(c);
 }
 
 template <typename T>
@@ -753,8 +754,8 @@ __global__ void k_pair_interp(int nq, int bF, const double *__restrict__ fFp, lo
 }
 
 // interpolation_father_to_son apply step (LBMBlockComm.f90:685-693)
-__global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, double tau_s,
-                                 const double *__restrict__ tauA_s, PairGeom p, int face,
+template <int P>
+__global__ void k_pair_f2s_apply(void *fs, int SY, int SZ, long long NS, TauSrc ts, PairGeom p, int face,
                                  const double *tf, const double *tt, int AS, int BS, double vf0, double vf1,
                                  double vf2, double dh, int *err) {
     int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
@@ -766,17 +767,17 @@ __global__ void k_pair_f2s_apply(double *fs, int SY, int SZ, long long NS, doubl
     long long c = cidx(zS - 1, yS - 1, xS - 1, SZ, SY);
     long long o = (long long)a + (long long)AS * b;
     if (c < 0 || c >= NS) { rec_err(err, 3, c); return; }
-    double coeff = ((tauA_s ? tauA_s[c] : tau_s) / tt[o]) / 2.0;
+    double coeff = (ts.at(c) / tt[o]) / 2.0;
     double fin[Q], vf[3] = {vf0, vf1, vf2};
     for (int e = 0; e < Q; e++) fin[e] = tf[Q * o + e];
     grid_transform(fin, coeff, vf, dh);
-    for (int e = 0; e < Q; e++) fs[c + NS * e] = fin[e];
+    for (int e = 0; e < Q; e++) FAcc<P>::store(fs, c + NS * e, e, fin[e]);
 }
 
 // deliver_son_to_father for one face (LBMBlockComm.f90:555-570 and siblings)
-__global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_f, const double *__restrict__ tauA_f,
-                           const double *__restrict__ fs, int SY, int SZ, long long NS, double tau_s,
-                           const double *__restrict__ tauA_s, PairGeom p, int face, int n1, int n2,
+template <int P>
+__global__ void k_pair_s2f(void *ff, int FY, int FZ, long long NF, TauSrc tf, const void *__restrict__ fs, int SY,
+                           int SZ, long long NS, TauSrc ts, PairGeom p, int face, int n1, int n2,
                            double vf0, double vf1, double vf2, double dh, int *err) {
     int i1 = blockIdx.x * blockDim.x + threadIdx.x, i2 = blockIdx.y;
     if (i1 >= n2 || i2 >= n1) return;
@@ -791,11 +792,11 @@ __global__ void k_pair_s2f(double *ff, int FY, int FZ, long long NF, double tau_
     long long cf = cidx(F[2] - 1, F[1] - 1, F[0] - 1, FZ, FY);
     if (cs < 0 || cs >= NS) { rec_err(err, 5, cs); return; }
     if (cf < 0 || cf >= NF) { rec_err(err, 6, cf); return; }
-    double coeff = ((tauA_f ? tauA_f[cf] : tau_f) / (tauA_s ? tauA_s[cs] : tau_s)) * 2.0;
+    double coeff = (tf.at(cf) / ts.at(cs)) * 2.0;
     double t[Q], vf[3] = {vf0, vf1, vf2};
-    for (int e = 0; e < Q; e++) t[e] = fs[cs + NS * e];
+    for (int e = 0; e < Q; e++) t[e] = FAcc<P>::load(fs, cs + NS * e, e);
     grid_transform(t, coeff, vf, dh);
-    for (int e = 0; e < Q; e++) ff[cf + NF * e] = t[e];
+    for (int e = 0; e < Q; e++) FAcc<P>::store(ff, cf + NF * e, e, t[e]);
 }
 
 // check_is_continue's trilinear re-grid (FluidDomain.f90:170-226): each
@@ -994,14 +995,24 @@ cudaError_t launch_probes(const double *u, int X, int Y, int Z, double dh, doubl
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair_extract(const double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f,
-                                const PairGeom &p, int face, double *buf, double *buft, int *err, cudaStream_t st) {
+#define FSI_PAIR_DISPATCH(prec, ...)                                                      \
+    switch (prec) {                                                                       \
+    case FSI_PREC_F64: { constexpr int PP = FSI_PREC_F64; __VA_ARGS__; } break;           \
+    case FSI_PREC_F64_FAST: { constexpr int PP = FSI_PREC_F64_FAST; __VA_ARGS__; } break; \
+    case FSI_PREC_F32: { constexpr int PP = FSI_PREC_F32; __VA_ARGS__; } break;           \
+    case FSI_PREC_F16: { constexpr int PP = FSI_PREC_F16; __VA_ARGS__; } break;           \
+    case FSI_PREC_BF16: { constexpr int PP = FSI_PREC_BF16; __VA_ARGS__; } break;         \
+    default: return cudaErrorInvalidValue;                                                \
+    }
+
+cudaError_t launch_pair_extract(const void *ff, int prec, int FX, int FY, int FZ, TauSrc tf, const PairGeom &p,
+                                int face, double *buf, double *buft, int *err, cudaStream_t st) {
     int ax = face >> 1, A, B;
     if (ax == 0) { A = p.zDimF; B = p.yDimF; }
     else if (ax == 1) { A = p.zDimF; B = p.xDimF; }
     else { A = p.yDimF; B = p.xDimF; }
-    k_pair_extract<<<dim3((A + 63) / 64, B), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, tauA_f, p, face,
-                                                          buf, buft, A, B, err);
+    FSI_PAIR_DISPATCH(prec, k_pair_extract<PP><<<dim3((A + 63) / 64, B), 64, 0, st>>>(
+                                ff, FY, FZ, (long long)FX * FY * FZ, tf, p, face, buf, buft, A, B, err))
     return cudaGetLastError();
 }
 
@@ -1030,8 +1041,7 @@ cudaError_t launch_pair_average(double *b1, const double *b2, long long n, cudaS
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, const double *tauA_s, const PairGeom &p,
-                            int face,
+cudaError_t launch_pair_f2s(void *fs, int prec, int SX, int SY, int SZ, TauSrc ts, const PairGeom &p, int face,
                             const double *buf, const double *buft, int scheme, double *scratch_f, double *scratch_t,
                             long long scratch_cells, const double vf[3], double dh, int *err, cudaStream_t st) {
     int ax = face >> 1, AF, BF, AS, BS;
@@ -1042,25 +1052,24 @@ cudaError_t launch_pair_f2s(double *fs, int SX, int SY, int SZ, double tau_s, co
     if ((long long)AS * BS > scratch_cells) return cudaErrorInvalidValue;
     k_pair_interp<<<1, 32, 0, st>>>(Q, AF, buf, Q * nF, AS, BS, scratch_f, Q * scratch_cells, scheme, err);
     k_pair_interp<<<1, 32, 0, st>>>(1, AF, buft, nF, AS, BS, scratch_t, scratch_cells, 1, err);
-    k_pair_f2s_apply<<<dim3((AS + 63) / 64, BS), 64, 0, st>>>(fs, SY, SZ, (long long)SX * SY * SZ, tau_s, tauA_s, p,
-                                                              face,
-                                                              scratch_f, scratch_t, AS, BS, vf[0], vf[1], vf[2], dh,
-                                                              err);
+    FSI_PAIR_DISPATCH(prec, k_pair_f2s_apply<PP><<<dim3((AS + 63) / 64, BS), 64, 0, st>>>(
+                                fs, SY, SZ, (long long)SX * SY * SZ, ts, p, face, scratch_f, scratch_t, AS, BS, vf[0],
+                                vf[1], vf[2], dh, err))
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair_s2f(double *ff, int FX, int FY, int FZ, double tau_f, const double *tauA_f, const double *fs,
-                            int SX, int SY, int SZ, double tau_s, const double *tauA_s, const PairGeom &p, int face,
-                            const double vf[3], double dh, int *err, cudaStream_t st) {
+cudaError_t launch_pair_s2f(void *ff, int prec, int FX, int FY, int FZ, TauSrc tf, const void *fs, int SX, int SY,
+                            int SZ, TauSrc ts, const PairGeom &p, int face, const double vf[3], double dh, int *err,
+                            cudaStream_t st) {
     int ax = face >> 1;
     int o1 = (ax == 0) ? 1 : 0, o2 = (ax == 2) ? 1 : 2;
     // Fortran DO trip count of si(lo),si(hi),2: zero when hi < lo
     int n1 = (p.si[2 * o1 + 1] >= p.si[2 * o1]) ? (p.si[2 * o1 + 1] - p.si[2 * o1]) / 2 + 1 : 0;
     int n2 = (p.si[2 * o2 + 1] >= p.si[2 * o2]) ? (p.si[2 * o2 + 1] - p.si[2 * o2]) / 2 + 1 : 0;
     if (n1 <= 0 || n2 <= 0) return cudaSuccess;
-    k_pair_s2f<<<dim3((n2 + 63) / 64, n1), 64, 0, st>>>(ff, FY, FZ, (long long)FX * FY * FZ, tau_f, tauA_f, fs, SY,
-                                                         SZ, (long long)SX * SY * SZ, tau_s, tauA_s, p, face, n1, n2,
-                                                         vf[0], vf[1], vf[2], dh, err);
+    FSI_PAIR_DISPATCH(prec, k_pair_s2f<PP><<<dim3((n2 + 63) / 64, n1), 64, 0, st>>>(
+                                ff, FY, FZ, (long long)FX * FY * FZ, tf, fs, SY, SZ, (long long)SX * SY * SZ, ts, p, face,
+                                n1, n2, vf[0], vf[1], vf[2], dh, err))
     return cudaGetLastError();
 }
 

@@ -2022,6 +2022,10 @@ __device__ __forceinline__ void batch_prologue(const BatchCase *__restrict__ cas
         cta.sc.dh3 = 3.0f * (float)C.a.dh;
         for (int k = 0; k < 3; k++) cta.sc.vf[k] = (float)C.a.vf[k];
         cta.sc.forced = (C.a.vf[0] != 0.0 || C.a.vf[1] != 0.0 || C.a.vf[2] != 0.0) ? 1 : 0;
+        cta.sc.om2 = (float)C.a.omega2;
+        cta.sc.tau = (float)C.a.tau;
+        cta.sc.nu = (float)C.a.nu;
+        cta.sc.cles = (float)C.a.cles;
         cta.R = C.R;
         cta.tpr = C.tpr;
         const int jj = j - C.g0;
@@ -2054,6 +2058,10 @@ __global__ void __launch_bounds__(128) k_win_fix_batch(const BatchCase *__restri
     sc.om = (float)C.a.omega;
     sc.dh = (float)C.a.dh;
     sc.dh3 = 3.0f * (float)C.a.dh;
+    sc.om2 = (float)C.a.omega2;
+    sc.tau = (float)C.a.tau;
+    sc.nu = (float)C.a.nu;
+    sc.cles = (float)C.a.cles;
     MrtS ms;
 #pragma unroll
     for (int k = 0; k < Q; k++) ms.sd[k] = C.sd[k];
@@ -2166,20 +2174,27 @@ cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
 cudaError_t launch_batch_step(const BatchCase *d_cases, const int *d_gcase, int n, int G, int threads, long long wmax,
                               int prec, int model, bool forced, cudaStream_t st) {
     if (n <= 0 || G <= 0) return cudaSuccess;
-    if (model == 3) {
-        if (forced) {
-            FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, true>(d_cases, d_gcase, n, G, threads, wmax, st)))
-        }
-        FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 3, false>(d_cases, d_gcase, n, G, threads, wmax, st)))
+#define FSI_BATCH_MODEL(M)                                                                                      \
+    if (model == M) {                                                                                           \
+        if (forced) { FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, M, true>(d_cases, d_gcase, n, G, threads, wmax, st))) } \
+        FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, M, false>(d_cases, d_gcase, n, G, threads, wmax, st)))   \
     }
-    if (forced) { FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, true>(d_cases, d_gcase, n, G, threads, wmax, st))) }
-    FSI_DISPATCH_OFF(prec, return (batch_step_inst<PP, 1, false>(d_cases, d_gcase, n, G, threads, wmax, st)))
+    FSI_BATCH_MODEL(CM_MRT)
+    FSI_BATCH_MODEL(CM_TRT)
+    FSI_BATCH_MODEL(CM_SMAG)
+    FSI_BATCH_MODEL(CM_SRT)
+#undef FSI_BATCH_MODEL
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_batch_winfix(const BatchCase *d_cases, int n, long long wmax, int prec, int model, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (model == 3) { FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, 3>(d_cases, n, wmax, st))) }
-    FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, 1>(d_cases, n, wmax, st)))
+    switch (model) {
+    case CM_MRT: { FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, CM_MRT>(d_cases, n, wmax, st))) }
+    case CM_TRT: { FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, CM_TRT>(d_cases, n, wmax, st))) }
+    case CM_SMAG: { FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, CM_SMAG>(d_cases, n, wmax, st))) }
+    default: { FSI_DISPATCH_OFF(prec, return (batch_winfix_inst<PP, CM_SRT>(d_cases, n, wmax, st))) }
+    }
 }
 
 cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int Bmax, int prec, cudaStream_t st) {

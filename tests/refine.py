@@ -12,7 +12,7 @@ SON = dict(dims=(9, 7, 7), dh=0.5, origin=(6.0, 4.0, 4.0), bnd=(0, 0, 0, 0, 0, 0
 
 
 class TwoLevel:
-    def __init__(self, gpu=True, scheme=1, model=1, nu=0.02, uvwIn=(0.05, 0.0, 0.0)):
+    def __init__(self, gpu=True, scheme=1, model=1, nu=0.02, uvwIn=(0.05, 0.0, 0.0), precision=None):
         self.fl = O.make_flow(uvwIn=uvwIn, nu=nu, interpolateScheme=scheme)
         self.ofa = O.Block(*FATHER["dims"], FATHER["dh"], FATHER["origin"], list(FATHER["bnd"]), model, self.fl)
         self.oso = O.Block(*SON["dims"], SON["dh"], SON["origin"], list(SON["bnd"]), model, self.fl)
@@ -24,7 +24,8 @@ class TwoLevel:
             b.set_bc()
         if gpu:
             import fsilbm3d_gb300 as F
-            kw = dict(iCollidModel=model, nu=nu, precision=F.PREC_F64, uvwIn=uvwIn)
+            kw = dict(iCollidModel=model, nu=nu, precision=F.PREC_F64 if precision is None else precision,
+                      uvwIn=uvwIn)
             self.gfa = F.Block(*FATHER["dims"], dh=FATHER["dh"], origin=FATHER["origin"], bndConds=FATHER["bnd"],
                                m_collid=self._m(self.ofa, "mc", model), m_force=self._m(self.ofa, "mf", model), **kw)
             self.gso = F.Block(*SON["dims"], dh=SON["dh"], origin=SON["origin"], bndConds=SON["bnd"],

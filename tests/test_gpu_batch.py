@@ -18,7 +18,8 @@ def _blocks(prec, model, with_plates=False):
     blocks, plates = [], []
     for k, (dims, bnd) in enumerate(SHAPES):
         b = F.Block(*dims, bndConds=bnd, iCollidModel=model, nu=0.01 + 0.005 * k, precision=prec,
-                    uvwIn=(0.04, 0.005 * k, -0.002), shearRateIn=(0.0, 0.0, 0.001 * (k % 2)))
+                    uvwIn=(0.04, 0.005 * k, -0.002), shearRateIn=(0.0, 0.0, 0.001 * (k % 2)),
+                    params=(3.0 / 16.0,) if model == 2 else None)
         b.initialise(0.0)
         b.set_boundary_conditions(0.0)
         p = None
@@ -30,7 +31,7 @@ def _blocks(prec, model, with_plates=False):
     return blocks, plates
 
 
-@pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("model", [1, 2, 3, 11])
 @pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F16, F.PREC_BF16])
 def test_batch_fluid_equals_single(gpu_lib, prec, model):
     solo, _ = _blocks(prec, model)
@@ -43,6 +44,8 @@ def test_batch_fluid_equals_single(gpu_lib, prec, model):
     for a, b in zip(solo, grouped):
         fa, fb = a.download_f(), b.download_f()
         assert np.array_equal(fa.view(np.uint64), fb.view(np.uint64))
+        if model == 11:
+            assert np.array_equal(a.tau_all().view(np.uint64), b.tau_all().view(np.uint64))
 
 
 @pytest.mark.parametrize("threads", [128, 256, 512])
@@ -116,4 +119,8 @@ def test_batch_refusals(gpu_lib):
     assert e.value.code == F.FSI_E_ARG
     with pytest.raises(F.FsiError) as e:
         F.Batch([ok, ok])
+    assert e.value.code == F.FSI_E_ARG
+    v = F.Block(16, 12, 10, precision=F.PREC_F16, iCollidModel=15)
+    with pytest.raises(F.FsiError) as e:  # the gradient models step alone
+        F.Batch([v, F.Block(16, 12, 10, precision=F.PREC_F16, iCollidModel=15)])
     assert e.value.code == F.FSI_E_ARG

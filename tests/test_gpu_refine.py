@@ -1,6 +1,7 @@
 """Block refinement on the GPU (fsi_pair_*) against the oracle: a father with
 one son, bitwise in the exact FP64 form, both interpolation schemes, with a
-uniform and with a per-cell (LES) relaxation time."""
+uniform and with a per-cell (LES) relaxation time; the fast storage forms to
+their rounding."""
 import numpy as np
 import pytest
 
@@ -30,3 +31,26 @@ def test_two_level_bitwise(gpu_lib, scheme, model):
         if model in (11, 15):
             assert np.array_equal(bits(tl.ofa.tau_all.reshape(tl.gfa.dims)), bits(tl.gfa.tau_all()))
             assert np.array_equal(bits(tl.oso.tau_all.reshape(tl.gso.dims)), bits(tl.gso.tau_all()))
+
+
+@pytest.mark.parametrize("model", [1, 3, 11])
+@pytest.mark.parametrize("prec,tol", [("f64_fast", 1e-12), ("f32", 2e-6), ("f16", 2e-3), ("bf16", 2e-2)])
+def test_two_level_fast_forms(gpu_lib, model, prec, tol):
+    import fsilbm3d_gb300 as F
+    tl = TwoLevel(gpu=True, scheme=2, model=model, precision=F.PRECISIONS[prec])
+    rng = np.random.default_rng(5)
+    f = tl.ofa.fview()
+    f *= 1.0 + 1e-3 * (rng.random(f.shape) - 0.5)
+    tl.gfa.upload_f(f)
+    for s in range(3):
+        tl.step()
+    fo, fg = tl.ofa.fview(), tl.gfa.download_f()
+    so, sg = tl.oso.fview(), tl.gso.download_f()
+    assert np.max(np.abs(fg - fo)) <= tol * np.max(np.abs(fo))
+    assert np.max(np.abs(sg - so)) <= tol * np.max(np.abs(so))
+    if model == 11:
+        # tau_all (about 0.62 here, eddy part about 1e-5) to the resolution of
+        # the stored form: FP32 tau_all, non-equilibrium parts from FP16/BF16
+        ttol = {"f64_fast": 1e-12, "f32": 1e-6, "f16": 2e-5, "bf16": 2e-4}[prec]
+        ts = tl.gso.tau_all().reshape(-1)
+        assert np.max(np.abs(ts - tl.oso.tau_all.reshape(tl.gso.dims).reshape(-1))) <= ttol
