@@ -289,16 +289,24 @@ MODEL_NAMES = {1: "srt", 2: "trt", 3: "mrt", 11: "smag", 14: "wale", 15: "vrem"}
 TRT_LAMBDA = 3.0 / 16.0
 
 
-def model_bytes(model, s):
+def model_bytes(model, s, form):
     """algorithmic HBM bytes per cell update: the populations read and
-    written once, plus tau_all (Smagorinsky writes it, WALE reads and writes
-    it) and, for WALE and Vreman, the macro pass (populations read, den and u
-    written) and the step's read of the velocity field"""
+    written once, plus the per-cell-rate models' fields. FP64 exact form:
+    tau_all in FP64 (Smagorinsky writes it; WALE, Vreman write it after a
+    velocity pass that reads the populations and writes den and u, and a
+    step that reads the velocity field; WALE also reads tau_all). Fast forms
+    (FP32 fields): Smagorinsky writes tau_all; Vreman and WALE run a velocity
+    pass (populations in, u out), a gradient pass (u in; Vreman's tau_all or
+    WALE's three rotation entries out) and the step (Vreman reads tau_all;
+    WALE reads the rotation entries and tau_all and writes tau_all)"""
     B = 2 * 19 * s
+    f = 8 if form == "f64" else 4
     if model == 11:
-        B += 8
-    elif model in (14, 15):
+        B += f
+    elif model in (14, 15) and form == "f64":
         B += 19 * s + 32 + 24 + (16 if model == 14 else 8)
+    elif model in (14, 15):
+        B += 19 * s + 3 * f + 3 * f + (3 * f + 3 * f + 2 * f if model == 14 else f + f)
     return B
 
 
@@ -321,7 +329,7 @@ def tgv_forms(F, steps, pk, forms=("f64", "f64_fast", "f32", "f16", "bf16"), mod
             n = steps if name != "f64" else max(4, steps // 4)
             ms = b.run(n)
             den, uuu = b.calculate_macro_quantities()
-            B = model_bytes(model, b.store_bytes)
+            B = model_bytes(model, b.store_bytes, name)
             mlups = N * n / (ms * 1e-3) / 1e6
             r = {"mlups": round(mlups, 1), "ms_per_step": ms / n, "steps": n, "bytes_per_cell": B,
                  "algorithmic_gbs": round(mlups * B / 1e3, 1), "hbm_frac": round(mlups * B / 1e3 / pk, 4)}

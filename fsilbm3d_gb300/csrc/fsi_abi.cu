@@ -133,6 +133,7 @@ struct fsi_block {
     double *tau_all = nullptr;  // per-cell relaxation time of the LES models (N), FP64 forms
     float *tauf = nullptr;      // the same in FP32 for the offset storage forms
     float *uf = nullptr;        // FP32 velocity field of WALE / Vreman, offset storage forms (3N)
+    void *og = nullptr;         // WALE, fast forms: rotation-rate entries O12, O13, O23 (3N, arithmetic type)
     int periodic[3] = {0, 0, 0};
     MrtMats mm{};
     int prec = 0;
@@ -316,6 +317,7 @@ void fill_step(fsi_block *h, const double vf[3], double blktime, bool use_window
     a.tau_all = h->tau_all;
     a.tauf = h->tauf;
     a.uf = h->uf;
+    a.og = h->og;
     // z faces of code 101 with a face velocity uniform over the face: the
     // paired kernels write their equilibrium while streaming
     if (is_fast(h) && step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel)) {
@@ -351,8 +353,10 @@ int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_wind
     a.join = (void *)join;
     cudaError_t e = cudaSuccess;
     // only the paired kernels defer their IB-window work behind the join
-    // event; every other step waits for the IB stage before it starts
-    if (join && !(is_fast(h) && step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel))) {
+    // event; every other step, and the velocity pass of the gradient
+    // models, waits for the IB stage before it starts
+    if (join && (grad_model(h->d.iCollidModel) || !(is_fast(h) && step_fast_paired(a, &h->mm, h->prec,
+                                                                                    h->d.iCollidModel)))) {
         e = cudaStreamWaitEvent(h->st, join, 0);
         a.join = nullptr;
     }
@@ -382,7 +386,7 @@ void free_block(fsi_block *h) {
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
                     h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
-                    h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf};
+                    h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf, h->og};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -521,6 +525,8 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
             if (e == cudaSuccess) chk(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
         }
         if (grad_model(d->iCollidModel) && off) chk(cudaMalloc((void **)&h->uf, sizeof(float) * 3 * h->N));
+        if (d->iCollidModel == CM_WALE && h->prec != FSI_PREC_F64)
+            chk(cudaMalloc(&h->og, (off ? sizeof(float) : sizeof(double)) * 3 * h->N));
     }
     if (h->prec != FSI_PREC_F64 && h->prec != FSI_PREC_F64_FAST)
         chk(cudaMalloc((void **)&h->stage, sizeof(double) * 19 * (size_t)h->N));
@@ -1120,7 +1126,8 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     if (mode == FSI_IB_AUTO && wm.step && h->prec != FSI_PREC_F64_FAST) {
         StepArgs t;
         fill_step(h, wm.step_vf, wm.step_time, true, t);
-        mode = step_fast_paired(t, &h->mm, h->prec, h->d.iCollidModel) ? FSI_IB_OVERLAP : FSI_IB_GRID;
+        mode = (step_fast_paired(t, &h->mm, h->prec, h->d.iCollidModel) && !grad_model(h->d.iCollidModel))
+                   ? FSI_IB_OVERLAP : FSI_IB_GRID;
     }
     if (wm.step && (mode == FSI_IB_CLUSTER || mode == FSI_IB_OVERLAP) && !wm.mlp && !wm.features &&
         h->prec != FSI_PREC_F64_FAST) {

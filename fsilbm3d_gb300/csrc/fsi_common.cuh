@@ -153,6 +153,9 @@ struct StepArgs {
     // the offset storage forms keep that velocity field and tau_all in FP32
     // (uf: 3N, tauf: N) and use them instead of u and tau_all
     float *uf, *tauf;
+    // fast forms, WALE: the rotation-rate entries O12, O13, O23 of every cell
+    // (3N, the arithmetic type), written by the gradient pass before the step
+    void *og;
 };
 
 struct BcArgs {

@@ -295,6 +295,85 @@ template <typename C> __device__ __forceinline__ C pw15(C x) { return x * sqrt(x
 template <typename C> __device__ __forceinline__ C pw25(C x) { return (x * x) * sqrt(x); }
 template <typename C> __device__ __forceinline__ C pw125(C x) { return x * sqrt(sqrt(x)); }
 
+// WALE's relaxation time from S_ij (the strain rate of the non-equilibrium
+// stress) and O12, O13, O23 (FluidDomain.f90:1337-1413), the tensors scaled by
+// their largest entry before the products
+template <typename C>
+__device__ __forceinline__ C wale_tau(const Scal<C> &sc, C S11, C S22, C S33, C S12, C S13, C S23, C O12, C O13,
+                                      C O23) {
+    C g = fmax(fmax(fmax(fabs(S11), fabs(S22)), fmax(fabs(S33), fabs(S12))),
+               fmax(fmax(fabs(S13), fabs(S23)), fmax(fmax(fabs(O12), fabs(O13)), fabs(O23))));
+    C OP = C(0);
+    if (g > C(0)) {
+        const C ig = C(1) / g;
+        S11 *= ig; S22 *= ig; S33 *= ig; S12 *= ig; S13 *= ig; S23 *= ig;
+        O12 *= ig; O13 *= ig; O23 *= ig;
+        const C S = S11 * S11 + S22 * S22 + S33 * S33 + C(2) * (S12 * S12 + S13 * S13 + S23 * S23);
+        const C O = C(2) * (O12 * O12 + O23 * O23 + O13 * O13);
+        const C a12 = O12 * O12, a13 = O13 * O13, a23 = O23 * O23;
+        const C SO11 = -((S11 * S11 + S12 * S12 + S13 * S13) * (a12 + a13));
+        const C SO22 = -((S12 * S12 + S22 * S22 + S23 * S23) * (a12 + a23));
+        const C SO33 = -((S13 * S13 + S23 * S23 + S33 * S33) * (a13 + a23));
+        const C SO12 = -((S11 * S12 + S12 * S22 + S13 * S23) * (O13 * O23));
+        const C SO13 = (S11 * S13 + S12 * S23 + S13 * S33) * (O12 * O23);
+        const C SO23 = -((S12 * S13 + S22 * S23 + S23 * S33) * (O12 * O13));
+        const C SO = SO11 + SO22 + SO33 + C(2) * (SO12 + SO13 + SO23);
+        const C SdSd = (S * S + O * O) * C(1.0 / 6.0) + C(2.0 / 3.0) * S * O + C(2) * SO;
+        OP = g * (pw15(SdSd) / (pw25(S) + pw125(SdSd)));
+        if (!(OP >= C(0)) || !isfinite(OP)) OP = C(0);
+    }
+    return (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5);
+}
+
+// The gradient pass of the fast forms (after the velocity pass): Vreman's
+// relaxation time (vrem, FluidDomain.f90:1428-1506), or WALE's rotation-rate
+// entries (:1341-1391), from the neighbours' velocity, one thread per cell.
+template <int P, int MODEL>
+__global__ void __launch_bounds__(256) k_les_grad(StepArgs a, Scal<typename ST<P>::C> sc) {
+    using C = typename ST<P>::C;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
+    if (z >= a.Z) return;
+    const long long c = cidx(z, y, x, a.Z, a.Y);
+    if (MODEL == CM_WALE) {
+        const C ox = C(0.5) * (les_diff_c<P>(a, 2, 1, z, y, x, c, sc.dh) - les_diff_c<P>(a, 1, 2, z, y, x, c, sc.dh));
+        const C oy = C(0.5) * (les_diff_c<P>(a, 0, 2, z, y, x, c, sc.dh) - les_diff_c<P>(a, 2, 0, z, y, x, c, sc.dh));
+        const C oz = C(0.5) * (les_diff_c<P>(a, 1, 0, z, y, x, c, sc.dh) - les_diff_c<P>(a, 0, 1, z, y, x, c, sc.dh));
+        C *og = (C *)a.og;
+        og[c] = C(-0.5) * oz;
+        og[c + a.N] = C(0.5) * oy;
+        og[c + 2 * a.N] = C(-0.5) * ox;
+        return;
+    }
+    C m[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) m[i][j] = C(0.5) * les_diff_c<P>(a, i, j, z, y, x, c, sc.dh);
+    C g = C(0);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) g = fmax(g, fabs(m[i][j]));
+    C OP = C(0);
+    if (g > C(0)) {
+        const C ig = C(1) / g;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) m[i][j] *= ig;
+        const C r0 = m[0][0] * m[0][0] + m[0][1] * m[0][1] + m[0][2] * m[0][2];
+        const C r1 = m[1][0] * m[1][0] + m[1][1] * m[1][1] + m[1][2] * m[1][2];
+        const C r2 = m[2][0] * m[2][0] + m[2][1] * m[2][1] + m[2][2] * m[2][2];
+        const C d01 = m[0][0] * m[1][0] + m[0][1] * m[1][1] + m[0][2] * m[1][2];
+        const C d02 = m[0][0] * m[2][0] + m[0][1] * m[2][1] + m[0][2] * m[2][2];
+        const C d12 = m[1][0] * m[2][0] + m[1][1] * m[2][1] + m[1][2] * m[2][2];
+        const C bb = (r0 * r1 - d01 * d01) + (r0 * r2 - d02 * d02) + (r1 * r2 - d12 * d12);
+        OP = g * sqrt(bb / (r0 + r1 + r2));
+        if (!isfinite(OP)) OP = C(0);
+    }
+    tau_put<P>(a, c, (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5));
+}
+
 template <int P, int MODEL>
 __device__ __forceinline__ typename ST<P>::C les_rate_c(const StepArgs &a, const Scal<typename ST<P>::C> &sc,
                                                         const typename ST<P>::C neq[Q], typename ST<P>::C rho, int z,
@@ -312,62 +391,12 @@ __device__ __forceinline__ typename ST<P>::C les_rate_c(const StepArgs &a, const
         C q[6];
         neq_stress_c(neq, q);
         const C k = -(C(1.5) * sc.dh) / (rho * tau_get<P>(a, c));
-        C S11 = k * q[0], S22 = k * q[1], S33 = k * q[2], S12 = k * q[3], S13 = k * q[4], S23 = k * q[5];
-        C ox = C(0.5) * (les_diff_c<P>(a, 2, 1, z, y, x, c, sc.dh) - les_diff_c<P>(a, 1, 2, z, y, x, c, sc.dh));
-        C oy = C(0.5) * (les_diff_c<P>(a, 0, 2, z, y, x, c, sc.dh) - les_diff_c<P>(a, 2, 0, z, y, x, c, sc.dh));
-        C oz = C(0.5) * (les_diff_c<P>(a, 1, 0, z, y, x, c, sc.dh) - les_diff_c<P>(a, 0, 1, z, y, x, c, sc.dh));
-        C O12 = C(-0.5) * oz, O13 = C(0.5) * oy, O23 = C(-0.5) * ox;
-        C g = fmax(fmax(fmax(fabs(S11), fabs(S22)), fmax(fabs(S33), fabs(S12))),
-                   fmax(fmax(fabs(S13), fabs(S23)), fmax(fmax(fabs(O12), fabs(O13)), fabs(O23))));
-        C OP = C(0);
-        if (g > C(0)) {
-            const C ig = C(1) / g;
-            S11 *= ig; S22 *= ig; S33 *= ig; S12 *= ig; S13 *= ig; S23 *= ig;
-            O12 *= ig; O13 *= ig; O23 *= ig;
-            const C S = S11 * S11 + S22 * S22 + S33 * S33 + C(2) * (S12 * S12 + S13 * S13 + S23 * S23);
-            const C O = C(2) * (O12 * O12 + O23 * O23 + O13 * O13);
-            const C a12 = O12 * O12, a13 = O13 * O13, a23 = O23 * O23;
-            const C SO11 = -((S11 * S11 + S12 * S12 + S13 * S13) * (a12 + a13));
-            const C SO22 = -((S12 * S12 + S22 * S22 + S23 * S23) * (a12 + a23));
-            const C SO33 = -((S13 * S13 + S23 * S23 + S33 * S33) * (a13 + a23));
-            const C SO12 = -((S11 * S12 + S12 * S22 + S13 * S23) * (O13 * O23));
-            const C SO13 = (S11 * S13 + S12 * S23 + S13 * S33) * (O12 * O23);
-            const C SO23 = -((S12 * S13 + S22 * S23 + S23 * S33) * (O12 * O13));
-            const C SO = SO11 + SO22 + SO33 + C(2) * (SO12 + SO13 + SO23);
-            const C SdSd = (S * S + O * O) * C(1.0 / 6.0) + C(2.0 / 3.0) * S * O + C(2) * SO;
-            OP = g * (pw15(SdSd) / (pw25(S) + pw125(SdSd)));
-            if (!(OP >= C(0)) || !isfinite(OP)) OP = C(0);
-        }
-        t = (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5);
+        const C *og = (const C *)a.og;
+        t = wale_tau<C>(sc, k * q[0], k * q[1], k * q[2], k * q[3], k * q[4], k * q[5], og[c], og[c + a.N],
+                        og[c + 2 * a.N]);
     } else {
-        C m[3][3];
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-#pragma unroll
-            for (int i = 0; i < 3; i++) m[i][j] = C(0.5) * les_diff_c<P>(a, i, j, z, y, x, c, sc.dh);
-        C g = C(0);
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = 0; j < 3; j++) g = fmax(g, fabs(m[i][j]));
-        C OP = C(0);
-        if (g > C(0)) {
-            const C ig = C(1) / g;
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = 0; j < 3; j++) m[i][j] *= ig;
-            const C r0 = m[0][0] * m[0][0] + m[0][1] * m[0][1] + m[0][2] * m[0][2];
-            const C r1 = m[1][0] * m[1][0] + m[1][1] * m[1][1] + m[1][2] * m[1][2];
-            const C r2 = m[2][0] * m[2][0] + m[2][1] * m[2][1] + m[2][2] * m[2][2];
-            const C d01 = m[0][0] * m[1][0] + m[0][1] * m[1][1] + m[0][2] * m[1][2];
-            const C d02 = m[0][0] * m[2][0] + m[0][1] * m[2][1] + m[0][2] * m[2][2];
-            const C d12 = m[1][0] * m[2][0] + m[1][1] * m[2][1] + m[1][2] * m[2][2];
-            const C bb = (r0 * r1 - d01 * d01) + (r0 * r2 - d02 * d02) + (r1 * r2 - d12 * d12);
-            OP = g * sqrt(bb / (r0 + r1 + r2));
-            if (!isfinite(OP)) OP = C(0);
-        }
-        t = (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5);
+        // Vreman: the gradient pass wrote tau_all
+        return C(1) / tau_get<P>(a, c);
     }
     tau_put<P>(a, c, t);
     return C(1) / t;
@@ -739,10 +768,19 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
             FA = f2(0.f);
         }
     };
-    if (MODEL == CM_SMAG) {
-        // SRT with the Smagorinsky rate (FluidDomain.f90:1239-1242, smag
-        // :1265-1281). The stress sums Q_ab = sum e_a e_b fneq_i take the
-        // pair sums s = neq_i + neq_o only (fneq = -neq).
+    if (MODEL == CM_SMAG || MODEL == CM_VREM) {
+        // SRT with a per-cell rate (FluidDomain.f90:1239-1262). Smagorinsky
+        // (smag :1265-1281): the stress sums Q_ab = sum e_a e_b fneq_i take the
+        // pair sums s = neq_i + neq_o only (fneq = -neq); *tau_rel receives
+        // tau_all. Vreman: *tau_rel holds tau_all from the gradient pass.
+        float2 omv, cfv;
+        if (MODEL == CM_VREM) {
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                setl(omv, l, 1.0f / getl(*tau_rel, l));
+                setl(cfv, l, 1.0f - 0.5f * getl(omv, l));
+            }
+        } else {
         float2 q11 = f2(0.f), q22 = f2(0.f), q33 = f2(0.f), q12 = f2(0.f), q13 = f2(0.f), q23 = f2(0.f);
 #pragma unroll
         for (int k = 0; k < 9; k++) {
@@ -759,13 +797,13 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
         }
         const float2 qq = fma2(q11, q11, fma2(q22, q22, fma2(q33, q33, mul2(f2(2.0f), fma2(q12, q12, fma2(q13, q13,
                                                                                                    mul2(q23, q23)))))));
-        float2 omv, cfv;
 #pragma unroll
         for (int l = 0; l < 2; l++) {
             const float tau_t = sqrtf(sc.tau * sc.tau + sc.cles * sqrtf(getl(qq, l)) / getl(rho, l));
             setl(omv, l, 2.0f / (sc.tau + tau_t));
             setl(cfv, l, 1.0f - 0.5f * getl(omv, l));
             if (tau_rel) setl(*tau_rel, l, 0.5f * (sc.tau + tau_t));
+        }
         }
         const float2 feq0 = mul2(f2(w0), sub2(drho, mul2(rho, k15)));
         float2 n0 = fma2(omv, sub2(feq0, g[0]), g[0]);
@@ -991,11 +1029,13 @@ __device__ __forceinline__ void pair_body(const StepArgs &a, const Offs<int> &of
     if (MODEL == CM_SRT || MODEL == CM_TRT) {
         // SRT, TRT: stored pair by pair, so that the 64-register budget holds
         collide_emit<MODEL, FORCED, false>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit);
-    } else if (MODEL == CM_SMAG) {
-        // tau_all(z0, z0+1) with the populations (c is even: an aligned pair)
-        float2 tr;
+    } else if (MODEL == CM_SMAG || MODEL == CM_VREM) {
+        // tau_all(z0, z0+1) with the populations (c is even: an aligned pair);
+        // Smagorinsky writes it, Vreman reads what the gradient pass wrote
+        float2 tr = f2(sc.tau);
+        if (MODEL == CM_VREM && active) tr = *(const float2 *)(a.tauf + c);
         collide_emit<MODEL, FORCED, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit, &tr);
-        if (active) *(float2 *)(a.tauf + c) = tr;
+        if (MODEL == CM_SMAG && active) *(float2 *)(a.tauf + c) = tr;
     } else {
         // MRT: all 19 collided first, then stored under one branch
         collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
@@ -1298,7 +1338,12 @@ __device__ __forceinline__ void win_fix_body(const StepArgs &a, const Scal<float
         setl(F1, l, (float)__ldcg(w.force + wc + w.n));
         setl(F2, l, (float)__ldcg(w.force + wc + 2 * w.n));
     }
-    float2 tr;
+    float2 tr = f2(sc.tau);
+    if (MODEL == CM_VREM) {
+#pragma unroll
+        for (int l = 0; l < 2; l++)
+            setl(tr, l, a.tauf[(long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l])]);
+    }
     collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, &tr);
     push_cell<P>(a, x[0], y[0], z[0], g, 0);
     if (two) push_cell<P>(a, x[1], y[1], z[1], g, 1);
@@ -1375,7 +1420,13 @@ __global__ void __launch_bounds__(128) k_face_hook(StepArgs a, Scal<float> sc, M
         }
         return;
     }
-    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
+    float2 tr = f2(sc.tau);
+    if (MODEL == CM_VREM) {
+#pragma unroll
+        for (int l = 0; l < 2; l++)
+            setl(tr, l, a.tauf[(long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l])]);
+    }
+    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, MODEL == CM_VREM ? &tr : nullptr);
 #pragma unroll
     for (int l = 0; l < 2; l++) {
         if (l == 1 && !two) break;
@@ -2131,7 +2182,8 @@ cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
     return prec != FSI_PREC_F64_FAST &&
-           (model == CM_SRT || model == CM_TRT || model == CM_SMAG || (model == CM_MRT && mm->diag)) && small &&
+           (model == CM_SRT || model == CM_TRT || model == CM_SMAG || model == CM_VREM ||
+            (model == CM_MRT && mm->diag)) && small &&
            a.Z % 2 == 0 && a.Z <= 512;
 }
 
@@ -2154,7 +2206,11 @@ cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st)
         Scal<CC> sc{};
         sc.dh = (CC)a.dh;
         for (int k = 0; k < 3; k++) sc.vf[k] = (CC)a.vf[k];
+        sc.nu = (CC)a.nu;
+        sc.cles = (CC)a.cles;
         k_step_macro_fast<PP><<<g, bz, 0, st>>>(a, sc);
+        if (a.og) k_les_grad<PP, CM_WALE><<<g, bz, 0, st>>>(a, sc);
+        else k_les_grad<PP, CM_VREM><<<g, bz, 0, st>>>(a, sc);
         return cudaGetLastError();
     })
 }
