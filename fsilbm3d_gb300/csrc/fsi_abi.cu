@@ -23,6 +23,14 @@ using namespace fsi;
 static_assert(FSI_MLP_IN == MLP_IN && FSI_MLP_OUT == MLP_OUT, "perceptron shape");
 static_assert(FSI_MLP_NPARAM == MLP_NP && FSI_MLP_NNORM == MLP_NNORM, "perceptron sizes");
 
+// CTAs of the IB stage when it runs beside the bulk step: at least this many,
+// about a sixth of the one-warp-per-marker grid (every IB CTA takes registers
+// from the bulk step on its SM; measured on the 33x33-marker headline plate:
+// 0.496 ms/step uncapped, 0.482 at 24 CTAs, 0.485 at 48, 0.488 at 80)
+#ifndef FSI_IB_OVERLAP_CTAS
+#define FSI_IB_OVERLAP_CTAS 24
+#endif
+
 namespace {
 
 thread_local std::string g_err;
@@ -1144,9 +1152,10 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         CK(cudaEventRecord(h->ev_fork, h->st));
         CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
         if (mode == FSI_IB_OVERLAP) {
+            // beside the bulk step the IB stage takes SM room from it: cap its grid
             long long need = std::max<long long>((h->Mtot + 7) / 8, (h->Nw + 255) / 256);
-            CK(launch_ib_coop(a, h->prec, (int)std::max<long long>(1, std::min<long long>(need, h->coop_grid)),
-                              h->st2));
+            long long cap = std::min<long long>(h->coop_grid, std::max<long long>(FSI_IB_OVERLAP_CTAS, need / 6));
+            CK(launch_ib_coop(a, h->prec, (int)std::max<long long>(1, std::min<long long>(need, cap)), h->st2));
         } else {
             CK(launch_ib_cluster(a, h->prec, h->st2));
         }
