@@ -225,9 +225,14 @@ def fsi_steps(b, plate, dh, t, n, forces=None):
 
 
 def n_face_kernels():
-    """face kernels per step: every non-periodic face, except z faces of code
-    101 with a uniform face velocity, which the paired bulk kernel writes"""
-    return sum(1 for k, c in enumerate(BND) if c not in (0, 1, 301) and not (k >= 4 and c == 101))
+    """face-kernel launches per headline step: every non-periodic face, except
+    z faces of code 101 with a uniform face velocity, which the paired bulk
+    kernel writes; the two faces of an axis share one launch"""
+    n = 0
+    for ax in range(3):
+        on = [c not in (0, 1, 301) and not (ax == 2 and c == 101) for c in BND[2 * ax:2 * ax + 2]]
+        n += 1 if all(on) and FSI_GRID[ax] >= 6 else sum(on)
+    return n
 
 
 def cpu_fsi_sample(threads, nsteps=None, seconds=12.0):

@@ -281,11 +281,24 @@ bool fill_bc(fsi_block *h, int k, void *f, double blktime, const int zdone[2], B
 }
 
 int apply_bcs(fsi_block *h, void *f, double blktime, const int zdone[2] = nullptr) {
-    for (int k = 0; k < 6; k++) {
-        BcArgs a;
-        if (!fill_bc(h, k, f, blktime, zdone, a)) continue;
-        cudaError_t e = is_fast(h) ? launch_bc_fast(a, h->prec, h->st) : launch_bc_f64(a, h->st);
-        if (e != cudaSuccess) return fail(FSI_E_CUDA, "boundary kernel: %s", cudaGetErrorString(e));
+    const bool off = h->prec == FSI_PREC_F32 || h->prec == FSI_PREC_F16 || h->prec == FSI_PREC_BF16;
+    for (int ax = 0; ax < 3; ax++) {
+        BcArgs a[2];
+        bool on[2];
+        for (int s = 0; s < 2; s++) on[s] = fill_bc(h, 2 * ax + s, f, blktime, zdone, a[s]);
+        // the two faces of an axis in one launch when each reads and writes
+        // only its own three layers and the axis keeps them apart
+        const int D = ax == 0 ? h->X : (ax == 1 ? h->Y : h->Z);
+        if (off && on[0] && on[1] && D >= 6) {
+            cudaError_t e = launch_bc_pair_fast(a[0], a[1], h->prec, h->st);
+            if (e != cudaSuccess) return fail(FSI_E_CUDA, "boundary kernel: %s", cudaGetErrorString(e));
+            continue;
+        }
+        for (int s = 0; s < 2; s++) {
+            if (!on[s]) continue;
+            cudaError_t e = is_fast(h) ? launch_bc_fast(a[s], h->prec, h->st) : launch_bc_f64(a[s], h->st);
+            if (e != cudaSuccess) return fail(FSI_E_CUDA, "boundary kernel: %s", cudaGetErrorString(e));
+        }
     }
     return FSI_OK;
 }

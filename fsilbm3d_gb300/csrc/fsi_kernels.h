@@ -123,6 +123,9 @@ cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int
 // true when launch_step_fast runs the paired kernels (which can write 101 z faces)
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model);
 cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st);
+// both faces of one axis in one launch (offset forms; faces that share no cell
+// they read or write)
+cudaError_t launch_bc_pair_fast(const BcArgs &lo, const BcArgs &hi, int prec, cudaStream_t st);
 cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st);
 cudaError_t launch_convert_from_store(const void *fs, double *f64, long long N, int prec, cudaStream_t st);
 cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, int X, int Y, int Z, double dh,

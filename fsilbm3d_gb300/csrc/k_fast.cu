@@ -2029,6 +2029,16 @@ __global__ void __launch_bounds__(256) k_bc_off(BcArgs a) {
     bc_off_body<P, FACE>(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
 
+// the two faces of one axis in one launch (blockIdx.z: 0 the low face, 1 the
+// high one); the host pairs them only when the axis is long enough that
+// neither face reads a cell the other writes
+template <int P, int AX>
+__global__ void __launch_bounds__(256) k_bc_off_pair(BcArgs lo, BcArgs hi) {
+    const int fa = blockIdx.x * blockDim.x + threadIdx.x, fb = blockIdx.y * blockDim.y + threadIdx.y;
+    if (blockIdx.z == 0) bc_off_body<P, 2 * AX>(lo, fa, fb);
+    else bc_off_body<P, 2 * AX + 1>(hi, fa, fb);
+}
+
 // face FACE of many blocks, blockIdx.z = block (code BC_FLUID: nothing to do)
 template <int P, int FACE>
 __global__ void __launch_bounds__(256) k_bc_off_batch(const BcArgs *__restrict__ bcs, int n) {
@@ -2219,6 +2229,7 @@ cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
     FSI_DISPATCH(prec, return bc_inst<PP>(a, st))
 }
 
+
 #define FSI_DISPATCH_OFF(prec, ...)                                          \
     switch (prec) {                                                          \
     case FSI_PREC_F32: { constexpr int PP = FSI_PREC_F32; __VA_ARGS__; }     \
@@ -2226,6 +2237,23 @@ cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
     case FSI_PREC_BF16: { constexpr int PP = FSI_PREC_BF16; __VA_ARGS__; }   \
     default: return cudaErrorInvalidValue;                                   \
     }
+
+cudaError_t launch_bc_pair_fast(const BcArgs &lo, const BcArgs &hi, int prec, cudaStream_t st) {
+    const int ax = lo.face >> 1;
+    const int A = (ax < 2) ? lo.Z : lo.Y;
+    const int B = (ax == 0) ? lo.Y : lo.X;
+    dim3 blk(64, 4), grd((A + 63) / 64, (B + 3) / 4, 2);
+    switch (prec) {
+    case FSI_PREC_F32: case FSI_PREC_F16: case FSI_PREC_BF16: break;
+    default: return cudaErrorInvalidValue;
+    }
+    FSI_DISPATCH_OFF(prec, {
+        if (ax == 0) k_bc_off_pair<PP, 0><<<grd, blk, 0, st>>>(lo, hi);
+        else if (ax == 1) k_bc_off_pair<PP, 1><<<grd, blk, 0, st>>>(lo, hi);
+        else k_bc_off_pair<PP, 2><<<grd, blk, 0, st>>>(lo, hi);
+        return cudaGetLastError();
+    })
+}
 
 cudaError_t launch_batch_step(const BatchCase *d_cases, const int *d_gcase, int n, int G, int threads, long long wmax,
                               int prec, int model, bool forced, cudaStream_t st) {
