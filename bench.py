@@ -761,7 +761,9 @@ def main_reference(a, rank, world, dist):
     line = {"impl": "reference", "metric": METRIC, "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": world,
             "steps": n, "warmup": 1, "ms_per_step": el / n * 1e3, "higher_is_better": True,
             "dtype": "f64", "data": "synthetic (uniform inflow initial field, prescribed plate kinematics)",
-            "config": {"workload": WORKLOAD, "grid": list(FSI_GRID)},
+            "config": {"workload": WORKLOAD, "grid": list(FSI_GRID), "collision": "MRT", "storage": "fp64 f",
+                       "markers": FSI_NODES * FSI_NODES, "ib": "ntol=%d dtol=%g" % (NTOL, DTOL),
+                       "parallelism": "host cores (rank 0)"},
             "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": thr, "kind": "port",
                              "sample": "%d reference steps (FP64 MRT + IB) of the headline workload (%.1f s)" % (n, el)},
             "e2e": {"value": round(mlups, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
