@@ -953,6 +953,13 @@ __device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, f
 // resident CTAs per SM the paired bulk kernel is compiled for (its register
 // budget), measured best on GB300: SRT 4 x 256 threads (<= 64 registers);
 // MRT unforced FP16/BF16 3 (<= 85, a little spill), MRT forced or FP32 2
+// threads per CTA of the paired bulk kernel (whole z-rows: at least Z/2).
+// Measured on GB300 (FP16, 256^3 TGV): 128-thread CTAs beat 256-thread ones
+// (MRT 58.7k -> 63.1k MLUPS, SRT 74.7k -> 76.0k): the z-shift barrier stalls
+// fewer warps at a time.
+#ifndef FSI_PAIR_THREADS
+#define FSI_PAIR_THREADS 128
+#endif
 #ifndef FSI_PAIR_MINB_SRT
 #define FSI_PAIR_MINB_SRT 4
 #endif
@@ -967,6 +974,19 @@ constexpr int pair_minb() {
     return (MODEL == CM_SRT || MODEL == CM_TRT)
                ? FSI_PAIR_MINB_SRT
                : ((FORCED || P == FSI_PREC_F32) ? FSI_PAIR_MINB_MRT_FORCED : FSI_PAIR_MINB_MRT);
+}
+// the same budgets for CTAs of FSI_PAIR_THREADS (the single-block kernel);
+// MRT unforced FP16/BF16 at 128 threads: 5 CTAs (up to 102 registers) beat 6
+// (85, spilling) and 4 (128): 256^3 TGV FP16 63.9k / 62.8k / 57.9k MLUPS
+#ifndef FSI_PAIR_CTAS_MRT
+#define FSI_PAIR_CTAS_MRT (FSI_PAIR_THREADS == 128 ? 5 : FSI_PAIR_MINB_MRT * 256 / FSI_PAIR_THREADS)
+#endif
+template <int P, int MODEL, bool FORCED, int T>
+constexpr int pair_ctas() {
+    return T != FSI_PAIR_THREADS ? pair_minb<P, MODEL, FORCED>() * 256 / T
+           : (MODEL != CM_SRT && MODEL != CM_TRT && !FORCED && P != FSI_PREC_F32)
+               ? FSI_PAIR_CTAS_MRT
+               : pair_minb<P, MODEL, FORCED>() * 256 / T;
 }
 
 // The bulk step: every cell takes den/u from its own distributions and the
@@ -1069,8 +1089,10 @@ __device__ __forceinline__ void pair_body(const StepArgs &a, const Offs<int> &of
 }
 
 
-template <int P, int MODEL, bool FORCED>
-__global__ void __launch_bounds__(256, pair_minb<P, MODEL, FORCED>())
+// T: the CTA size it is compiled for (FSI_PAIR_THREADS, or 256 for rows
+// longer than FSI_PAIR_THREADS pairs)
+template <int P, int MODEL, bool FORCED, int T>
+__global__ void __launch_bounds__(T, pair_ctas<P, MODEL, FORCED, T>())
 k_step_pair(StepArgs a, Offs<int> of, Scal<float> sc, MrtS ms) {
     extern __shared__ unsigned char smraw[];
     const int R = blockDim.y;
@@ -1460,7 +1482,9 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
     if (MODEL == 3)
         for (int k = 0; k < Q; k++) ms.sd[k] = (float)mm->sd[k];
     const int tpr = a.Z / 2;
-    const int R = std::max(1, 256 / tpr);
+    // rows of more than FSI_PAIR_THREADS pairs take the 256-thread build
+    const bool big = tpr > FSI_PAIR_THREADS;
+    const int R = std::max(1, (big ? 256 : FSI_PAIR_THREADS) / tpr);
     dim3 blk(tpr, R), grd(1, (a.Y + R - 1) / R, a.X);
     size_t smem = (size_t)10 * R * a.Z * sizeof(typename V2<P>::S);
     // the pipelined persistent form (on request, SRT and MRT; it needs
@@ -1473,9 +1497,11 @@ cudaError_t pair_launch(const StepArgs &a, const MrtMats *mm, bool hooks, cudaSt
             if (e != cudaSuccess) return e;
         }
     } else if (sc.forced) {
-        k_step_pair<P, MODEL, true><<<grd, blk, smem, st>>>(a, of, sc, ms);
+        if (big) k_step_pair<P, MODEL, true, 256><<<grd, blk, smem, st>>>(a, of, sc, ms);
+        else k_step_pair<P, MODEL, true, FSI_PAIR_THREADS><<<grd, blk, smem, st>>>(a, of, sc, ms);
     } else {
-        k_step_pair<P, MODEL, false><<<grd, blk, smem, st>>>(a, of, sc, ms);
+        if (big) k_step_pair<P, MODEL, false, 256><<<grd, blk, smem, st>>>(a, of, sc, ms);
+        else k_step_pair<P, MODEL, false, FSI_PAIR_THREADS><<<grd, blk, smem, st>>>(a, of, sc, ms);
     }
     // what needs the IB stage's window waits for it
     if (a.join) {
