@@ -1891,6 +1891,8 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
         fill_step(h, z3, 0.0, false, a);
         if (!step_fast_paired(a, &h->mm, h->prec, h->d.iCollidModel) || h->Z / 2 > 512)
             return fail(FSI_E_ARG, "block %d: needs the paired kernels (even zDim <= 1024, diagonal MRT)", c);
+        if ((unsigned long long)19 * h->N * h->esz >= (1ULL << 32))
+            return fail(FSI_E_ARG, "block %d: a batched block's distributions must span less than 4 GiB", c);
         for (int k = 0; k < 6; k++) {
             const int code = h->d.bndConds[k];
             if (code == BC_NEQ || code == BC_WALL_HW || code == BC_MWALL_HW || code == BC_FLUID ||
