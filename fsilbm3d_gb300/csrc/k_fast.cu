@@ -459,10 +459,18 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
     const long long N = a.N;
     const IT c = (IT)z + (IT)Z * ((IT)y + (IT)Y * (IT)x);
     const S *__restrict__ sp = (const S *)a.src + c;
+    // IT = int: the buffer spans less than 4 GiB and every access is a 32-bit
+    // byte offset from its base (as in the paired kernel)
+    constexpr bool U32 = sizeof(IT) == 4;
 
     C g[Q];
 #pragma unroll
-    for (int i = 0; i < Q; i++) g[i] = T::dec(__ldcs(sp + of.ld[i]));
+    for (int i = 0; i < Q; i++) {
+        if constexpr (U32)
+            g[i] = T::dec(__ldcs((const S *)((const char *)a.src + (unsigned)(c + of.ld[i]) * (unsigned)sizeof(S))));
+        else
+            g[i] = T::dec(__ldcs(sp + of.ld[i]));
+    }
 
     C rho, drho, u0, u1, u2, F0 = C(0), F1 = C(0), F2 = C(0);
     bool forced = false;
@@ -522,7 +530,10 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const IT corr = wrap_corr(ez_(i), czp, czm) + wrap_corr(ey_(i), cyp, cym) + wrap_corr(ex_(i), cxp, cxm);
-        __stcs((dp + corr) + of.st[i], T::enc(g[i]));
+        if constexpr (U32)
+            __stcs((S *)((char *)a.dst + (unsigned)(c + corr + of.st[i]) * (unsigned)sizeof(S)), T::enc(g[i]));
+        else
+            __stcs((dp + corr) + of.st[i], T::enc(g[i]));
     }
 }
 
@@ -1958,8 +1969,8 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     // and non-equilibrium extrapolation faces
     bool hooks = a.win.x1 >= a.win.x0;
     for (int k = 0; k < 6; k++) hooks = hooks || a.hw[k] != nullptr || a.l2[k] != 0;
-    // 32-bit element indices while all 19 populations fit
-    const bool small = (long long)Q * a.N < (1LL << 31) - 1;
+    // 32-bit byte offsets while all 19 populations span less than 4 GiB
+    const bool small = (unsigned long long)Q * a.N * sizeof(typename ST<P>::S) < (1ULL << 32);
     if (step_fast_paired(a, mm, P, MODEL))
         return pair_launch<P == FSI_PREC_F64_FAST ? FSI_PREC_F32 : P, MODEL>(a, mm, hooks, st);
     if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
