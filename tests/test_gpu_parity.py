@@ -383,3 +383,29 @@ def test_ib_step_equals_solve_then_step(gpu_lib, prec, tol, mode):
         assert np.max(np.abs(e1 - e0)) <= tol * np.max(np.abs(e0))
     f0, f1 = blocks[0].download_f(), blocks[1].download_f()
     assert np.max(np.abs(f1 - f0)) <= tol * np.max(np.abs(f0))
+
+
+def test_large_buffer_paths_match_small(gpu_lib):
+    # an FP32 block whose distributions span more than 4 GiB takes the 64-bit
+    # addressing of the paired kernel; a periodic state tiled 2x2x2 from a
+    # small block (32-bit offsets) must evolve bitwise like the small one
+    small = (192, 192, 192)
+    fs = Case(small, model=3, nu=0.02, precision=F.PREC_F32)
+    fs.init_tgv(0.05)
+    f0 = fs.ob.fview().copy()
+    big = tuple(2 * n for n in small)
+    bb = F.Block(*big, iCollidModel=3, nu=0.02, precision=F.PREC_F32)
+    assert 19 * bb.N * 4 >= 1 << 32
+    bb.upload_f(np.tile(f0, (1, 2, 2, 2)))
+    for s in range(2):
+        fs.gb.step(blktime=s + 1.0)
+        bb.step(blktime=s + 1.0)
+    a = fs.gb.download_f()
+    b = bb.download_f()
+    X, Y, Z = small
+    for tx in range(2):
+        for ty in range(2):
+            for tz in range(2):
+                blk = b[:, tx * X:(tx + 1) * X, ty * Y:(ty + 1) * Y, tz * Z:(tz + 1) * Z]
+                assert np.array_equal(blk.view(np.uint64), a.view(np.uint64)), (tx, ty, tz)
+    bb.close()
