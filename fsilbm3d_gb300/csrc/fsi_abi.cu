@@ -139,7 +139,8 @@ struct fsi_block {
     double omega2 = 0;          // TRT antisymmetric rate
     double cles = 0;            // constant of the LES model (ConstParams.f90:40-45)
     double *tau_all = nullptr;  // per-cell relaxation time of the LES models (N), FP64 forms
-    float *tauf = nullptr;      // the same in FP32 for the offset storage forms
+    float *tauf = nullptr;      // the same in FP32 for the offset storage forms (current)
+    float *tauf2 = nullptr;     // WALE, offset forms: the other buffer (the step reads one, writes the other)
     float *uf = nullptr;        // FP32 velocity field of WALE / Vreman, offset storage forms (3N)
     void *og = nullptr;         // WALE, fast forms: rotation-rate entries O12, O13, O23 (3N, arithmetic type)
     int periodic[3] = {0, 0, 0};
@@ -336,7 +337,10 @@ void fill_step(fsi_block *h, const double vf[3], double blktime, bool use_window
     a.nu = h->d.nu;
     a.cles = h->cles;
     a.tau_all = h->tau_all;
-    a.tauf = h->tauf;
+    // WALE in the offset forms reads the current tau_all and writes the other
+    // buffer (swapped with the distributions after the step)
+    a.tauf = h->tauf2 ? h->tauf2 : h->tauf;
+    a.tauf_prev = h->tauf;
     a.uf = h->uf;
     a.og = h->og;
     // z faces of code 101 with a face velocity uniform over the face: the
@@ -390,6 +394,7 @@ int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_wind
     int rc = apply_bcs(h, h->fb, blktime, a.zeq);
     if (rc) return rc;
     std::swap(h->fa, h->fb);
+    if (h->tauf2) std::swap(h->tauf, h->tauf2);
     return FSI_OK;
 }
 
@@ -407,7 +412,7 @@ void free_block(fsi_block *h) {
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
                     h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
-                    h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf, h->og};
+                    h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf, h->og, h->tauf2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -541,6 +546,10 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
         if (les_model(d->iCollidModel) && off) {
             chk(cudaMalloc((void **)&h->tauf, sizeof(float) * h->N));
             if (e == cudaSuccess) chk(launch_fill_f32(h->tauf, h->N, (float)h->tau, h->st));
+            if (d->iCollidModel == CM_WALE) {
+                chk(cudaMalloc((void **)&h->tauf2, sizeof(float) * h->N));
+                if (e == cudaSuccess) chk(launch_fill_f32(h->tauf2, h->N, (float)h->tau, h->st));
+            }
         } else if (les_model(d->iCollidModel)) {
             chk(cudaMalloc((void **)&h->tau_all, sizeof(double) * h->N));
             if (e == cudaSuccess) chk(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
@@ -864,6 +873,7 @@ int fsi_block_initialise(fsi_block_t h, double time) {
     // calculate_SRT_params (FluidDomain.f90:450-456) resets tau_all
     if (h->tau_all) CK(launch_fill_f64(h->tau_all, h->N, h->tau, h->st));
     if (h->tauf) CK(launch_fill_f32(h->tauf, h->N, (float)h->tau, h->st));
+    if (h->tauf2) CK(launch_fill_f32(h->tauf2, h->N, (float)h->tau, h->st));
     CK(cudaStreamSynchronize(h->st));
     return FSI_OK;
 }

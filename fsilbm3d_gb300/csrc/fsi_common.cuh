@@ -156,6 +156,9 @@ struct StepArgs {
     // fast forms, WALE: the rotation-rate entries O12, O13, O23 of every cell
     // (3N, the arithmetic type), written by the gradient pass before the step
     void *og;
+    // offset forms: the tau_all the step reads (WALE reads the previous
+    // step's and writes tauf; the others read and write the same array)
+    float *tauf_prev;
 };
 
 struct BcArgs {

@@ -269,7 +269,7 @@ template <int P> __device__ __forceinline__ typename ST<P>::C uval(const StepArg
     else return (typename ST<P>::C)a.u[i];
 }
 template <int P> __device__ __forceinline__ typename ST<P>::C tau_get(const StepArgs &a, long long c) {
-    if (ST<P>::OFF) return a.tauf[c];
+    if (ST<P>::OFF) return a.tauf_prev[c];
     else return (typename ST<P>::C)a.tau_all[c];
 }
 template <int P> __device__ __forceinline__ void tau_put(const StepArgs &a, long long c, typename ST<P>::C v) {
@@ -756,7 +756,8 @@ __device__ __forceinline__ void mrt_backward(const float2 t[Q], float2 &E0, floa
 template <int MODEL, bool FORCED, bool KEEPG, class EMIT>
 __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1,
                                              float2 u2, float2 F0, float2 F1, float2 F2, const Scal<float> &sc,
-                                             const MrtS &ms, EMIT &&emit, float2 *tau_rel = nullptr) {
+                                             const MrtS &ms, EMIT &&emit, float2 *tau_rel = nullptr,
+                                             const float2 *les_in = nullptr) {
     const float om = sc.om;
     const float2 k15 = mul2(f2(1.5f), fma2(u0, u0, fma2(u1, u1, mul2(u2, u2))));
     float2 uF = f2(0.f);
@@ -779,11 +780,14 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
             FA = f2(0.f);
         }
     };
-    if (MODEL == CM_SMAG || MODEL == CM_VREM) {
+    if (MODEL == CM_SMAG || MODEL == CM_VREM || MODEL == CM_WALE) {
         // SRT with a per-cell rate (FluidDomain.f90:1239-1262). Smagorinsky
         // (smag :1265-1281): the stress sums Q_ab = sum e_a e_b fneq_i take the
         // pair sums s = neq_i + neq_o only (fneq = -neq); *tau_rel receives
         // tau_all. Vreman: *tau_rel holds tau_all from the gradient pass.
+        // WALE: the same stress sums give S_ij with the previous tau_all
+        // (les_in[0]) and les_in[1..3] hold O12, O13, O23; *tau_rel receives
+        // tau_all.
         float2 omv, cfv;
         if (MODEL == CM_VREM) {
 #pragma unroll
@@ -808,12 +812,25 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
         }
         const float2 qq = fma2(q11, q11, fma2(q22, q22, fma2(q33, q33, mul2(f2(2.0f), fma2(q12, q12, fma2(q13, q13,
                                                                                                    mul2(q23, q23)))))));
+        if (MODEL == CM_WALE) {
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                const float k = -(1.5f * sc.dh) / (getl(rho, l) * getl(les_in[0], l));
+                const float t = wale_tau<float>(sc, k * getl(q11, l), k * getl(q22, l), k * getl(q33, l),
+                                                k * getl(q12, l), k * getl(q13, l), k * getl(q23, l),
+                                                getl(les_in[1], l), getl(les_in[2], l), getl(les_in[3], l));
+                setl(omv, l, 1.0f / t);
+                setl(cfv, l, 1.0f - 0.5f * getl(omv, l));
+                if (tau_rel) setl(*tau_rel, l, t);
+            }
+        } else {
 #pragma unroll
         for (int l = 0; l < 2; l++) {
             const float tau_t = sqrtf(sc.tau * sc.tau + sc.cles * sqrtf(getl(qq, l)) / getl(rho, l));
             setl(omv, l, 2.0f / (sc.tau + tau_t));
             setl(cfv, l, 1.0f - 0.5f * getl(omv, l));
             if (tau_rel) setl(*tau_rel, l, 0.5f * (sc.tau + tau_t));
+        }
         }
         }
         const float2 feq0 = mul2(f2(w0), sub2(drho, mul2(rho, k15)));
@@ -953,10 +970,10 @@ __device__ __forceinline__ void collide_emit(const float2 g[Q], float2 rho, floa
 template <int MODEL, bool FORCED>
 __device__ __forceinline__ void collide2(float2 g[Q], float2 rho, float2 drho, float2 u0, float2 u1, float2 u2,
                                          float2 F0, float2 F1, float2 F2, const Scal<float> &sc, const MrtS &ms,
-                                         float2 *tau_rel = nullptr) {
+                                         float2 *tau_rel = nullptr, const float2 *les_in = nullptr) {
     float2 out[Q];
     collide_emit<MODEL, FORCED, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms,
-                                      [&](int i, float2 v) { out[i] = v; }, tau_rel);
+                                      [&](int i, float2 v) { out[i] = v; }, tau_rel, les_in);
 #pragma unroll
     for (int i = 0; i < Q; i++) g[i] = out[i];
 }
@@ -1076,13 +1093,22 @@ __device__ __forceinline__ void pair_body(const StepArgs &a, const Offs<int> &of
     if (MODEL == CM_SRT || MODEL == CM_TRT) {
         // SRT, TRT: stored pair by pair, so that the 64-register budget holds
         collide_emit<MODEL, FORCED, false>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit);
-    } else if (MODEL == CM_SMAG || MODEL == CM_VREM) {
+    } else if (MODEL == CM_SMAG || MODEL == CM_VREM || MODEL == CM_WALE) {
         // tau_all(z0, z0+1) with the populations (c is even: an aligned pair);
-        // Smagorinsky writes it, Vreman reads what the gradient pass wrote
+        // Smagorinsky and WALE write it, Vreman reads what the gradient pass
+        // wrote; WALE reads the previous one and its rotation entries
         float2 tr = f2(sc.tau);
+        float2 li[4] = {f2(sc.tau), f2(0.f), f2(0.f), f2(0.f)};
         if (MODEL == CM_VREM && active) tr = *(const float2 *)(a.tauf + c);
-        collide_emit<MODEL, FORCED, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit, &tr);
-        if (MODEL == CM_SMAG && active) *(float2 *)(a.tauf + c) = tr;
+        if (MODEL == CM_WALE && active) {
+            const float *og = (const float *)a.og;
+            li[0] = *(const float2 *)(a.tauf_prev + c);
+            li[1] = *(const float2 *)(og + c);
+            li[2] = *(const float2 *)(og + c + N);
+            li[3] = *(const float2 *)(og + c + 2 * N);
+        }
+        collide_emit<MODEL, FORCED, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, emit, &tr, li);
+        if (MODEL != CM_VREM && active) *(float2 *)(a.tauf + c) = tr;
     } else {
         // MRT: all 19 collided first, then stored under one branch
         collide2<MODEL, FORCED>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms);
@@ -1362,6 +1388,27 @@ __device__ __forceinline__ void push_cell(const StepArgs &a, int x, int y, int z
     }
 }
 
+// the per-cell-rate inputs of two arbitrary cells (the fix-up kernels):
+// Vreman's tau_all into tr; WALE's previous tau_all and rotation entries
+template <int MODEL>
+__device__ __forceinline__ void les_cells(const StepArgs &a, const int x[2], const int y[2], const int z[2],
+                                          float2 &tr, float2 li[4]) {
+    if (MODEL != CM_VREM && MODEL != CM_WALE) return;
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        const long long c = (long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l]);
+        if (MODEL == CM_VREM) {
+            setl(tr, l, a.tauf[c]);
+        } else {
+            const float *og = (const float *)a.og;
+            setl(li[0], l, a.tauf_prev[c]);
+            setl(li[1], l, og[c]);
+            setl(li[2], l, og[c + a.N]);
+            setl(li[3], l, og[c + 2 * a.N]);
+        }
+    }
+}
+
 // The IB window: its cells collide with the den/u/force of the IB stage and
 // push again, replacing what the bulk step pushed for them. Two window cells
 // per thread (any two: the lanes are independent).
@@ -1388,15 +1435,12 @@ __device__ __forceinline__ void win_fix_body(const StepArgs &a, const Scal<float
         setl(F2, l, (float)__ldcg(w.force + wc + 2 * w.n));
     }
     float2 tr = f2(sc.tau);
-    if (MODEL == CM_VREM) {
-#pragma unroll
-        for (int l = 0; l < 2; l++)
-            setl(tr, l, a.tauf[(long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l])]);
-    }
-    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, &tr);
+    float2 li[4] = {f2(sc.tau), f2(0.f), f2(0.f), f2(0.f)};
+    les_cells<MODEL>(a, x, y, z, tr, li);
+    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, &tr, li);
     push_cell<P>(a, x[0], y[0], z[0], g, 0);
     if (two) push_cell<P>(a, x[1], y[1], z[1], g, 1);
-    if (MODEL == CM_SMAG) {
+    if (MODEL == CM_SMAG || MODEL == CM_WALE) {
 #pragma unroll
         for (int l = 0; l < 2; l++) {
             if (l == 1 && !two) break;
@@ -1470,12 +1514,9 @@ __global__ void __launch_bounds__(128) k_face_hook(StepArgs a, Scal<float> sc, M
         return;
     }
     float2 tr = f2(sc.tau);
-    if (MODEL == CM_VREM) {
-#pragma unroll
-        for (int l = 0; l < 2; l++)
-            setl(tr, l, a.tauf[(long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l])]);
-    }
-    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, MODEL == CM_VREM ? &tr : nullptr);
+    float2 li[4] = {f2(sc.tau), f2(0.f), f2(0.f), f2(0.f)};
+    les_cells<MODEL>(a, x, y, z, tr, li);
+    collide2<MODEL, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, ms, MODEL == CM_VREM ? &tr : nullptr, li);
 #pragma unroll
     for (int l = 0; l < 2; l++) {
         if (l == 1 && !two) break;
@@ -2249,7 +2290,7 @@ cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
     return prec != FSI_PREC_F64_FAST &&
-           (model == CM_SRT || model == CM_TRT || model == CM_SMAG || model == CM_VREM ||
+           (model == CM_SRT || model == CM_TRT || model == CM_SMAG || model == CM_VREM || model == CM_WALE ||
             (model == CM_MRT && mm->diag)) && small &&
            a.Z % 2 == 0 && a.Z <= 512;
 }

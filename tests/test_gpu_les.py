@@ -69,16 +69,20 @@ def test_exact_walls_and_plate(gpu_lib, model):
             assert r["ef_g"].tobytes() == r["ef_o"].tobytes()
 
 
-@pytest.mark.parametrize("model", [11, 15])
-def test_graph_run_matches_steps(gpu_lib, model):
-    kw = dict(bndConds=(101, 104, 201, 202, 302, 302), nu=0.003, uvwIn=(0.05, 0, 0), iCollidModel=model)
+@pytest.mark.parametrize("prec", [F.PREC_F64, F.PREC_F16])
+@pytest.mark.parametrize("model", [11, 14, 15])
+def test_graph_run_matches_steps(gpu_lib, model, prec):
+    # graph runs (pairs of captured steps) against single steps; FP16 WALE
+    # alternates two tau_all buffers with the distributions
+    kw = dict(bndConds=(101, 104, 201, 202, 302, 302), nu=0.003, uvwIn=(0.05, 0, 0), iCollidModel=model,
+              precision=prec)
     a, b = F.Block(16, 12, 10, **kw), F.Block(16, 12, 10, **kw)
     for blk in (a, b):
         blk.initialise(0.0)
         blk.set_boundary_conditions(0.0)
-    for s in range(6):
+    for s in range(7):
         a.step(blktime=(s + 1) * 1.0)
-    b.run(6, blktime0=1.0)
+    b.run(7, blktime0=1.0)
     assert _same(a.download_f(), b.download_f())
     assert _same(a.tau_all(), b.tau_all())
 
