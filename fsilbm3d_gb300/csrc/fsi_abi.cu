@@ -1101,7 +1101,25 @@ struct Warm {
     bool step = false;
     const double *step_vf = nullptr;
     double step_time = 0.0;
+    // the IB stage beside the bulk step, already forked onto the second
+    // stream (markers uploaded there): its mode
+    int forked = 0;
 };
+
+// the IB mode fsi_block_ib_step runs for h (FSI_IB_AUTO resolved): OVERLAP
+// for the offset forms on the paired kernels (not the gradient models, whose
+// velocity pass needs the IB stage's window first), else GRID
+int resolve_ib_mode(fsi_block *h, const double vf[3], double blktime) {
+    int mode = h->ib_mode;
+    if (h->prec == FSI_PREC_F64 || h->prec == FSI_PREC_F64_FAST) return FSI_IB_GRID;
+    if (mode == FSI_IB_AUTO) {
+        StepArgs t;
+        fill_step(h, vf, blktime, true, t);
+        mode = (step_fast_paired(t, &h->mm, h->prec, h->d.iCollidModel) && !grad_model(h->d.iCollidModel))
+                   ? FSI_IB_OVERLAP : FSI_IB_GRID;
+    }
+    return mode;
+}
 
 // the IB stage's arguments for block h after compute_window (its own marker,
 // force, status and residual arrays)
@@ -1142,7 +1160,8 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         h->tolacc_cap = std::max(ntol, 64);
         CK(cudaMalloc((void **)&h->d_tolacc, sizeof(double) * h->tolacc_cap));
     }
-    CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 4, h->st));
+    // a forked IB stage zeroes its status on the second stream, ahead of it
+    CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 4, wm.forked ? h->st2 : h->st));
     IbCoop a;
     fill_ib(h, vf, denIn, dt, Uref, ntol, dtol, a);
     a.mlp = wm.mlp ? wm.mlp->P : nullptr;
@@ -1150,18 +1169,10 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     a.aux = wm.aux ? h->d_aux : nullptr;
     a.feat = wm.features ? h->d_feat : nullptr;
     a.Uref = Uref;
-    // the IB stage beside the bulk step: on request, and by default for the
-    // offset forms when the paired kernels run the step (their window fix-up
-    // and face hooks wait for it)
-    int mode = h->ib_mode;
-    if (mode == FSI_IB_AUTO && wm.step && h->prec != FSI_PREC_F64_FAST) {
-        StepArgs t;
-        fill_step(h, wm.step_vf, wm.step_time, true, t);
-        mode = (step_fast_paired(t, &h->mm, h->prec, h->d.iCollidModel) && !grad_model(h->d.iCollidModel))
-                   ? FSI_IB_OVERLAP : FSI_IB_GRID;
-    }
-    if (wm.step && (mode == FSI_IB_CLUSTER || mode == FSI_IB_OVERLAP) && !wm.mlp && !wm.features &&
-        h->prec != FSI_PREC_F64_FAST) {
+    // the IB stage beside the bulk step (fsi_block_ib_step forked it onto the
+    // second stream); the window fix-up and the face hooks wait for it
+    const int mode = wm.forked;
+    if (mode) {
         // the IB stage on one cluster on the second stream, beside the bulk
         // step (both only read the state); the window fix-up and the face
         // hooks wait for it
@@ -1172,8 +1183,6 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
             CK(cudaHostAlloc((void **)&h->h_ef, sizeof(double) * 3 * h->Mtot, cudaHostAllocDefault));
             h->h_ef_cap = h->Mtot;
         }
-        CK(cudaEventRecord(h->ev_fork, h->st));
-        CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
         if (mode == FSI_IB_OVERLAP) {
             // beside the bulk step the IB stage takes SM room from it: cap its grid
             long long need = std::max<long long>((h->Mtot + 7) / 8, (h->Nw + 255) / 256);
@@ -1242,13 +1251,14 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
 }
 
 // the window and the marker arrays of one solve
-int ib_upload(fsi_block *h, const double *xyz, const double *vel, const double *area) {
+int ib_upload(fsi_block *h, const double *xyz, const double *vel, const double *area, cudaStream_t st = nullptr) {
     int rc = compute_window(h, xyz);
     if (rc) return rc;
     const int Mt = h->Mtot;
-    CK(cudaMemcpyAsync(h->d_xyz, xyz, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->d_vel, vel, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->d_area, area, sizeof(double) * Mt, cudaMemcpyHostToDevice, h->st));
+    if (!st) st = h->st;
+    CK(cudaMemcpyAsync(h->d_xyz, xyz, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->d_vel, vel, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->d_area, area, sizeof(double) * Mt, cudaMemcpyHostToDevice, st));
     return FSI_OK;
 }
 
@@ -1367,12 +1377,22 @@ int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const
     if (iters) *iters = 0;
     if (residual) *residual = 0.0;
     if (!xyz || !vel || !area || !eforce) return fail(FSI_E_ARG, "null marker array");
-    int rc = ib_upload(h, xyz, vel, area);
-    if (rc) return rc;
     Warm wm;
     wm.step = true;
     wm.step_vf = vf;
     wm.step_time = blktime;
+    const int mode = resolve_ib_mode(h, vf, blktime);
+    cudaStream_t ust = h->st;
+    if (mode == FSI_IB_OVERLAP || mode == FSI_IB_CLUSTER) {
+        // the IB stage beside the bulk step: fork after the previous step, and
+        // keep the marker uploads off the bulk step's stream as well
+        CK(cudaEventRecord(h->ev_fork, h->st));
+        CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+        ust = h->st2;
+        wm.forked = mode;
+    }
+    int rc = ib_upload(h, xyz, vel, area, ust);
+    if (rc) return rc;
     return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
 }
 
