@@ -1,7 +1,7 @@
 /*
  * fsi_oracle.c -- CPU FP64 restatement of FSILBM3D's per-time-step hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path, never shipped or
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA path is tested against, never shipped or
  * called by the product. See fsi_oracle.h for the parity status (unpinned
  * against the Fortran itself; pinned by analytic known-answer tests and by
  * committed golden vectors).

@@ -1,7 +1,7 @@
 /*
  * fsi_oracle.h -- CPU FP64 restatement of FSILBM3D's per-time-step hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker for the CUDA path:
+ * TEST INFRASTRUCTURE ONLY. This library is the oracle the CUDA path is tested against:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
  * load it. The product (libfsi_gpu.so) never links or calls it.
  *
