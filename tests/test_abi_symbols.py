@@ -50,3 +50,40 @@ def test_unsupported_collision_models_are_refused(gpu_lib):
         with pytest.raises(F.FsiError) as e:
             F.Block(8, 8, 8, iCollidModel=m)
         assert e.value.code == F.FSI_E_ARG and what in str(e.value)
+
+
+def test_binding_constants_match_header():
+    # every #define of include/fsi_gpu.h that the Python binding mirrors
+    import fsilbm3d_gb300.abi as A
+    src = open(os.path.join(ROOT, "include", "fsi_gpu.h")).read()
+    defs = dict((k, int(v)) for k, v in re.findall(r"#define\s+(FSI_\w+)\s+(-?\d+)", src))
+    mirror = {
+        "FSI_OK": A.FSI_OK, "FSI_E_ARG": A.FSI_E_ARG, "FSI_E_CUDA": A.FSI_E_CUDA, "FSI_E_NAN": A.FSI_E_NAN,
+        "FSI_E_TIMEOUT": A.FSI_E_TIMEOUT, "FSI_E_BC": A.FSI_E_BC, "FSI_E_RANGE": A.FSI_E_RANGE,
+        "FSI_E_STATE": A.FSI_E_STATE, "FSI_PREC_F64": A.PREC_F64, "FSI_PREC_F64_FAST": A.PREC_F64_FAST,
+        "FSI_PREC_F32": A.PREC_F32, "FSI_PREC_F16": A.PREC_F16, "FSI_PREC_BF16": A.PREC_BF16,
+        "FSI_KERNEL_AUTO": A.KERNEL_AUTO, "FSI_KERNEL_PAIRED": A.KERNEL_PAIRED,
+        "FSI_KERNEL_PIPELINED": A.KERNEL_PIPELINED, "FSI_IB_AUTO": A.IB_AUTO, "FSI_IB_GRID": A.IB_GRID,
+        "FSI_IB_CLUSTER": A.IB_CLUSTER, "FSI_IB_OVERLAP": A.IB_OVERLAP, "FSI_MLP_IN": A.MLP_IN,
+        "FSI_MLP_OUT": A.MLP_OUT, "FSI_MLP_NPARAM": A.MLP_NPARAM, "FSI_MLP_NNORM": A.MLP_NNORM,
+        "FSI_STATIC_FACE_CELLS": A.STATIC_FACE_CELLS,
+    }
+    for k, v in mirror.items():
+        assert defs[k] == v, k
+
+
+def test_block_descriptor_layout_matches_header():
+    # the ctypes mirror of fsi_block_desc has the header's fields in order
+    import fsilbm3d_gb300.abi as A
+    src = open(os.path.join(ROOT, "include", "fsi_gpu.h")).read()
+    body = re.search(r"typedef struct \{(.*?)\} fsi_block_desc;", src, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        for part in decl.split(","):
+            m = re.search(r"\*?\s*(\w+)\s*(\[\d+\])?\s*$", part.strip())
+            names.append(m.group(1))
+    assert names == [f[0] for f in A.BlockDesc._fields_]
