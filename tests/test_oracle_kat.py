@@ -185,15 +185,21 @@ def test_ib_stationary_plate_symmetric_force():
 
 
 @pytest.mark.parametrize("scheme", [1, 2])
-def test_refined_uniform_flow_stays_uniform(scheme):
+@pytest.mark.parametrize("model", [1, 11, 15])
+def test_refined_uniform_flow_stays_uniform(scheme, model):
+    # the LES models see no stress and no gradient: tau_all stays tau and the
+    # exchange carries it per cell
     from refine import TwoLevel
-    tl = TwoLevel(gpu=False, scheme=scheme)
+    tl = TwoLevel(gpu=False, scheme=scheme, model=model)
     f0 = tl.ofa.fview().copy()
     s0 = tl.oso.fview().copy()
     for _ in range(3):
         tl.step()
     assert np.max(np.abs(tl.ofa.fview() - f0)) < 1e-15
     assert np.max(np.abs(tl.oso.fview() - s0)) < 1e-15
+    if model != 1:
+        assert np.max(np.abs(tl.ofa.tau_all - tl.ofa.b.tau)) < 1e-12
+        assert np.max(np.abs(tl.oso.tau_all - tl.oso.b.tau)) < 1e-12
 
 
 def test_trt_with_equal_rates_is_srt():
