@@ -2195,7 +2195,7 @@ __device__ __forceinline__ void batch_prologue(const BatchCase *__restrict__ cas
 }
 
 template <int P, int MODEL, bool FORCED, int T>
-__global__ void __launch_bounds__(T, T == 512 ? 1 : (T == 128 ? 2 * pair_minb<P, MODEL, FORCED>() : pair_minb<P, MODEL, FORCED>()))
+__global__ void __launch_bounds__(T, T == 512 ? 1 : pair_ctas<P, MODEL, FORCED, T>())
 k_step_batch(const BatchCase *__restrict__ cases, const int *__restrict__ gcase) {
     using S = typename V2<P>::S;
     __shared__ BatchCta cta;
