@@ -10,7 +10,7 @@ reference's host-side structural solver, which stays outside the GPU path.
 One step = the IB stage (markers host -> device, the penalty loop to
 ntol = 5 / dtol = 1e-4 in one cooperative launch, the Lagrangian force
 device -> host) + the fused collide/stream kernel + the face kernels, through
-one fsi_block_ib_step call (the fluid step is queued behind the IB stage).
+one fsi_block_ib_step call (the IB stage runs beside the bulk kernel).
 Distributions are stored as FP16 offsets f - w_i, collision runs in FP32,
 the Lagrangian force in FP64.
 
@@ -38,6 +38,25 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+
+
+def pin_rank_device(env=os.environ):
+    """One GPU per rank under torchrun: expose only this rank's GPU to the
+    process (the LOCAL_RANK-th of the visible ones) before any CUDA call, so
+    that the library, torch and nvidia-smi sampling agree on it. Returns the
+    GPU's id as nvidia-smi -i takes it (an index or a UUID)."""
+    vis = env.get("CUDA_VISIBLE_DEVICES")
+    devs = [d.strip() for d in vis.split(",") if d.strip()] if vis else None
+    lr = env.get("LOCAL_RANK")
+    if lr is None or int(env.get("WORLD_SIZE", "1")) <= 1:
+        return devs[0] if devs else "0"
+    lr = int(lr)
+    dev = devs[lr] if devs and lr < len(devs) else str(lr)
+    env["CUDA_VISIBLE_DEVICES"] = dev
+    return dev
+
+
+GPU_INDEX = pin_rank_device()
 
 FSI_GRID = (384, 256, 256)
 FSI_NODES = 33
@@ -632,7 +651,7 @@ def main():
     # ---- headline: mixed path, K steps timed on the block's stream
     b = fsi_block(F, F.PREC_F16, dh, nu, plate)
     t, _ = fsi_steps(b, plate, dh, 0.0, a.warmup)
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks = ClockSampler(GPU_INDEX)
     clocks.start()
     barrier(dist)
     b.timer_start()

@@ -41,3 +41,17 @@ def test_two_gloo_ranks_replicas():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert res == [(0, 2.0, 300.0), (1, 2.0, 300.0)]
+
+
+def test_bench_pins_one_gpu_per_rank():
+    # under torchrun each rank sees only its own GPU (the LOCAL_RANK-th of
+    # the visible ones); a single process keeps the environment as it is
+    import bench
+    env = {"LOCAL_RANK": "2", "WORLD_SIZE": "4", "CUDA_VISIBLE_DEVICES": "4,5,6,7"}
+    assert bench.pin_rank_device(env) == "6" and env["CUDA_VISIBLE_DEVICES"] == "6"
+    env = {"LOCAL_RANK": "1", "WORLD_SIZE": "2"}
+    assert bench.pin_rank_device(env) == "1" and env["CUDA_VISIBLE_DEVICES"] == "1"
+    env = {"WORLD_SIZE": "1"}
+    assert bench.pin_rank_device(env) == "0" and "CUDA_VISIBLE_DEVICES" not in env
+    env = {"WORLD_SIZE": "1", "CUDA_VISIBLE_DEVICES": "GPU-abc"}
+    assert bench.pin_rank_device(env) == "GPU-abc" and env["CUDA_VISIBLE_DEVICES"] == "GPU-abc"
