@@ -1,10 +1,14 @@
 """Build libfsi_gpu.so (sm_103a) in-tree with nvcc.
 
-Four translation units, compiled in parallel:
+Eight translation units, compiled in parallel:
   k_f64_exact.cu  -fmad=false  FP64 kernels in the reference's operation order
-  k_fast.cu                    FP64 regrouped and FP32/FP16/BF16 storage forms
+  k_fast.cu       x4           FP64 regrouped and FP32/FP16/BF16 storage forms,
+                               one unit per form (-DFSI_FAST_PREC=1..4)
+  fast_route.cu                forwards the fast launchers to the unit of a form
   k_mlp.cu                     warm-start perceptron: inference, gradient, Adam
   fsi_abi.cu                   host implementation of include/fsi_gpu.h
+The library is linked with --no-undefined, so that a launcher missing from a
+unit fails the build rather than the first load.
 """
 import os
 import subprocess
@@ -20,14 +24,15 @@ ROOT = os.path.dirname(HERE)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I" + os.path.join(ROOT, "include")]
-UNITS = {
-    "k_f64_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
-    "k_fast.cu": [],
-    "k_mlp.cu": [],
+# (source, object, extra flags); the slowest units first
+UNITS = [("k_fast.cu", "k_fast_p%d.o" % p, ["-DFSI_FAST_PREC=%d" % p]) for p in (3, 4, 2, 1)] + [
+    ("k_f64_exact.cu", "k_f64_exact.o", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     # host arithmetic (tau, MRT matrices) without contraction, as the reference
-    "fsi_abi.cu": ["-Xcompiler", "-ffp-contract=off"],
-}
-HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "bc_impl.cuh", "ib_impl.cuh", "mlp_impl.cuh"]
+    ("fsi_abi.cu", "fsi_abi.o", ["-Xcompiler", "-ffp-contract=off"]),
+    ("k_mlp.cu", "k_mlp.o", []),
+    ("fast_route.cu", "fast_route.o", []),
+]
+HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "store_acc.cuh", "bc_impl.cuh", "ib_impl.cuh", "mlp_impl.cuh"]
 
 
 def _nvcc():
@@ -50,9 +55,9 @@ def build(force=False, verbose=False):
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "fsi_gpu.h")]
     jobs = []
     objs = []
-    for src, extra in UNITS.items():
+    for src, obj, extra in UNITS:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, obj)
         objs.append(o)
         if force or _stale(o, [s, __file__] + hdrs):
             jobs.append([nvcc] + ARCH + COMMON + extra + ["-c", s, "-o", o])
@@ -65,12 +70,12 @@ def build(force=False, verbose=False):
             raise RuntimeError("nvcc failed:\n%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
         return r.stderr
 
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), max(2, os.cpu_count() or 2))) as ex:
         for msg in ex.map(run, jobs):
             if verbose and msg:
                 print(msg)
     if force or jobs or _stale(LIB, objs):
-        run([nvcc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs)
+        run([nvcc] + ARCH + ["-shared", "-Xlinker", "--no-undefined", "-o", LIB + ".tmp"] + objs)
         os.replace(LIB + ".tmp", LIB)
     return LIB
 

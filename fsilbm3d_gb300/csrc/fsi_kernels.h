@@ -17,7 +17,6 @@ cudaError_t launch_step_f64_exact(const StepArgs &a, const MrtMats *mm, int mode
 // stage), written to a.den/a.u before the step of a model that reads its
 // neighbours' velocity (grad_model)
 cudaError_t launch_step_macro_f64(const StepArgs &a, cudaStream_t st);
-cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st);
 cudaError_t launch_bc_f64(const BcArgs &a, cudaStream_t st);
 cudaError_t launch_halfway_f64(const double *f, double *hw, int X, int Y, int Z, int face,
                                cudaStream_t st);
@@ -73,11 +72,6 @@ struct IbCoop {
     float *feat;                 // (12,Mtot) features out, or null
     double Uref;
 };
-cudaError_t launch_ib_coop(const IbCoop &a, int prec, int grid, cudaStream_t st);
-// the same on one thread-block cluster, which may run beside other kernels
-// (offset storage forms)
-cudaError_t launch_ib_cluster(const IbCoop &a, int prec, cudaStream_t st);
-int ib_coop_grid(int prec);  // co-resident CTAs (256 threads) on this device, 0 on error
 
 // ---- output packing (k_f64_exact.cu, reference operation order) ----
 cudaError_t launch_pack_flow(const double *den, const double *u, int X, int Y, int Z, int off, double denIn,
@@ -118,43 +112,77 @@ cudaError_t launch_pair_s2f(void *ff, int prec, int FX, int FY, int FZ, TauSrc t
                             int SZ, TauSrc ts, const PairGeom &p, int face, const double vf[3], double dh, int *err,
                             cudaStream_t st);
 
-// ---- fast kernels (k_fast.cu): FP64 regrouped, FP32/FP16/BF16 storage ----
-cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st);
-// true when launch_step_fast runs the paired kernels (which can write 101 z faces)
-bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model);
-cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st);
-// both faces of one axis in one launch (offset forms; faces that share no cell
-// they read or write)
-cudaError_t launch_bc_pair_fast(const BcArgs &lo, const BcArgs &hi, int prec, cudaStream_t st);
-cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st);
-cudaError_t launch_convert_from_store(const void *fs, double *f64, long long N, int prec, cudaStream_t st);
-cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, int X, int Y, int Z, double dh,
-                              const double vf[3], cudaStream_t st);
-cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double *wu, const IbGeom &g, long long N,
-                                  const double vf[3], cudaStream_t st);
-
-// ---- many blocks stepped together (k_fast.cu; offset forms, paired kernels) ----
-// One entry per block: its step arguments (src/dst of this step, window, z
-// faces), the MRT rates S_k/|row k|^2, and its row groups: tpr = zDim/2 pairs
-// per z-row, R rows per group, ngy groups per x-plane, g0 = first global group.
+// ---- the throughput forms (k_fast.cu, built once per storage form) ----
+// Many blocks stepped together (offset forms, paired kernels): one entry per
+// block with its step arguments (src/dst of this step, window, z faces), the
+// MRT rates S_k/|row k|^2, and its row groups: tpr = zDim/2 pairs per z-row,
+// R rows per group, ngy groups per x-plane, g0 = first global group.
 struct BatchCase {
     StepArgs a;
     float sd[19];
     int tpr, R, ngy, g0;
 };
-// the bulk step of every block (G groups in all, gcase[j] = block of group
-// j) with CTAs of `threads`; then the IB-window fix-up of every block (wmax >=
-// each block's window cells)
-cudaError_t launch_batch_step(const BatchCase *d_cases, const int *d_gcase, int n, int G, int threads, long long wmax,
-                              int prec, int model, bool forced, cudaStream_t st);
-// the IB-window fix-up alone (after the bulk step and the IB stage)
-cudaError_t launch_batch_winfix(const BatchCase *d_cases, int n, long long wmax, int prec, int model, cudaStream_t st);
-// face k of every block (bcs: n entries for this face; code BC_FLUID = none)
-cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int Bmax, int prec, cudaStream_t st);
-// the IB stage of every block, one CTA per block
-cudaError_t launch_batch_ib(const IbCoop *d_ib, int n, int threads, int prec, cudaStream_t st);
 // thread counts the batched bulk kernel is built for (the autotuner's choices)
 constexpr int BATCH_THREADS[3] = {256, 512, 128};
+
+// Every launcher of k_fast.cu takes the storage form `prec` and returns
+// cudaErrorInvalidValue (0 / false for the two queries) for a form it does not
+// serve. k_fast.cu is compiled once per form (FSI_PREC_F64_FAST, F32, F16,
+// BF16) into namespace fast_p<prec>; fast_route.cu defines the names below in
+// namespace fsi and forwards each call to the unit of its form.
+//
+//  step_fast_paired        true when launch_step_fast runs the paired kernels
+//                          (which can write 101 z faces)
+//  launch_step_fast        the fused collide+stream step of one block
+//  launch_step_macro_fast  den/u (FP32 `uf`) of every cell as the collision
+//                          sees them, then the LES gradient pass (WALE, Vreman)
+//  launch_bc_fast          one face
+//  launch_bc_pair_fast     both faces of one axis in one launch (offset forms;
+//                          faces that share no cell they read or write)
+//  launch_convert_to_store / launch_convert_from_store   FP64 <-> storage form
+//  launch_macro_fast       den/u of the whole block (output)
+//  launch_win_macro_fast   den/u of the IB window
+//  launch_ib_coop          the IB solve as one cooperative launch of `grid` CTAs
+//  launch_ib_cluster       the same on one thread-block cluster, which may run
+//                          beside other kernels (offset forms)
+//  ib_coop_grid            co-resident CTAs (256 threads) on this device, 0 on error
+//  launch_batch_step       the bulk step of every block (G groups in all,
+//                          gcase[j] = block of group j) with CTAs of `threads`;
+//                          then the IB-window fix-up of every block (wmax >=
+//                          each block's window cells)
+//  launch_batch_winfix     the IB-window fix-up alone (after the bulk step and
+//                          the IB stage)
+//  launch_batch_bc         face k of every block (bcs: n entries for this face;
+//                          code BC_FLUID = none)
+//  launch_batch_ib         the IB stage of every block, one CTA per block
+#define FSI_FAST_API                                                                                             \
+    bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model);                           \
+    cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st);    \
+    cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st);                            \
+    cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st);                                      \
+    cudaError_t launch_bc_pair_fast(const BcArgs &lo, const BcArgs &hi, int prec, cudaStream_t st);              \
+    cudaError_t launch_convert_to_store(const double *f64, void *fs, long long N, int prec, cudaStream_t st);    \
+    cudaError_t launch_convert_from_store(const void *fs, double *f64, long long N, int prec, cudaStream_t st);  \
+    cudaError_t launch_macro_fast(const void *fs, int prec, double *den, double *u, int X, int Y, int Z,         \
+                                  double dh, const double vf[3], cudaStream_t st);                               \
+    cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double *wu, const IbGeom &g,       \
+                                      long long N, const double vf[3], cudaStream_t st);                         \
+    cudaError_t launch_ib_coop(const IbCoop &a, int prec, int grid, cudaStream_t st);                            \
+    cudaError_t launch_ib_cluster(const IbCoop &a, int prec, cudaStream_t st);                                   \
+    int ib_coop_grid(int prec);                                                                                  \
+    cudaError_t launch_batch_step(const BatchCase *d_cases, const int *d_gcase, int n, int G, int threads,       \
+                                  long long wmax, int prec, int model, bool forced, cudaStream_t st);            \
+    cudaError_t launch_batch_winfix(const BatchCase *d_cases, int n, long long wmax, int prec, int model,        \
+                                    cudaStream_t st);                                                            \
+    cudaError_t launch_batch_bc(const BcArgs *d_bcs, int n, int face, int Amax, int Bmax, int prec,              \
+                                cudaStream_t st);                                                                \
+    cudaError_t launch_batch_ib(const IbCoop *d_ib, int n, int threads, int prec, cudaStream_t st);
+
+FSI_FAST_API
+namespace fast_p1 { FSI_FAST_API }  // FSI_PREC_F64_FAST
+namespace fast_p2 { FSI_FAST_API }  // FSI_PREC_F32
+namespace fast_p3 { FSI_FAST_API }  // FSI_PREC_F16
+namespace fast_p4 { FSI_FAST_API }  // FSI_PREC_BF16
 
 // ---- warm-start perceptron (k_mlp.cu) ----
 cudaError_t launch_mlp_forward(const float *P, const float *nrm, const float *X, float *Y, int n, cudaStream_t st);

@@ -13,6 +13,12 @@
 // Physics and step order are those of the exact form (collision_ SRT/MRT
 // with Guo forcing, FluidDomain.f90:1208-1238; streaming_ :1514-1625; the
 // IB window and face hooks of k_f64_exact.cu); only rounding differs.
+//
+// This file is compiled once per storage form, with -DFSI_FAST_PREC=<form>
+// (1..4: FSI_PREC_F64_FAST, F32, F16, BF16), so that the four forms' kernels
+// build in parallel. Each unit defines the launchers of fsi_kernels.h's
+// FSI_FAST_API in namespace fsi::fast_p<form>; fast_route.cu forwards the
+// public names to them.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -24,6 +30,16 @@
 #include "ib_impl.cuh"
 #include "mlp_impl.cuh"
 #include "../../include/fsi_gpu.h"
+
+#ifndef FSI_FAST_PREC
+#error "k_fast.cu is built once per storage form: -DFSI_FAST_PREC=1|2|3|4"
+#endif
+#if FSI_FAST_PREC < FSI_PREC_F64_FAST || FSI_FAST_PREC > FSI_PREC_BF16
+#error "FSI_FAST_PREC must be FSI_PREC_F64_FAST, F32, F16 or BF16"
+#endif
+#define FSI_CAT2(a, b) a##b
+#define FSI_CAT(a, b) FSI_CAT2(a, b)
+#define FSI_FAST_NS FSI_CAT(fast_p, FSI_FAST_PREC)
 
 namespace fsi {
 namespace {
@@ -334,7 +350,7 @@ __global__ void __launch_bounds__(256) k_les_grad(StepArgs a, Scal<typename ST<P
     const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
     if (z >= a.Z) return;
     const long long c = cidx(z, y, x, a.Z, a.Y);
-    if (MODEL == CM_WALE) {
+    if constexpr (MODEL == CM_WALE) {
         const C ox = C(0.5) * (les_diff_c<P>(a, 2, 1, z, y, x, c, sc.dh) - les_diff_c<P>(a, 1, 2, z, y, x, c, sc.dh));
         const C oy = C(0.5) * (les_diff_c<P>(a, 0, 2, z, y, x, c, sc.dh) - les_diff_c<P>(a, 2, 0, z, y, x, c, sc.dh));
         const C oz = C(0.5) * (les_diff_c<P>(a, 1, 0, z, y, x, c, sc.dh) - les_diff_c<P>(a, 0, 1, z, y, x, c, sc.dh));
@@ -342,36 +358,36 @@ __global__ void __launch_bounds__(256) k_les_grad(StepArgs a, Scal<typename ST<P
         og[c] = C(-0.5) * oz;
         og[c + a.N] = C(0.5) * oy;
         og[c + 2 * a.N] = C(-0.5) * ox;
-        return;
-    }
-    C m[3][3];
+    } else {
+        C m[3][3];
 #pragma unroll
-    for (int j = 0; j < 3; j++)
+        for (int j = 0; j < 3; j++)
 #pragma unroll
-        for (int i = 0; i < 3; i++) m[i][j] = C(0.5) * les_diff_c<P>(a, i, j, z, y, x, c, sc.dh);
-    C g = C(0);
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) g = fmax(g, fabs(m[i][j]));
-    C OP = C(0);
-    if (g > C(0)) {
-        const C ig = C(1) / g;
+            for (int i = 0; i < 3; i++) m[i][j] = C(0.5) * les_diff_c<P>(a, i, j, z, y, x, c, sc.dh);
+        C g = C(0);
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int j = 0; j < 3; j++) m[i][j] *= ig;
-        const C r0 = m[0][0] * m[0][0] + m[0][1] * m[0][1] + m[0][2] * m[0][2];
-        const C r1 = m[1][0] * m[1][0] + m[1][1] * m[1][1] + m[1][2] * m[1][2];
-        const C r2 = m[2][0] * m[2][0] + m[2][1] * m[2][1] + m[2][2] * m[2][2];
-        const C d01 = m[0][0] * m[1][0] + m[0][1] * m[1][1] + m[0][2] * m[1][2];
-        const C d02 = m[0][0] * m[2][0] + m[0][1] * m[2][1] + m[0][2] * m[2][2];
-        const C d12 = m[1][0] * m[2][0] + m[1][1] * m[2][1] + m[1][2] * m[2][2];
-        const C bb = (r0 * r1 - d01 * d01) + (r0 * r2 - d02 * d02) + (r1 * r2 - d12 * d12);
-        OP = g * sqrt(bb / (r0 + r1 + r2));
-        if (!isfinite(OP)) OP = C(0);
+            for (int j = 0; j < 3; j++) g = fmax(g, fabs(m[i][j]));
+        C OP = C(0);
+        if (g > C(0)) {
+            const C ig = C(1) / g;
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) m[i][j] *= ig;
+            const C r0 = m[0][0] * m[0][0] + m[0][1] * m[0][1] + m[0][2] * m[0][2];
+            const C r1 = m[1][0] * m[1][0] + m[1][1] * m[1][1] + m[1][2] * m[1][2];
+            const C r2 = m[2][0] * m[2][0] + m[2][1] * m[2][1] + m[2][2] * m[2][2];
+            const C d01 = m[0][0] * m[1][0] + m[0][1] * m[1][1] + m[0][2] * m[1][2];
+            const C d02 = m[0][0] * m[2][0] + m[0][1] * m[2][1] + m[0][2] * m[2][2];
+            const C d12 = m[1][0] * m[2][0] + m[1][1] * m[2][1] + m[1][2] * m[2][2];
+            const C bb = (r0 * r1 - d01 * d01) + (r0 * r2 - d02 * d02) + (r1 * r2 - d12 * d12);
+            OP = g * sqrt(bb / (r0 + r1 + r2));
+            if (!isfinite(OP)) OP = C(0);
+        }
+        tau_put<P>(a, c, (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5));
     }
-    tau_put<P>(a, c, (sc.nu + sc.cles * OP * sc.dh * sc.dh) / (sc.dh * C(1.0 / 3.0)) + C(0.5));
 }
 
 template <int P, int MODEL>
@@ -1393,18 +1409,19 @@ __device__ __forceinline__ void push_cell(const StepArgs &a, int x, int y, int z
 template <int MODEL>
 __device__ __forceinline__ void les_cells(const StepArgs &a, const int x[2], const int y[2], const int z[2],
                                           float2 &tr, float2 li[4]) {
-    if (MODEL != CM_VREM && MODEL != CM_WALE) return;
+    if constexpr (MODEL == CM_VREM || MODEL == CM_WALE) {
 #pragma unroll
-    for (int l = 0; l < 2; l++) {
-        const long long c = (long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l]);
-        if (MODEL == CM_VREM) {
-            setl(tr, l, a.tauf[c]);
-        } else {
-            const float *og = (const float *)a.og;
-            setl(li[0], l, a.tauf_prev[c]);
-            setl(li[1], l, og[c]);
-            setl(li[2], l, og[c + a.N]);
-            setl(li[3], l, og[c + 2 * a.N]);
+        for (int l = 0; l < 2; l++) {
+            const long long c = (long long)z[l] + (long long)a.Z * ((long long)y[l] + (long long)a.Y * x[l]);
+            if (MODEL == CM_VREM) {
+                setl(tr, l, a.tauf[c]);
+            } else {
+                const float *og = (const float *)a.og;
+                setl(li[0], l, a.tauf_prev[c]);
+                setl(li[1], l, og[c]);
+                setl(li[2], l, og[c + a.N]);
+                setl(li[3], l, og[c + 2 * a.N]);
+            }
         }
     }
 }
@@ -2278,14 +2295,12 @@ cudaError_t bc_inst(const BcArgs &a, cudaStream_t st) {
 
 }  // namespace
 
-#define FSI_DISPATCH(prec, ...)                                                    \
-    switch (prec) {                                                                \
-    case FSI_PREC_F64_FAST: { constexpr int PP = FSI_PREC_F64_FAST; __VA_ARGS__; } \
-    case FSI_PREC_F32: { constexpr int PP = FSI_PREC_F32; __VA_ARGS__; }           \
-    case FSI_PREC_F16: { constexpr int PP = FSI_PREC_F16; __VA_ARGS__; }           \
-    case FSI_PREC_BF16: { constexpr int PP = FSI_PREC_BF16; __VA_ARGS__; }         \
-    default: return cudaErrorInvalidValue;                                         \
-    }
+namespace FSI_FAST_NS {
+
+// the body with PP = this unit's storage form; any other form is refused
+#define FSI_DISPATCH(prec, ...)                                 \
+    if ((prec) != FSI_FAST_PREC) return cudaErrorInvalidValue; \
+    { constexpr int PP = FSI_FAST_PREC; __VA_ARGS__; }
 
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
@@ -2328,13 +2343,12 @@ cudaError_t launch_bc_fast(const BcArgs &a, int prec, cudaStream_t st) {
 }
 
 
-#define FSI_DISPATCH_OFF(prec, ...)                                          \
-    switch (prec) {                                                          \
-    case FSI_PREC_F32: { constexpr int PP = FSI_PREC_F32; __VA_ARGS__; }     \
-    case FSI_PREC_F16: { constexpr int PP = FSI_PREC_F16; __VA_ARGS__; }     \
-    case FSI_PREC_BF16: { constexpr int PP = FSI_PREC_BF16; __VA_ARGS__; }   \
-    default: return cudaErrorInvalidValue;                                   \
-    }
+// the same for the kernels of the offset forms alone
+#if FSI_FAST_PREC == FSI_PREC_F64_FAST
+#define FSI_DISPATCH_OFF(prec, ...) return cudaErrorInvalidValue;
+#else
+#define FSI_DISPATCH_OFF(prec, ...) FSI_DISPATCH(prec, __VA_ARGS__)
+#endif
 
 cudaError_t launch_bc_pair_fast(const BcArgs &lo, const BcArgs &hi, int prec, cudaStream_t st) {
     const int ax = lo.face >> 1;
@@ -2431,14 +2445,8 @@ int ib_coop_grid(int prec) {
     int dev = 0, sms = 0, nb = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    cudaError_t e = cudaErrorInvalidValue;
-    switch (prec) {
-    case FSI_PREC_F64_FAST: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_F64_FAST>, 256, 0); break;
-    case FSI_PREC_F32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_F32>, 256, 0); break;
-    case FSI_PREC_F16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_F16>, 256, 0); break;
-    case FSI_PREC_BF16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_PREC_BF16>, 256, 0); break;
-    default: break;
-    }
+    if (prec != FSI_FAST_PREC) return 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ib_coop<FSI_FAST_PREC>, 256, 0);
     return e == cudaSuccess ? nb * sms : 0;
 }
 
@@ -2451,4 +2459,5 @@ cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double
                  return cudaGetLastError())
 }
 
+}  // namespace FSI_FAST_NS
 }  // namespace fsi
