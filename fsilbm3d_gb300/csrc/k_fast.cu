@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "bc_impl.cuh"
 #include "fsi_kernels.h"
@@ -1342,27 +1343,33 @@ cudaError_t pipe_run(const StepArgs &a, const Offs<int> &of, const Scal<float> &
     auto kern = k_step_pipe<P, MODEL, FORCED>;
     const size_t smem = pipe_smem<P>(R, a.Z);
     static int grid_cache[64][2] = {};  // per device: grid, smem it was sized for
+    static std::mutex grid_mu;          // callers on several host threads
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (grid_cache[dev][1] != (int)smem) {
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        int nb = 0, sms = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, tpr * R, smem);
-        if (e != cudaSuccess) return e;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-        if (nb < 1) return cudaErrorInvalidConfiguration;
-        grid_cache[dev][0] = nb * sms;
-        grid_cache[dev][1] = (int)smem;
+    int resident = 0;
+    {
+        std::lock_guard<std::mutex> lock(grid_mu);
+        if (grid_cache[dev][1] != (int)smem) {
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            int nb = 0, sms = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, tpr * R, smem);
+            if (e != cudaSuccess) return e;
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            if (nb < 1) return cudaErrorInvalidConfiguration;
+            grid_cache[dev][0] = nb * sms;
+            grid_cache[dev][1] = (int)smem;
+        }
+        resident = grid_cache[dev][0];
     }
     PipeGeom pg;
     pg.R = R;
     pg.ngy = (a.Y + R - 1) / R;
     pg.G = pg.ngy * a.X;
-    const int grid = std::min(grid_cache[dev][0], pg.G);
+    const int grid = std::min(resident, pg.G);
     kern<<<grid, dim3(tpr, R), smem, st>>>(a, of, sc, ms, pg);
     return cudaGetLastError();
 }

@@ -8,6 +8,8 @@
 //                    shared memory, then every parameter's gradient summed
 //                    over the tile and added to the global gradient
 //  k_mlp_adam        Adam step with bias correction; clears the gradient
+#include <atomic>
+
 #include "fsi_kernels.h"
 #include "mlp_impl.cuh"
 
@@ -150,16 +152,17 @@ cudaError_t launch_mlp_grad(const float *P, const float *nrm, const float *X, co
                             long long b0, int nb, int batch_total, float *grad, float *loss, cudaStream_t st) {
     if (nb <= 0) return cudaSuccess;
     // the tile needs more than the default 48 KB of shared memory; the
-    // attribute is set once per device
-    static bool attr[64] = {};
+    // attribute is set once per device (setting it twice is harmless, so an
+    // atomic flag is enough for callers on several host threads)
+    static std::atomic<bool> attr[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!attr[dev]) {
+    if (!attr[dev].load(std::memory_order_acquire)) {
         e = cudaFuncSetAttribute(k_mlp_tile_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_tile_smem());
         if (e != cudaSuccess) return e;
-        attr[dev] = true;
+        attr[dev].store(true, std::memory_order_release);
     }
     k_mlp_tile_grad<<<(nb + TS - 1) / TS, 256, mlp_tile_smem(), st>>>(P, nrm, X, Y, perm, b0, nb,
                                                                      1.0f / (3.0f * (float)batch_total), grad, loss);
