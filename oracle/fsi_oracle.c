@@ -233,14 +233,23 @@ void or_macro(or_block *b) {
             }
 }
 
-/* ResetVolumeForce_ / add_volume_force_, FluidDomain.f90:1182-1206 */
-void or_reset_force(or_block *b) { memset(b->force, 0, sizeof(double) * 3 * ncell(b)); }
+/* ResetVolumeForce_ / add_volume_force_, FluidDomain.f90:1182-1206: x-slabs
+ * shared among the threads as the reference's OpenMP loops share them */
+void or_reset_force(or_block *b) {
+    size_t n = ncell(b), slab = (size_t)b->Y * b->Z;
+    #pragma omp parallel for schedule(static)
+    for (int x = 0; x < b->X; x++)
+        for (int k = 0; k < 3; k++) memset(b->force + n * k + slab * x, 0, sizeof(double) * slab);
+}
 void or_add_force(or_block *b) {
-    size_t n = ncell(b);
-    for (int k = 0; k < 3; k++) {
-        double v = b->volumeForce[k];
-        for (size_t i = 0; i < n; i++) b->force[i + n * k] = b->force[i + n * k] + v;
-    }
+    size_t n = ncell(b), slab = (size_t)b->Y * b->Z;
+    const double *vf = b->volumeForce;
+    #pragma omp parallel for schedule(static)
+    for (int x = 0; x < b->X; x++)
+        for (int k = 0; k < 3; k++) {
+            double *f = b->force + n * k + slab * x;
+            for (size_t i = 0; i < slab; i++) f[i] = f[i] + vf[k];
+        }
 }
 
 /* ConstParams.f90:19-20: the TRT population pairs */

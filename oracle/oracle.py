@@ -73,12 +73,25 @@ class OrPair(C.Structure):
 
 
 _lib = None
+_kind = "parity"
+
+
+def select_build(kind):
+    """Choose the build this process loads ("parity", the default, or
+    "timing": see build_oracle.py) before the first oracle call. Returns
+    the build in use, which stays the loaded one once a call has been made."""
+    global _kind
+    if kind not in build_oracle.FLAGS:
+        raise ValueError("unknown oracle build %r" % (kind,))
+    if _lib is None:
+        _kind = kind
+    return _kind
 
 
 def lib():
     global _lib
     if _lib is None:
-        path = build_oracle.build()
+        path = build_oracle.build(kind=_kind)
         L = C.CDLL(path)
         BP, FP, BDP = C.POINTER(OrBlock), C.POINTER(OrFlow), C.POINTER(OrBody)
         L.or_evaluate_velocity.argtypes = [FP, C.c_double, C.c_double, C.c_double, C.c_double, DP]
