@@ -291,6 +291,15 @@ def cpu_fsi_sample(threads, nsteps=None, seconds=12.0):
     return X * Y * Z * n / el / 1e6, n, el, kind
 
 
+def cpu_baseline_leg(threads, seconds=12.0):
+    """The line's cpu_baseline object: the oracle on `threads` host cores for
+    about `seconds` of the headline workload."""
+    mlups, n, el, kind = cpu_fsi_sample(threads, seconds=seconds)
+    return {"value": round(mlups, 2), "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": "oracle (C/OpenMP restatement of the reference step, FP64 MRT + IB, %s build) on the "
+                      "headline workload, %d steps after one warm-up step, %.1f s" % (kind, n, el)}
+
+
 # ---------------------------------------------------- periodic TGV forms
 
 def tgv_f64(grid):
@@ -739,11 +748,7 @@ def main():
 
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:
-        thr = os.cpu_count() or 1
-        mlups_cpu, n, el, kind = cpu_fsi_sample(thr, seconds=12.0)
-        cpu = {"value": round(mlups_cpu, 2), "unit": "MLUPS", "cores": thr, "kind": "port",
-               "sample": "oracle (C/OpenMP restatement of the reference step, FP64 MRT + IB, %s build) on the "
-                         "headline workload, %d steps after one warm-up step, %.1f s" % (kind, n, el)}
+        cpu = cpu_baseline_leg(os.cpu_count() or 1)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,

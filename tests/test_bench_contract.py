@@ -1,10 +1,10 @@
-"""The JSON line of bench.py's reference arm (runs without a GPU).
+"""The CPU parts of bench.py's JSON lines (runs without a GPU).
 
 `bench.py --impl reference` times the CPU restatement of the reference step on
-the headline workload. Here the same code path runs on a shrunken case (a
-9x9-marker plate in a 32x24x24 block, one step) and the printed line is
-checked against the benchmark contract: the keys, their types and the
-agreement of value, cpu_baseline and e2e.
+the headline workload, and the GPU arm's cpu_baseline object comes from the
+same code. Here both run on a shrunken case (a 9x9-marker plate in a
+32x24x24 block) and their output is checked against the benchmark contract:
+the keys, their types and the agreement of value, cpu_baseline and e2e.
 """
 import json
 import types
@@ -41,3 +41,13 @@ def test_reference_arm_silent_on_other_ranks(capsys):
     a = types.SimpleNamespace(steps=1, warmup=1)
     bench.main_reference(a, 1, 2, None)
     assert capsys.readouterr().out.strip() == ""
+
+
+def test_cpu_baseline_leg(monkeypatch):
+    import bench
+    monkeypatch.setattr(bench, "FSI_GRID", (32, 24, 24))
+    monkeypatch.setattr(bench, "FSI_NODES", 9)
+    cb = bench.cpu_baseline_leg(2, seconds=0.05)
+    assert set(cb) == {"value", "unit", "cores", "kind", "sample"}
+    assert cb["value"] > 0 and cb["unit"] == "MLUPS" and cb["cores"] == 2 and cb["kind"] == "port"
+    assert "build" in cb["sample"] and "steps" in cb["sample"]
