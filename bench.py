@@ -243,6 +243,21 @@ def fsi_steps(b, plate, dh, t, n, forces=None):
     return t, its
 
 
+def e2e_summary(dist, cells, steps, markers, seconds):
+    """The line's e2e object for the whole job: every rank's cell updates over
+    the slowest rank's wall time; the host<->device bytes per step of all
+    ranks (per rank: the FP64 fIn once each way over the K steps, and every
+    step the markers in -- xyz, vel (3 each), area -- and the force out)."""
+    t = max_over_ranks(dist, seconds)
+    updates = sum_over_ranks(dist, float(cells) * steps)
+    h2d = sum_over_ranks(dist, (19.0 * cells * 8 + steps * markers * 7 * 8) / steps)
+    d2h = sum_over_ranks(dist, (19.0 * cells * 8 + steps * markers * 3 * 8) / steps)
+    return {"value": round(updates / t / 1e6, 1), "unit": "MLUPS",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "note": "C-ABI: fsi_block_upload_f (FP64 fIn, pinned host) + K x fsi_block_ib_step (host markers "
+                    "in, Lagrangian force out, IB stage beside the bulk step) + fsi_block_download_f"}
+
+
 def n_face_kernels():
     """face-kernel launches per headline step: every non-periodic face, except
     z faces of code 101 with a uniform face velocity, which the paired bulk
@@ -723,6 +738,7 @@ def main():
             host = np.empty((19, X, Y, Z))
         b = fsi_block(F, F.PREC_F16, dh, nu, plate)
         b.download_f(host)
+        barrier(dist)
         te0 = time.perf_counter()
         b.upload_f(host)
         fsi_steps(b, plate, dh, 0.0, a.steps)
@@ -730,12 +746,7 @@ def main():
         te = time.perf_counter() - te0
         b.close()
         del host
-        M = plate.M
-        e2e = {"value": round(N * a.steps / te / 1e6, 1), "unit": "MLUPS",
-               "h2d_bytes_per_step": int((19 * N * 8 + a.steps * M * 7 * 8) / a.steps),
-               "d2h_bytes_per_step": int((19 * N * 8 + a.steps * M * 3 * 8) / a.steps),
-               "note": "C-ABI: fsi_block_upload_f (FP64 fIn, pinned host) + K x fsi_block_ib_step (host markers "
-                       "in, Lagrangian force out, IB stage beside the bulk step) + fsi_block_download_f"}
+        e2e = e2e_summary(dist, N, a.steps, plate.M, te)
 
     extra = {}
     if not a.no_extra and rank == 0:

@@ -1,5 +1,6 @@
 """The multi-rank path of bench.py (replicas: barrier, max-over-ranks time,
-sum of updates over ranks) with two gloo ranks on the CPU."""
+sum of updates over ranks, the whole-job e2e object) with two gloo ranks on
+the CPU."""
 import os
 import socket
 
@@ -25,7 +26,10 @@ def _worker(rank, world, port, out):
     bench.barrier(dist)
     t = bench.max_over_ranks(dist, 1.0 + rank)        # per-rank time -> the slowest
     n = bench.sum_over_ranks(dist, 100.0 * (rank + 1))  # per-rank updates -> all ranks'
-    out.put((rank, t, n))
+    # the e2e object: both ranks' updates over the slower rank's time, both
+    # ranks' copy bytes
+    e = bench.e2e_summary(dist, 1000000, 10, 5, 1.0 + rank)
+    out.put((rank, t, n, e["value"], e["h2d_bytes_per_step"], e["d2h_bytes_per_step"]))
     dist.destroy_process_group()
 
 
@@ -40,7 +44,17 @@ def test_two_gloo_ranks_replicas():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    assert res == [(0, 2.0, 300.0), (1, 2.0, 300.0)]
+    h2d = 2 * (19 * 1000000 * 8 + 10 * 5 * 7 * 8) // 10
+    d2h = 2 * (19 * 1000000 * 8 + 10 * 5 * 3 * 8) // 10
+    assert res == [(0, 2.0, 300.0, 10.0, h2d, d2h), (1, 2.0, 300.0, 10.0, h2d, d2h)]
+
+
+def test_e2e_summary_one_rank():
+    import bench
+    e = bench.e2e_summary(None, 25165824, 1000, 1089, 0.5)
+    assert e["value"] == round(25165824 * 1000 / 0.5 / 1e6, 1) and e["unit"] == "MLUPS"
+    assert e["h2d_bytes_per_step"] == int((19 * 25165824 * 8 + 1000 * 1089 * 56) / 1000)
+    assert e["d2h_bytes_per_step"] == int((19 * 25165824 * 8 + 1000 * 1089 * 24) / 1000)
 
 
 def test_bench_pins_one_gpu_per_rank():
