@@ -87,3 +87,22 @@ def test_block_descriptor_layout_matches_header():
             m = re.search(r"\*?\s*(\w+)\s*(\[\d+\])?\s*$", part.strip())
             names.append(m.group(1))
     assert names == [f[0] for f in A.BlockDesc._fields_]
+
+
+def test_c_host_builds_against_the_header_and_gets_status_codes(gpu_lib, tmp_path):
+    # the header is plain C (C99, pedantic, warnings as errors); a C program
+    # links the library and reads each refused call's code and message
+    import fsilbm3d_gb300 as F
+    lib = F.library_path()
+    exe = str(tmp_path / "c_host")
+    subprocess.run(["gcc", "-std=c99", "-pedantic", "-Wall", "-Wextra", "-Werror",
+                    "-I" + os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "c_host.c"),
+                    "-o", exe, lib, "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    rows = {l.split(" ", 1)[0]: l.split(" ", 3)[1:] for l in out.stdout.splitlines()}
+    for name in ("create_rbgk", "create_elbm", "create_small", "create_null", "pair_null", "continue_null"):
+        rc, n, msg = rows[name]
+        assert int(rc) == -1 and int(n) == len(msg) > 0, (name, rows[name])
+    assert "RBGK" in rows["create_rbgk"][2] and "ELBM" in rows["create_elbm"][2]
+    assert rows["destroy_null"][0] == "0"
