@@ -14,11 +14,26 @@
 #include <algorithm>
 #include <mutex>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/fsi_gpu.h"
 #include "fsi_kernels.h"
 #include "mlp_impl.cuh"
 
 using namespace fsi;
+
+namespace {
+// One NVTX range per call of the entry points a time loop makes, named after
+// the function, so that a profiler's timeline shows the host side of every
+// step beside its kernels (a no-op when no profiler is attached).
+struct CallRange {
+    explicit CallRange(const char *name) { nvtxRangePushA(name); }
+    ~CallRange() { nvtxRangePop(); }
+    CallRange(const CallRange &) = delete;
+    CallRange &operator=(const CallRange &) = delete;
+};
+}  // namespace
+#define FSI_CALL_RANGE() CallRange fsi_call_range_(__func__)
 
 static_assert(FSI_MLP_IN == MLP_IN && FSI_MLP_OUT == MLP_OUT, "perceptron shape");
 static_assert(FSI_MLP_NPARAM == MLP_NP && FSI_MLP_NNORM == MLP_NNORM, "perceptron sizes");
@@ -633,6 +648,7 @@ int fsi_block_get_tau_all(fsi_block_t h, double *tau_all) {
 }
 
 int fsi_block_upload_f(fsi_block_t h, const double *fIn) {
+    FSI_CALL_RANGE();
     if (!h || !fIn) return fail(FSI_E_ARG, "null argument");
     size_t n = 19 * (size_t)h->N;
     if (h->esz == 8) {
@@ -646,6 +662,7 @@ int fsi_block_upload_f(fsi_block_t h, const double *fIn) {
 }
 
 int fsi_block_download_f(fsi_block_t h, double *fIn) {
+    FSI_CALL_RANGE();
     if (!h || !fIn) return fail(FSI_E_ARG, "null argument");
     size_t n = 19 * (size_t)h->N;
     if (h->esz == 8) {
@@ -660,6 +677,7 @@ int fsi_block_download_f(fsi_block_t h, double *fIn) {
 // ---------------------------------------------------------------- restart
 
 int fsi_continue_write(const char *path, const fsi_block_t *blocks, int n, int step, double time) {
+    FSI_CALL_RANGE();
     if (!path || !blocks || n <= 0) return fail(FSI_E_ARG, "invalid argument");
     for (int i = 0; i < n; i++)
         if (!blocks[i]) return fail(FSI_E_ARG, "null block %d", i);
@@ -689,6 +707,7 @@ int fsi_continue_write(const char *path, const fsi_block_t *blocks, int n, int s
 }
 
 int fsi_continue_read(const char *path, const fsi_block_t *blocks, int n, int *step, double *time) {
+    FSI_CALL_RANGE();
     if (!path || !blocks || n <= 0) return fail(FSI_E_ARG, "invalid argument");
     for (int i = 0; i < n; i++)
         if (!blocks[i]) return fail(FSI_E_ARG, "null block %d", i);
@@ -819,6 +838,7 @@ int out_scratch(fsi_block *h, size_t bytes) {
 }  // namespace
 
 int fsi_block_pack_flow(fsi_block_t h, const double vf[3], double denIn, double Uref, int offset, float *out) {
+    FSI_CALL_RANGE();
     if (!h || !out) return fail(FSI_E_ARG, "null argument");
     if (!(Uref != 0.0)) return fail(FSI_E_ARG, "Uref must be nonzero");
     if (offset < 0 || 2 * offset >= h->X || 2 * offset >= h->Y || 2 * offset >= h->Z)
@@ -832,6 +852,7 @@ int fsi_block_pack_flow(fsi_block_t h, const double vf[3], double denIn, double 
 }
 
 int fsi_block_flux(fsi_block_t h, const double vf[3], double denIn, double Uref, double flux[3]) {
+    FSI_CALL_RANGE();
     if (!h || !flux) return fail(FSI_E_ARG, "null argument");
     if (int rc = macro_device(h, vf)) return rc;
     if (int rc = out_scratch(h, sizeof(double) * 3)) return rc;
@@ -845,6 +866,7 @@ int fsi_block_flux(fsi_block_t h, const double vf[3], double denIn, double Uref,
 }
 
 int fsi_block_probes(fsi_block_t h, const double vf[3], int n, const double *xyz, double Uref, double *uvw) {
+    FSI_CALL_RANGE();
     if (!h || n < 0 || (n > 0 && (!xyz || !uvw))) return fail(FSI_E_ARG, "invalid argument");
     if (n == 0) return FSI_OK;
     const double xmax = h->d.xmin + h->d.dh * (h->X - 1), ymax = h->d.ymin + h->d.dh * (h->Y - 1),
@@ -879,6 +901,7 @@ int fsi_block_initialise(fsi_block_t h, double time) {
 }
 
 int fsi_block_set_boundary_conditions(fsi_block_t h, double blktime) {
+    FSI_CALL_RANGE();
     if (!h) return fail(FSI_E_ARG, "null handle");
     int rc = apply_bcs(h, h->fa, blktime);
     if (rc) return rc;
@@ -887,6 +910,7 @@ int fsi_block_set_boundary_conditions(fsi_block_t h, double blktime) {
 }
 
 int fsi_block_macro(fsi_block_t h, const double vf[3], double *den, double *uuu) {
+    FSI_CALL_RANGE();
     if (!h) return fail(FSI_E_ARG, "null handle");
     double z3[3] = {0, 0, 0};
     const double *v = vf ? vf : z3;
@@ -901,6 +925,7 @@ int fsi_block_macro(fsi_block_t h, const double vf[3], double *den, double *uuu)
 }
 
 int fsi_block_step(fsi_block_t h, const double vf[3], double blktime) {
+    FSI_CALL_RANGE();
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
     int rc = enqueue_step(h, vf, blktime, true);
     h->win_valid = false;
@@ -942,6 +967,7 @@ int fsi_block_timer(fsi_block_t h, int stop, float *ms) {
 }
 
 int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps, float *ms) {
+    FSI_CALL_RANGE();
     if (!h || !vf || nsteps < 0) return fail(FSI_E_ARG, "invalid argument");
     h->win_valid = false;
     // a captured pair of steps is valid when no kernel argument changes from
@@ -1267,6 +1293,7 @@ int ib_upload(fsi_block *h, const double *xyz, const double *vel, const double *
 int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
                  double denIn, double dt, double Uref, int ntol, double dtol, double *eforce, int *iters,
                  double *residual) {
+    FSI_CALL_RANGE();
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
     h->win_valid = false;
     if (iters) *iters = 0;
@@ -1329,6 +1356,7 @@ int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const doub
 int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double *aux,
                       const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol, fsi_mlp_t warm,
                       float *features, double *eforce, int *iters, double *residual) {
+    FSI_CALL_RANGE();
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
     if (h->prec == FSI_PREC_F64)
         return fail(FSI_E_ARG, "the warm start needs a fast form; FSI_PREC_F64 keeps the reference's iteration");
@@ -1367,6 +1395,7 @@ int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const
 int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
                       double denIn, double dt, double Uref, int ntol, double dtol, double blktime, double *eforce,
                       int *iters, double *residual) {
+    FSI_CALL_RANGE();
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
     if (h->prec == FSI_PREC_F64 || h->nb == 0 || h->Mtot == 0) {
         int rc = fsi_ib_solve(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, eforce, iters, residual);
@@ -1510,6 +1539,7 @@ int pair_check(fsi_pair *p) {
 extern "C" {
 
 int fsi_pair_extract(fsi_pair_t p, int time_level) {
+    FSI_CALL_RANGE();
     if (!p || (time_level != 1 && time_level != 2)) return fail(FSI_E_ARG, "invalid argument");
     fsi_block *fa = p->fa;
     for (int k = 0; k < 6; k++) {
@@ -1528,6 +1558,7 @@ int fsi_pair_extract(fsi_pair_t p, int time_level) {
 }
 
 int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]) {
+    FSI_CALL_RANGE();
     if (!p || !vf) return fail(FSI_E_ARG, "invalid argument");
     fsi_block *so = p->so, *fa = p->fa;
     CK(cudaStreamSynchronize(fa->st));
@@ -1542,6 +1573,7 @@ int fsi_pair_father_to_son(fsi_pair_t p, int n_timeStep, const double vf[3]) {
 }
 
 int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]) {
+    FSI_CALL_RANGE();
     if (!p || !vf) return fail(FSI_E_ARG, "invalid argument");
     fsi_block *so = p->so, *fa = p->fa;
     CK(cudaStreamSynchronize(so->st));
@@ -1723,6 +1755,7 @@ int fsi_mlp_grad(fsi_mlp_t m, const float *x, const float *y, int n, float *grad
 
 int fsi_mlp_train(fsi_mlp_t m, const float *x, const float *y, int n, int epochs, int batch, float lr,
                   unsigned long long seed, float *loss_per_epoch) {
+    FSI_CALL_RANGE();
     if (!m || n <= 0 || !x || !y || epochs <= 0 || batch <= 0 || !(lr > 0.0f))
         return fail(FSI_E_ARG, "invalid argument");
     if (!m->norm_set) return fail(FSI_E_STATE, "network statistics not set (fsi_mlp_set_norm)");
@@ -2013,6 +2046,7 @@ int fsi_batch_destroy(fsi_batch_t b) {
 int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const double *area, const double *vf,
                       const double *denIn, const double *dt, const double *Uref, int ntol, double dtol,
                       const double *blktime, double *eforce, int *iters, double *residual) {
+    FSI_CALL_RANGE();
     if (!b || !vf || !denIn || !dt || !Uref || !blktime || ntol < 0) return fail(FSI_E_ARG, "null argument");
     if (b->Mall > 0 && (!xyz || !vel || !area || !eforce)) return fail(FSI_E_ARG, "null marker array");
     const int n = b->n;
@@ -2104,6 +2138,7 @@ int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const
 }
 
 int fsi_batch_tune(fsi_batch_t b, int reps, int *threads, float *ms_per_step) {
+    FSI_CALL_RANGE();
     if (!b || reps <= 0) return fail(FSI_E_ARG, "invalid argument");
     // the bulk step of every block, fa -> fb without swapping: the state does
     // not change (fb is rewritten by the next step)
@@ -2178,6 +2213,7 @@ int static_scratch(double **out) {
 }  // namespace
 
 extern "C" int fsi_pair_father_to_son_static(fsi_pair_t p, int n_timeStep, const double vf[3]) {
+    FSI_CALL_RANGE();
     if (!p || !vf) return fail(FSI_E_ARG, "invalid argument");
     fsi_block *so = p->so, *fa = p->fa;
     for (int k = 0; k < 6; k++) {
