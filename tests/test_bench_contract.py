@@ -51,3 +51,24 @@ def test_cpu_baseline_leg(monkeypatch):
     assert set(cb) == {"value", "unit", "cores", "kind", "sample"}
     assert cb["value"] > 0 and cb["unit"] == "MLUPS" and cb["cores"] == 2 and cb["kind"] == "port"
     assert "build" in cb["sample"] and "steps" in cb["sample"]
+
+
+def test_algorithmic_bytes_per_update():
+    # one read and one write of the 19 populations, plus each model's fields
+    import bench
+    for s in (8, 4, 2):
+        assert bench.model_bytes(1, s, "f16") == bench.model_bytes(3, s, "f16") == 38 * s
+    assert bench.model_bytes(11, 2, "f16") == 80       # + tau_all written (FP32)
+    assert bench.model_bytes(15, 2, "f16") == 146      # + velocity pass, gradient pass, tau_all read
+    assert bench.model_bytes(14, 2, "f16") == 170      # + rotation entries, tau_all read and written
+    assert bench.model_bytes(11, 8, "f64") == 312
+    assert bench.model_bytes(15, 8, "f64") == 304 + 152 + 32 + 24 + 8
+
+
+def test_headline_launches_per_step():
+    # IB stage, bulk step, IB-window fix-up, and one launch per axis whose two
+    # faces need a face kernel (x: 101/104, y: 101/101; the z faces of code
+    # 101 are written by the bulk kernel)
+    import bench
+    assert bench.BND == (101, 104, 101, 101, 101, 101)
+    assert bench.n_face_kernels() == 2
