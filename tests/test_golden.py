@@ -3,7 +3,10 @@
 CPU: the oracle replays every case and must reproduce the stored states
 bitwise (SHA-256 of the FP64 bytes after the initial boundary call and after
 each step) -- this pins the oracle. GPU: the exact FP64 path replays the same
-cases through the C-ABI and must match the same digests.
+cases through the C-ABI and must match the same digests. The aux_* vectors
+(make_golden_aux.py) pin the oracle's refinement exchange, output arithmetic
+and continue re-grid on the CPU; the GPU tests of those paths compare with
+the oracle live.
 """
 import os
 import sys
@@ -15,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 
 import make_golden as G  # noqa: E402
+import make_golden_aux as GA  # noqa: E402
 import oracle as O  # noqa: E402
 
 
@@ -74,3 +78,18 @@ def test_gpu_exact_matches_golden(gpu_lib, name):
     if spec.get("plate"):
         ei, ew = b.ib_stencil()
         assert np.array_equal(ei, ref["ei"]) and ew.tobytes() == ref["ew"].tobytes()
+
+
+@pytest.mark.parametrize("name", sorted(GA.CASES))
+def test_oracle_reproduces_aux_golden(name):
+    # refinement exchange, output arithmetic and continue re-grid of the
+    # oracle, bitwise against the committed vectors (CPU only)
+    ref = load(name)
+    out = GA.CASES[name]()
+    assert sorted(out) == sorted(ref)
+    for k in ref:
+        a, b = np.asarray(out[k]), np.asarray(ref[k])
+        if k.startswith("sha_"):
+            assert str(a) == str(b), (name, k)
+        else:
+            assert a.shape == b.shape and a.dtype == b.dtype and a.tobytes() == b.tobytes(), (name, k)
