@@ -6,6 +6,11 @@ the library, mirrors the reference's block and body interfaces
 (FluidDomain.f90 LBMBlock, Solidbody.f90 VirtualBody) and the per-step
 orchestration of LBMBlockComm.f90:279-338.
 
+Modules: abi (the ctypes binding: Block, Pair, Mlp, Batch), bodies (rigid
+plate markers, Solidbody.f90:604-646), inflow (the fluid sections of the
+reference's inFlow.dat), d3q19 (lattice tables), build (the in-tree nvcc
+build).
+
 There is no CPU fallback: if the CUDA library cannot be loaded, or no GPU is
 present, every compute call raises.
 """
