@@ -455,12 +455,14 @@ void or_halfway_set(or_block *b) {
 }
 
 /* streaming_, FluidDomain.f90:1514-1625: every population shifts by e_i with
- * periodic wrap in all three axes. A pull copy through tmp moves the same
- * values as the reference's in-place cyclic shifts. */
+ * periodic wrap in all three axes. A pull copy through tmp and back moves the
+ * same values as the reference's in-place cyclic shifts, with the same two
+ * passes over each moving population, shared among the threads by x-slabs as
+ * the reference's OpenMP loops are; the rest population (q = 0) stays. */
 void or_stream(or_block *b, double *tmp) {
-    size_t n = ncell(b);
+    size_t n = ncell(b), slab = (size_t)b->Y * b->Z;
     int X = b->X, Y = b->Y, Z = b->Z;
-    for (int q = 0; q < Q; q++) {
+    for (int q = 1; q < Q; q++) {
         #pragma omp parallel for schedule(static)
         for (int x = 0; x < X; x++) {
             int xs = (x - EX[q] + X) % X;
@@ -472,8 +474,10 @@ void or_stream(or_block *b, double *tmp) {
                 }
             }
         }
+        #pragma omp parallel for schedule(static)
+        for (int x = 0; x < X; x++)
+            memcpy(b->f + n * q + slab * x, tmp + n * q + slab * x, sizeof(double) * slab);
     }
-    memcpy(b->f, tmp, sizeof(double) * n * Q);
 }
 
 /* velocity point of face cell (a,b) of face k, shifted outward by `off` */
