@@ -20,11 +20,14 @@ Restated behaviour (file:line of the reference):
     blanks or commas, ``r*c`` repeats, ``r*`` null values, '/' ends the
     record, D exponents); items beyond those a read asks for are ignored.
 Sections: Parallel and FlowCondition (read_flow_conditions,
-FlowCondition.f90:31-77), FluidBlocks (read_fuild_blocks,
-FluidDomain.f90:61-108, with check_periodic_boundary_ :110-126), ProbingFluid
-and ProbingSolid (read_probe_params, FlowCondition.f90:79-113). The
-reference scales of calculate_reference_params (Solidbody.f90:219-284) are
-computed for the choices that need no solid body.
+FlowCondition.f90:31-77), the global lines of SolidBody (read_solid_files,
+Solidbody.f90:100-115: penalty and structural-solver globals, the number of
+bodies and groups; the bodies' own entries and mesh files are not read),
+FluidBlocks (read_fuild_blocks, FluidDomain.f90:61-108, with
+check_periodic_boundary_ :110-126), ProbingFluid and ProbingSolid
+(read_probe_params, FlowCondition.f90:79-113). The reference scales of
+calculate_reference_params (Solidbody.f90:219-284) are computed for the
+choices that need no body data (or only the chord, when given).
 
 Like the reference, a malformed file stops the run: here with
 InFlowError.
@@ -175,6 +178,22 @@ class FlowConditions:
 
 
 @dataclass
+class SolidGlobals:
+    """the global lines of the SolidBody section (Solidbody.f90:100-115)"""
+    IBPenaltyAlpha: float = 1.0
+    GeoGamma: float = 0.0
+    NewmarkGamma: float = 0.0
+    NewmarkBeta: float = 0.0
+    dampK: float = 0.0
+    dampM: float = 0.0
+    dtolFEM: float = 0.0
+    ntolFEM: int = 0
+    nFish: int = 0
+    nGroup: int = 0
+    isKB: int = 0
+
+
+@dataclass
 class FluidBlock:
     """one entry of the FluidBlocks section (FluidDomain.f90:75-84)"""
     ID: int
@@ -217,6 +236,19 @@ def _flow(r, fc):
     (fc.interpolateScheme,) = _read(r.next_data(), "i", "interpolateScheme")
 
 
+def _solid(r):
+    r.find("SolidBody")
+    sg = SolidGlobals()
+    sg.IBPenaltyAlpha, sg.GeoGamma = _read(r.next_data(), "rr", "IBPenaltyAlpha, GeoGamma")
+    sg.NewmarkGamma, sg.NewmarkBeta = _read(r.next_data(), "rr", "NewmarkGamma, NewmarkBeta")
+    sg.dampK, sg.dampM = _read(r.next_data(), "rr", "dampK, dampM")
+    sg.dtolFEM, sg.ntolFEM = _read(r.next_data(), "ri", "dtolFEM, ntolFEM")
+    sg.nFish, sg.nGroup, sg.isKB = _read(r.next_data(), "iii", "nFish, nGroup, isKB")
+    if not sg.IBPenaltyAlpha > 1e-6:
+        raise InFlowError("ERROR: IBPenaltyalpha should be positive (default 1) %g" % sg.IBPenaltyAlpha)
+    return sg
+
+
 def _blocks(r):
     r.find("FluidBlocks")
     (n,) = _read(r.next_data(), "i", "number of blocks")
@@ -257,15 +289,19 @@ def _probes(r, fc):
     fc.solidProbingNode = [_read(r.next_data(), "i", "solid probe")[0] for _ in range(max(0, fc.solidProbingNum))]
 
 
-def reference_scales(fc, nbodies=0):
+def reference_scales(fc, nbodies=0, lchod=None):
     """calculate_reference_params (Solidbody.f90:219-284) for the choices
-    that need no solid body: Lref (type 0 without bodies: 1), Uref (types
-    0-4, or the input value for types above 7), Tref (type 0 or the input),
-    then nu = Uref Lref / Re. Types that read the bodies raise."""
+    that need no body data: Lref (type 0: 1 without bodies, the chord Lchod
+    with bodies, which the caller passes), Uref (types 0-4, or the input
+    value for types above 7), Tref (type 0 or the input), then
+    nu = Uref Lref / Re. Choices that read the bodies' motion raise."""
     if fc.LrefType == 0:
         if nbodies:
-            raise InFlowError("LrefType 0 with bodies takes Lchod from the solid input")
-        fc.Lref = 1.0
+            if lchod is None:
+                raise InFlowError("LrefType 0 with bodies takes the chord Lchod of the solid input: pass lchod")
+            fc.Lref = float(lchod)
+        else:
+            fc.Lref = 1.0
     u = fc.uvwIn
     if fc.UrefType == 0:
         fc.Uref = abs(u[0])
@@ -293,6 +329,7 @@ def reference_scales(fc, nbodies=0):
 class InFlow:
     flow: FlowConditions
     blocks: List[FluidBlock]
+    solid: SolidGlobals
 
     def block_kwargs(self, i, precision=None):
         """keyword arguments of fsilbm3d_gb300.Block for block i (an index
@@ -310,17 +347,20 @@ class InFlow:
         return kw
 
 
-def read_inflow(path, probes=True, scales=True):
-    """The fluid sections of inFlow.dat at `path`: flow conditions, blocks
-    (and probes); with scales, the body-free reference scales and nu."""
+def read_inflow(path, probes=True, scales=True, lchod=None):
+    """The fluid sections of inFlow.dat at `path` in the reference's order
+    (main.f90:29-32): flow conditions, the SolidBody globals, blocks (and
+    probes); with scales, the reference scales and nu (lchod: the bodies'
+    chord, for LrefType 0 with bodies)."""
     with open(path) as fh:
         lines = fh.read().splitlines()
     r = _Reader(lines)
     fc = FlowConditions()
     _flow(r, fc)
+    solid = _solid(r)
     blocks = _blocks(r)
     if probes:
         _probes(r, fc)
     if scales:
-        reference_scales(fc)
-    return InFlow(fc, blocks)
+        reference_scales(fc, nbodies=solid.nFish, lchod=lchod)
+    return InFlow(fc, blocks, solid)

@@ -40,7 +40,11 @@ FluidBlocks
 0 0 0 0 0 0
 0.1875 9*0.0 / ignored tail
 SolidBody
-0
+1.0 0.5
+0.5 0.25
+0.0 0.0
+1.0e-6 20
+0 0 1
 ProbingFluid
 2 1
 0.5 1.5 1.0
@@ -65,6 +69,8 @@ def test_reads_flow_blocks_and_probes(tmp_path):
     assert (fc.Re, fc.denIn) == (200.0, 1.0) and fc.uvwIn == (0.05, 0.0, 0.0)
     assert fc.volumeForceIn == (0.0, 0.0, 1.5e-6)
     assert (fc.UrefType, fc.ntolLBM, fc.dtolLBM, fc.interpolateScheme) == (0, 5, 1e-4, 2)
+    assert inf.solid.IBPenaltyAlpha == 1.0 and (inf.solid.nFish, inf.solid.nGroup, inf.solid.isKB) == (0, 0, 1)
+    assert (inf.solid.dtolFEM, inf.solid.ntolFEM) == (1e-6, 20)
     assert fc.fluidProbingNum == 2 and fc.inWhichBlock == 1
     assert fc.fluidProbingCoords == [(0.5, 1.5, 1.0), (1.0, 1.5, 0.5)]
     assert fc.solidProbingNum == 1 and fc.solidProbingNode == [7]
@@ -112,6 +118,8 @@ def test_keyword_match_is_the_references(tmp_path, header, found):
     (("0 0.05\n5 1.0e-4", "5 0.05\n5 1.0e-4"), "UrefType 5"),
     (("==========\n", "----------\n"), "readequal"),
     (("1 3 1 0", "1 3.5 1 0"), "cannot read"),
+    (("1.0 0.5\n0.5 0.25", "0.0 0.5\n0.5 0.25"), "IBPenaltyalpha"),
+    (("0 0 1\n", "2 1 1\n"), "pass lchod"),                 # bodies, LrefType 0, no chord given
 ])
 def test_malformed_files_stop(tmp_path, edit, msg):
     with pytest.raises(I.InFlowError, match=msg):
@@ -122,3 +130,8 @@ def test_list_directed_items():
     assert I._items("1, 2  3*0.5 , 2* / tail 9") == ["1", "2", "0.5", "0.5", "0.5", None, None]
     assert I._items("   ") == [] and I._items("a,,b") == ["a", None, "b"]
     assert I._read("1.d0 2.5D-3 7", "rri", "x") == [1.0, 2.5e-3, 7]
+
+
+def test_chord_sets_the_reference_length_with_bodies(tmp_path):
+    inf = I.read_inflow(write(tmp_path, CASE.replace("0 0 1\n", "2 1 1\n", 1)), lchod=2.0)
+    assert inf.solid.nFish == 2 and inf.flow.Lref == 2.0 and inf.flow.nu == 0.05 * 2.0 / 200.0
