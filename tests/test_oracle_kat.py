@@ -307,3 +307,30 @@ def test_continue_regrid_is_linear_exact():
     for q in range(19):
         want = 0.1 + 0.01 * q + 0.003 * xb - 0.002 * yb + 0.001 * zb
         assert np.max(np.abs(b.fview()[q][inside] - want[inside])) < 1e-15
+
+
+def test_faces_applied_in_order_last_writer_at_edges():
+    # set_boundary_conditions_ applies x-, x+, y-, y+, z-, z+ in turn
+    # (FluidDomain.f90:616-1126), so an edge cell keeps the last face's
+    # values: with an equilibrium inflow (101) on x- and stationary walls
+    # (201, f_i = f_opp(i) for the face's incoming set) on z- and z+, the
+    # edge cells x = 0, z = 0 / Z-1 hold the inflow equilibrium with each
+    # z face's incoming populations bounced back from it
+    X, Y, Z = 8, 6, 5
+    u_in = (0.05, 0.01, -0.02)
+    fl = O.make_flow(uvwIn=u_in, nu=0.02)
+    b = O.Block(X, Y, Z, 1.0, (0, 0, 0), [101, 104, 301, 301, 201, 201], 1, fl)
+    b.initialise(0.0)
+    f = b.fview()
+    f[...] = f + 1e-3 * np.arange(Q)[:, None, None, None]  # no longer an equilibrium anywhere
+    b.set_bc()
+    f = b.fview()
+    eq = O.feq(1.0, u_in)
+    opp = [0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15]
+    for z, incoming in ((0, (5, 11, 12, 15, 16)), (Z - 1, (6, 13, 14, 17, 18))):
+        expect = np.array([eq[opp[i]] if i in incoming else eq[i] for i in range(Q)])
+        for y in range(Y):
+            assert np.array_equal(f[:, 0, y, z], expect), (y, z)
+    # inside the x- face (away from the z faces) the inflow equilibrium alone
+    for z in range(1, Z - 1):
+        assert np.array_equal(f[:, 0, 2, z], eq)
