@@ -334,3 +334,33 @@ def test_faces_applied_in_order_last_writer_at_edges():
     # inside the x- face (away from the z faces) the inflow equilibrium alone
     for z in range(1, Z - 1):
         assert np.array_equal(f[:, 0, 2, z], eq)
+
+
+def test_neq_face_uses_the_stored_second_layer_moments():
+    # code 102 (FluidDomain.f90:633-647): the incoming populations become
+    # feq(denIn, u_in) + (f(layer 2) - feq(den, uuu of layer 2)), with den and
+    # uuu the block's stored fields -- in a step, the pre-collision,
+    # IB-corrected moments -- not moments recomputed from the streamed f
+    X, Y, Z = 7, 5, 4
+    u_in = (0.04, 0.0, 0.01)
+    fl = O.make_flow(uvwIn=u_in, nu=0.02)
+    b = O.Block(X, Y, Z, 1.0, (0, 0, 0), [102, 103, 301, 301, 301, 301], 1, fl)
+    rng = np.random.default_rng(3)
+    f = b.fview()
+    f[...] = (np.array(O.feq(1.0, (0.02, 0.0, 0.0)))[:, None, None, None]
+              * (1.0 + 0.05 * rng.random((Q, X, Y, Z))))
+    den = b.den.reshape(X, Y, Z)
+    u = b.u.reshape(3, X, Y, Z)
+    den[1] = 1.02                       # layer 2: moments that f does not imply
+    u[:, 1] = np.array([0.03, -0.01, 0.02])[:, None, None]
+    before = f.copy()
+    b.set_bc()
+    f = b.fview()
+    eq_in = O.feq(1.0, u_in)
+    eq2 = O.feq(1.02, (0.03, -0.01, 0.02))
+    incoming = (1, 7, 9, 11, 13)
+    for y in range(Y):
+        for z in range(Z):
+            for i in range(Q):
+                want = eq_in[i] + (before[i, 1, y, z] - eq2[i]) if i in incoming else before[i, 0, y, z]
+                assert f[i, 0, y, z] == want, (i, y, z)
