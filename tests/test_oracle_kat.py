@@ -364,3 +364,36 @@ def test_neq_face_uses_the_stored_second_layer_moments():
             for i in range(Q):
                 want = eq_in[i] + (before[i, 1, y, z] - eq2[i]) if i in incoming else before[i, 0, y, z]
                 assert f[i, 0, y, z] == want, (i, y, z)
+
+
+def test_macro_takes_half_the_volume_force_and_not_the_ib_force():
+    # calculate_macro_quantities_ (FluidDomain.f90:1128-1145): den = sum f,
+    # u = (sum f e + 0.5 F_vol dh) / den; the force field (IB and volume
+    # force, which the collision uses) does not enter
+    X, Y, Z = 4, 3, 3
+    fl = O.make_flow(nu=0.02, volumeForceIn=(2e-4, -1e-4, 5e-5))
+    b = O.Block(X, Y, Z, 0.5, (0, 0, 0), [301] * 6, 1, fl)
+    rng = np.random.default_rng(8)
+    f = b.fview()
+    f[...] = 0.05 * (1.0 + rng.random((Q, X, Y, Z)))
+    b.b.volumeForce[:] = [2e-4, -1e-4, 5e-5]
+    b.force[:] = 1.0e3
+    b.macro()
+    ex = [0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0]
+    ey = [0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1]
+    ez = [0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1]
+    den = b.den.reshape(X, Y, Z)
+    u = b.u.reshape(3, X, Y, Z)
+    for x in range(X):
+        for y in range(Y):
+            for z in range(Z):
+                fc = [float(f[q, x, y, z]) for q in range(Q)]
+                d = 0.0  # plain left-to-right sums, as SUM runs (Python's sum() compensates)
+                for v in fc:
+                    d += v
+                assert den[x, y, z] == d
+                for k, e in enumerate((ex, ey, ez)):
+                    m = 0.0
+                    for q in range(Q):
+                        m += fc[q] * e[q]
+                    assert u[k, x, y, z] == (m + (0.5 * b.b.volumeForce[k]) * 0.5) / d
