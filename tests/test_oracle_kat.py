@@ -397,3 +397,20 @@ def test_macro_takes_half_the_volume_force_and_not_the_ib_force():
                     for q in range(Q):
                         m += fc[q] * e[q]
                     assert u[k, x, y, z] == (m + (0.5 * b.b.volumeForce[k]) * 0.5) / d
+
+
+def test_volume_force_wave():
+    # update_volume_force_ (FluidDomain.f90:1174-1180): x component
+    # In + Amp sin(2 pi f t + phi/180 pi), y and z the inputs; Pi as
+    # ConstParams.f90:36
+    import ctypes
+    import math
+    PI = 3.141592653589793
+    fl = O.make_flow(nu=0.02, volumeForceIn=(1e-4, 2e-5, -3e-5), volumeForceAmp=5e-5, volumeForceFreq=0.125,
+                     volumeForcePhi=30.0)
+    b = O.Block(3, 3, 3, 1.0, (0, 0, 0), [301] * 6, 1, fl)
+    for t in (0.0, 1.0, 7.25, 123.5):
+        b.b.blktime = t
+        O.lib().or_update_volume_force(ctypes.byref(b.b), ctypes.byref(fl))
+        want = 1e-4 + 5e-5 * math.sin(((2.0 * PI) * 0.125) * t + (30.0 / 180.0) * PI)
+        assert list(b.b.volumeForce) == [want, 2e-5, -3e-5]
