@@ -1443,6 +1443,14 @@ int fsi_ib_get_window(fsi_block_t h, int box[6]) {
 
 // ---------------------------------------------------------- block refinement
 
+}  // extern "C"
+
+namespace {
+int static_scratch(double **out);  // the allocation-free variant's scratch, end of this file
+}  // namespace
+
+extern "C" {
+
 int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme) {
     if (!out || !fa || !so) return fail(FSI_E_ARG, "null argument");
     *out = nullptr;
@@ -1473,6 +1481,29 @@ int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme)
         delete p;
         return fail(FSI_E_ARG, "son block does not lie inside its father");
     }
+    // interpolate_fIn (LBMBlockComm.f90:808-956) reads father face node
+    // (n+1)/2 for the last odd son node n of a face direction, and the
+    // third/fourth-order stencil reaches three son nodes and two father nodes
+    // past its own: on narrower faces (son faces under 5 nodes a side, or a
+    // son periodic along an odd face direction) the reference reads outside
+    // its face arrays. Such pairs are refused here rather than left to read
+    // whatever lies next to the face.
+    for (int k = 0; k < 6; k++) {
+        if (so->d.bndConds[k] != BC_FLUID) continue;
+        int ax = k >> 1;
+        int AF = ax == 2 ? g.yDimF : g.zDimF, BF = ax == 0 ? g.yDimF : g.xDimF;
+        int AS = ax == 2 ? g.yDimS : g.zDimS, BS = ax == 0 ? g.yDimS : g.xDimS;
+        int AO = (AS % 2) ? AS : AS - 1, BO = (BS % 2) ? BS : BS - 1;  // last odd son node
+        bool ok = (AO + 1) / 2 <= AF && (BO + 1) / 2 <= BF;
+        if (scheme == 2) ok = ok && AS >= 5 && BS >= 5;
+        if (!ok) {
+            delete p;
+            return fail(FSI_E_ARG,
+                        "son face %d (%d x %d nodes, father %d x %d) is too narrow for interpolation scheme %d: "
+                        "the reference's stencil would read outside the face",
+                        k, AS, BS, AF, BF, scheme);
+        }
+    }
     size_t maxS = 0;
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 6; k++) {
@@ -1497,6 +1528,16 @@ int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme)
     if (e != cudaSuccess) {
         fsi_pair_destroy(p);
         return fail(FSI_E_CUDA, "pair allocation: %s", cudaGetErrorString(e));
+    }
+    // Place the static scratch of fsi_pair_father_to_son_static on this device
+    // now, at set-up: under lazy module loading the array's module (and its
+    // memory) would otherwise load at the first static call, inside the
+    // host's time loop.
+    double *scr = nullptr;
+    int rc = static_scratch(&scr);
+    if (rc) {
+        fsi_pair_destroy(p);
+        return rc;
     }
     *out = p;
     return FSI_OK;
@@ -2187,15 +2228,17 @@ int fsi_batch_set_threads(fsi_batch_t b, int threads) {
 // ------------------------------------------------- allocation-free variant
 // Scratch of fsi_pair_father_to_son_static: the interpolated son face
 // (19 populations per face cell) followed by its interpolated tau, for at
-// most FSI_STATIC_FACE_CELLS face cells. Each device that loads the library
-// holds this array until the process exits.
+// most FSI_STATIC_FACE_CELLS face cells. A device holds this array from the
+// first fsi_pair_create on it (which looks up its address) until the process
+// exits.
 static __device__ __align__(256) double g_pair_face_scratch[20LL * FSI_STATIC_FACE_CELLS];
 
 namespace {
 std::mutex g_scratch_mu;
 double *g_scratch_ptr[256] = {};  // device address of the array, per device
 
-// looked up once per device, with that device current
+// looked up once per device, with that device current (fsi_pair_create
+// does it, so the static calls that follow find it resolved)
 int static_scratch(double **out) {
     int dev = 0;
     CK(cudaGetDevice(&dev));

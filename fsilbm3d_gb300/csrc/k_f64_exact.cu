@@ -1049,9 +1049,13 @@ cudaError_t launch_pair_f2s(void *fs, int prec, int SX, int SY, int SZ, TauSrc t
     else if (ax == 1) { AF = p.zDimF; BF = p.xDimF; AS = p.zDimS; BS = p.xDimS; }
     else { AF = p.yDimF; BF = p.xDimF; AS = p.yDimS; BS = p.xDimS; }
     const long long nF = (long long)AF * BF;
-    if ((long long)AS * BS > scratch_cells) return cudaErrorInvalidValue;
-    k_pair_interp<<<1, 32, 0, st>>>(Q, AF, buf, Q * nF, AS, BS, scratch_f, Q * scratch_cells, scheme, err);
-    k_pair_interp<<<1, 32, 0, st>>>(1, AF, buft, nF, AS, BS, scratch_t, scratch_cells, 1, err);
+    // the interpolation is bounded by this face's own cells, not by the
+    // scratch's capacity: a read past the face is reported, never served from
+    // what an earlier (larger) face left in the scratch
+    const long long nS = (long long)AS * BS;
+    if (nS > scratch_cells) return cudaErrorInvalidValue;
+    k_pair_interp<<<1, 32, 0, st>>>(Q, AF, buf, Q * nF, AS, BS, scratch_f, Q * nS, scheme, err);
+    k_pair_interp<<<1, 32, 0, st>>>(1, AF, buft, nF, AS, BS, scratch_t, nS, 1, err);
     FSI_PAIR_DISPATCH(prec, k_pair_f2s_apply<PP><<<dim3((AS + 63) / 64, BS), 64, 0, st>>>(
                                 fs, SY, SZ, (long long)SX * SY * SZ, ts, p, face, scratch_f, scratch_t, AS, BS, vf[0],
                                 vf[1], vf[2], dh, err))

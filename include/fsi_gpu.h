@@ -8,7 +8,7 @@
  * LBMBlockComm.f90:279-338. Each entry point below replaces the body of one
  * or more of those procedures; the comment on each names the reference
  * routine (file:line) it stands in for. A Fortran host binds these through
- * ISO_C_BINDING; any C, C++ or Python (ctypes) host can
+ * an ISO_C_BINDING interface module; any C, C++ or Python (ctypes) host can
  * call them directly.
  *
  * Conventions
@@ -326,14 +326,17 @@ int fsi_pair_son_to_father(fsi_pair_t p, const double vf[3]);
  * from its stepping code -- since fsi_pair_father_to_son interpolates the
  * father's face into scratch planes that fsi_pair_create allocated. This
  * variant allocates nothing: its scratch is one file-scope device array of
- * FSI_STATIC_FACE_CELLS son face cells (20 doubles each, 10 MiB, held by
- * every GPU that loads the library until the process exits). Faces larger
- * than that return FSI_E_ARG. The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture. All calls share the one array and each call leaves its
- * last contents there (every element is written before it is read, so
- * nothing needs clearing): calls that overlap on the GPU, from different
- * threads or streams, race. Same arguments and results as
+ * FSI_STATIC_FACE_CELLS son face cells (20 doubles each, 10 MiB). The array
+ * is placed on a device, and its device address looked up
+ * (cudaGetSymbolAddress), by the first fsi_pair_create on that device, so
+ * the memory is taken at set-up and held until the process exits; the static
+ * calls themselves take none. Create pairs before any stream capture. Faces
+ * larger than FSI_STATIC_FACE_CELLS return FSI_E_ARG. All calls share the one
+ * array and each call leaves its last contents there (every element a call
+ * reads lies inside its own face and is written by that call first, so
+ * nothing needs clearing; a stencil that would read past the face returns
+ * FSI_E_RANGE, as in fsi_pair_father_to_son): calls that overlap on the GPU,
+ * from different threads or streams, race. Same arguments and results as
  * fsi_pair_father_to_son. */
 #define FSI_STATIC_FACE_CELLS 65536
 int fsi_pair_father_to_son_static(fsi_pair_t p, int n_timeStep, const double vf[3]);

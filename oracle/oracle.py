@@ -249,6 +249,19 @@ class Pair:
         self.p = OrPair()
         lib().or_build_pair(C.byref(father.b), C.byref(son.b), C.byref(self.p))
         p = self.p
+        # interpolate_fIn (LBMBlockComm.f90:808-956) reads outside its face
+        # arrays on narrow faces (under 5 son nodes a side with scheme 2, or a
+        # last odd son node past the father's face): refused, as the library does
+        for k in range(6):
+            if son.b.bnd[k] != 0:
+                continue
+            ax = k // 2
+            AF, BF = [(p.zDimF, p.yDimF), (p.zDimF, p.xDimF), (p.yDimF, p.xDimF)][ax]
+            AS, BS = [(p.zDimS, p.yDimS), (p.zDimS, p.xDimS), (p.yDimS, p.xDimS)][ax]
+            AO, BO = (AS if AS % 2 else AS - 1), (BS if BS % 2 else BS - 1)
+            ok = (AO + 1) // 2 <= AF and (BO + 1) // 2 <= BF and (scheme != 2 or min(AS, BS) >= 5)
+            if not ok:
+                raise ValueError("son face %d too narrow for interpolation scheme %d" % (k, scheme))
         self.keep = []
         self.bf = ((DP * 2) * 6)()
         self.bt = ((DP * 2) * 6)()

@@ -11,6 +11,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built libfsi_gpu.so")
+    config.addinivalue_line("markers", "slow: full-size acceptance runs (minutes of oracle time on the host)")
 
 
 @pytest.fixture(scope="session")

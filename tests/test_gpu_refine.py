@@ -54,3 +54,21 @@ def test_two_level_fast_forms(gpu_lib, model, prec, tol):
         ttol = {"f64_fast": 1e-12, "f32": 1e-6, "f16": 2e-5, "bf16": 2e-4}[prec]
         ts = tl.gso.tau_all().reshape(-1)
         assert np.max(np.abs(ts - tl.oso.tau_all.reshape(tl.gso.dims).reshape(-1))) <= ttol
+
+
+@pytest.mark.parametrize("son_dims,scheme,ok", [
+    ((9, 4, 7), 1, True), ((9, 4, 7), 2, False), ((9, 7, 3), 2, False),
+])
+def test_narrow_refinement_faces_are_refused(gpu_lib, son_dims, scheme, ok):
+    # the reference's face interpolation reads outside its face arrays on son
+    # faces under 5 nodes a side with the third/fourth-order scheme: the pair
+    # is refused at creation with FSI_E_ARG (the oracle refuses it too)
+    import fsilbm3d_gb300 as F
+    fa = F.Block(20, 12, 12, bndConds=(101, 104, 301, 301, 301, 301), nu=0.02, uvwIn=(0.05, 0.0, 0.0))
+    so = F.Block(*son_dims, dh=0.5, origin=(6.0, 4.0, 4.0), bndConds=(0,) * 6, nu=0.02, uvwIn=(0.05, 0.0, 0.0))
+    if ok:
+        F.Pair(fa, so, scheme)
+    else:
+        with pytest.raises(F.FsiError) as e:
+            F.Pair(fa, so, scheme)
+        assert e.value.code == -1

@@ -414,3 +414,20 @@ def test_volume_force_wave():
         O.lib().or_update_volume_force(ctypes.byref(b.b), ctypes.byref(fl))
         want = 1e-4 + 5e-5 * math.sin(((2.0 * PI) * 0.125) * t + (30.0 / 180.0) * PI)
         assert list(b.b.volumeForce) == [want, 2e-5, -3e-5]
+
+
+@pytest.mark.parametrize("son_dims,scheme,ok", [
+    ((9, 7, 7), 2, True), ((9, 4, 7), 1, True), ((9, 4, 7), 2, False), ((9, 7, 3), 2, False),
+])
+def test_narrow_refinement_faces_are_refused(son_dims, scheme, ok):
+    # interpolate_fIn's third/fourth-order stencil (LBMBlockComm.f90:826-870)
+    # reaches three son nodes past its own: on a son face under 5 nodes a side
+    # the reference reads outside its face arrays, so such a pair is refused
+    fl = O.make_flow(uvwIn=(0.05, 0.0, 0.0), nu=0.02, interpolateScheme=scheme)
+    fa = O.Block(20, 12, 12, 1.0, (0.0, 0.0, 0.0), [101, 104, 301, 301, 301, 301], 1, fl)
+    so = O.Block(*son_dims, 0.5, (6.0, 4.0, 4.0), [0] * 6, 1, fl)
+    if ok:
+        O.Pair(fa, so, scheme)
+    else:
+        with pytest.raises(ValueError):
+            O.Pair(fa, so, scheme)

@@ -9,10 +9,15 @@ tolerance of the exact FP64 form's tests), plus its size limit. This file is
 collected last so that a run stopping at the first failure has run every
 other test first.
 """
+import os
+import subprocess
+import sys
+
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def make_pair(F, son_dims=(9, 7, 7), father_dims=(20, 12, 12), son_origin=(6.0, 4.0, 4.0), seed=11):
@@ -56,3 +61,36 @@ def test_static_variant_rejects_oversized_faces(gpu_lib):
     assert e.value.code == -1
     # the allocating variant still serves that pair
     p.father_to_son(0)
+
+
+# Run in a fresh process, so that nothing earlier in the test session has
+# already placed the static scratch on the device.
+_FRESH = r"""
+import sys
+sys.path[:0] = [%r, %r]
+import torch
+torch.cuda.mem_get_info()  # torch's runtime on the device before anything is measured
+import fsilbm3d_gb300 as F
+from test_zz_no_alloc import make_pair
+fa, so, p = make_pair(F)
+so.step(blktime=1.0)
+p.father_to_son(0)  # loads the face kernels the static variant launches too
+torch.cuda.synchronize()
+free0 = torch.cuda.mem_get_info()[0]
+so.step(blktime=1.5)
+p.father_to_son_static(1)
+torch.cuda.synchronize()
+free1 = torch.cuda.mem_get_info()[0]
+print("FREE", free0, free1)
+"""
+
+
+def test_static_variant_takes_no_memory_in_the_time_loop(gpu_lib):
+    """The scratch is placed on the device when the pair is created: the first
+    static call afterwards leaves the device's free memory unchanged."""
+    code = _FRESH % (os.path.dirname(HERE), HERE)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("FREE")][-1]
+    free0, free1 = (int(v) for v in line.split()[1:])
+    assert free0 == free1, (free0, free1)
