@@ -16,9 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 FSI_OK = 0
 FSI_E_ARG, FSI_E_CUDA, FSI_E_NAN, FSI_E_TIMEOUT, FSI_E_BC, FSI_E_RANGE, FSI_E_STATE = -1, -2, -3, -4, -5, -6, -7
-PREC_F64, PREC_F64_FAST, PREC_F32, PREC_F16, PREC_BF16 = 0, 1, 2, 3, 4
-PRECISIONS = {"f64": PREC_F64, "f64_fast": PREC_F64_FAST, "f32": PREC_F32, "f16": PREC_F16, "bf16": PREC_BF16}
-_STORE_BYTES = {PREC_F64: 8, PREC_F64_FAST: 8, PREC_F32: 4, PREC_F16: 2, PREC_BF16: 2}
+PREC_F64, PREC_F64_FAST, PREC_F32, PREC_F16, PREC_BF16, PREC_F64_DW = 0, 1, 2, 3, 4, 5
+PRECISIONS = {"f64": PREC_F64, "f64_fast": PREC_F64_FAST, "f32": PREC_F32, "f16": PREC_F16, "bf16": PREC_BF16,
+              "f64_dw": PREC_F64_DW}
+_STORE_BYTES = {PREC_F64: 8, PREC_F64_FAST: 8, PREC_F32: 4, PREC_F16: 2, PREC_BF16: 2, PREC_F64_DW: 8}
 
 DP = C.POINTER(C.c_double)
 

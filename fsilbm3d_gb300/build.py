@@ -1,9 +1,10 @@
 """Build libfsi_gpu.so (sm_103a) in-tree with nvcc.
 
-Eight translation units, compiled in parallel:
+Nine translation units, compiled in parallel:
   k_f64_exact.cu  -fmad=false  FP64 kernels in the reference's operation order
-  k_fast.cu       x4           FP64 regrouped and FP32/FP16/BF16 storage forms,
-                               one unit per form (-DFSI_FAST_PREC=1..4)
+  k_fast.cu       x5           FP64 regrouped, FP32/FP16/BF16 storage forms and
+                               the double-word FP64 form's bulk step, one unit
+                               per form (-DFSI_FAST_PREC=1..5)
   fast_route.cu                forwards the fast launchers to the unit of a form
   k_mlp.cu                     warm-start perceptron: inference, gradient, Adam
   fsi_abi.cu                   host implementation of include/fsi_gpu.h
@@ -28,14 +29,15 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
 # serves one storage form, so the helpers of the other forms are unused there
 # (warning 177, "declared but never referenced"): that warning is off for them.
 UNITS = [("k_fast.cu", "k_fast_p%d.o" % p, ["-DFSI_FAST_PREC=%d" % p, "-diag-suppress", "177"])
-         for p in (3, 4, 2, 1)] + [
+         for p in (3, 4, 2, 1, 5)] + [
     ("k_f64_exact.cu", "k_f64_exact.o", ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
     # host arithmetic (tau, MRT matrices) without contraction, as the reference
     ("fsi_abi.cu", "fsi_abi.o", ["-Xcompiler", "-ffp-contract=off"]),
     ("k_mlp.cu", "k_mlp.o", []),
     ("fast_route.cu", "fast_route.o", []),
 ]
-HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "store_acc.cuh", "bc_impl.cuh", "ib_impl.cuh", "mlp_impl.cuh"]
+HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "store_acc.cuh", "bc_impl.cuh", "ib_impl.cuh", "mlp_impl.cuh",
+           "dw.cuh"]
 
 
 def _nvcc():

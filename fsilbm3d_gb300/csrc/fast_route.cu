@@ -18,12 +18,24 @@ namespace fsi {
     default: return refused;                           \
     }
 
+// the bulk step also serves the double-word form, whose blocks otherwise run
+// on the FP64 units (the host passes FSI_PREC_F64_DW to these two only)
+#define FSI_ROUTE_STEP(prec, refused, CALL)            \
+    switch (prec) {                                    \
+    case FSI_PREC_F64_FAST: return fast_p1::CALL;      \
+    case FSI_PREC_F32: return fast_p2::CALL;           \
+    case FSI_PREC_F16: return fast_p3::CALL;           \
+    case FSI_PREC_BF16: return fast_p4::CALL;          \
+    case FSI_PREC_F64_DW: return fast_p5::CALL;        \
+    default: return refused;                           \
+    }
+
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
-    FSI_ROUTE(prec, false, step_fast_paired(a, mm, prec, model))
+    FSI_ROUTE_STEP(prec, false, step_fast_paired(a, mm, prec, model))
 }
 
 cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st) {
-    FSI_ROUTE(prec, cudaErrorInvalidValue, launch_step_fast(a, mm, prec, model, st))
+    FSI_ROUTE_STEP(prec, cudaErrorInvalidValue, launch_step_fast(a, mm, prec, model, st))
 }
 
 cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st) {

@@ -160,7 +160,8 @@ struct fsi_block {
     void *og = nullptr;         // WALE, fast forms: rotation-rate entries O12, O13, O23 (3N, arithmetic type)
     int periodic[3] = {0, 0, 0};
     MrtMats mm{};
-    int prec = 0;
+    int prec = 0;               // storage form of every kernel but the bulk step
+    bool dw = false;            // FSI_PREC_F64_DW: the bulk step in double-word arithmetic
     size_t esz = 8;
     void *fa = nullptr, *fb = nullptr;
     double *den = nullptr, *u = nullptr;
@@ -403,7 +404,7 @@ int enqueue_step(fsi_block *h, const double vf[3], double blktime, bool use_wind
     if (e == cudaSuccess && grad_model(h->d.iCollidModel))
         e = is_fast(h) ? launch_step_macro_fast(a, h->prec, h->st) : launch_step_macro_f64(a, h->st);
     if (e == cudaSuccess)
-        e = is_fast(h) ? launch_step_fast(a, &h->mm, h->prec, h->d.iCollidModel, h->st)
+        e = is_fast(h) ? launch_step_fast(a, &h->mm, h->dw ? FSI_PREC_F64_DW : h->prec, h->d.iCollidModel, h->st)
                        : launch_step_f64_exact(a, &h->mm, h->d.iCollidModel, h->st);
     if (e != cudaSuccess) return fail(FSI_E_CUDA, "step kernel: %s", cudaGetErrorString(e));
     int rc = apply_bcs(h, h->fb, blktime, a.zeq);
@@ -490,7 +491,10 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
             return fail(FSI_E_ARG, "iCollidModel %d not supported (1 SRT, 2 TRT, 3 MRT, 11 Smagorinsky, 14 WALE, "
                                    "15 Vreman)", m);
     }
-    if (d->precision < FSI_PREC_F64 || d->precision > FSI_PREC_BF16) return fail(FSI_E_ARG, "unknown precision");
+    if (d->precision < FSI_PREC_F64 || d->precision > FSI_PREC_F64_DW) return fail(FSI_E_ARG, "unknown precision");
+    if (d->precision == FSI_PREC_F64_DW && d->iCollidModel != CM_SRT && d->iCollidModel != CM_MRT)
+        return fail(FSI_E_ARG, "the double-word form computes SRT and MRT collisions only (iCollidModel %d)",
+                    d->iCollidModel);
     if (d->velocityKind != 0 && d->velocityKind != 2)
         return fail(FSI_E_ARG, "velocityKind %d not supported (0 shear, 2 oscillatory)", d->velocityKind);
     for (int k = 0; k < 6; k++)
@@ -536,7 +540,14 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
         build_mrt(h->omega, h->mm.mc, h->mm.mf);
     }
     mrt_moment_form(h->mm);
-    h->prec = d->precision;
+    if (d->precision == FSI_PREC_F64_DW && d->iCollidModel == CM_MRT && !h->mm.diag) {
+        delete h;
+        return fail(FSI_E_ARG, "the double-word form needs MRT matrices of the moment form M^-1 S M");
+    }
+    // the double-word form stores FP64 like FSI_PREC_F64_FAST and shares its
+    // kernels except the bulk step
+    h->dw = d->precision == FSI_PREC_F64_DW;
+    h->prec = h->dw ? FSI_PREC_F64_FAST : d->precision;
     h->esz = elem_size(h->prec);
     size_t fbytes = h->esz * 19 * (size_t)h->N;
     cudaError_t e = cudaSuccess;

@@ -183,6 +183,10 @@ namespace fast_p1 { FSI_FAST_API }  // FSI_PREC_F64_FAST
 namespace fast_p2 { FSI_FAST_API }  // FSI_PREC_F32
 namespace fast_p3 { FSI_FAST_API }  // FSI_PREC_F16
 namespace fast_p4 { FSI_FAST_API }  // FSI_PREC_BF16
+namespace fast_p5 {                   // FSI_PREC_F64_DW: the bulk step only
+bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model);
+cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int model, cudaStream_t st);
+}
 
 // ---- warm-start perceptron (k_mlp.cu) ----
 cudaError_t launch_mlp_forward(const float *P, const float *nrm, const float *X, float *Y, int n, cudaStream_t st);

@@ -3,6 +3,8 @@
 //  FSI_PREC_F64_FAST  FP64 storage of f, FP64 arithmetic regrouped around the
 //                     nine opposite-direction pairs (ConstParams.f90:19-20)
 //                     with fused multiply-add.
+//  FSI_PREC_F64_DW    FP64 storage of f, the collision in double-word FP32
+//                     arithmetic (dw.cuh) on the FP32 pipe; SRT and MRT.
 //  FSI_PREC_F32/F16/BF16
 //                     storage of the offsets g_i = f_i - w_i (w_i: lattice
 //                     weights, ConstParams.f90:22-25) in FP32, FP16 or BF16;
@@ -15,8 +17,9 @@
 // IB window and face hooks of k_f64_exact.cu); only rounding differs.
 //
 // This file is compiled once per storage form, with -DFSI_FAST_PREC=<form>
-// (1..4: FSI_PREC_F64_FAST, F32, F16, BF16), so that the four forms' kernels
-// build in parallel. Each unit defines the launchers of fsi_kernels.h's
+// (1..5: FSI_PREC_F64_FAST, F32, F16, BF16, F64_DW), so that the forms'
+// kernels build in parallel. The F64_DW unit defines only the bulk step: its
+// blocks use the F64_FAST unit for everything else (same FP64 storage). Each unit defines the launchers of fsi_kernels.h's
 // FSI_FAST_API in namespace fsi::fast_p<form>; fast_route.cu forwards the
 // public names to them.
 #include <cuda_bf16.h>
@@ -27,16 +30,17 @@
 #include <mutex>
 
 #include "bc_impl.cuh"
+#include "dw.cuh"
 #include "fsi_kernels.h"
 #include "ib_impl.cuh"
 #include "mlp_impl.cuh"
 #include "../../include/fsi_gpu.h"
 
 #ifndef FSI_FAST_PREC
-#error "k_fast.cu is built once per storage form: -DFSI_FAST_PREC=1|2|3|4"
+#error "k_fast.cu is built once per storage form: -DFSI_FAST_PREC=1|2|3|4|5"
 #endif
-#if FSI_FAST_PREC < FSI_PREC_F64_FAST || FSI_FAST_PREC > FSI_PREC_BF16
-#error "FSI_FAST_PREC must be FSI_PREC_F64_FAST, F32, F16 or BF16"
+#if FSI_FAST_PREC < FSI_PREC_F64_FAST || FSI_FAST_PREC > FSI_PREC_F64_DW
+#error "FSI_FAST_PREC must be FSI_PREC_F64_FAST, F32, F16, BF16 or F64_DW"
 #endif
 #define FSI_CAT2(a, b) a##b
 #define FSI_CAT(a, b) FSI_CAT2(a, b)
@@ -53,6 +57,12 @@ template <> struct ST<FSI_PREC_F64_FAST> {
     static constexpr bool OFF = false;
     static __device__ __forceinline__ C dec(S s) { return s; }
     static __device__ __forceinline__ S enc(C c) { return c; }
+};
+template <> struct ST<FSI_PREC_F64_DW> {
+    using S = double; using C = dw;
+    static constexpr bool OFF = false;
+    static __device__ __forceinline__ C dec(S s) { return dw_from_f64(s); }
+    static __device__ __forceinline__ S enc(C c) { return dw_to_f64(c); }
 };
 template <> struct ST<FSI_PREC_F32> {
     using S = float; using C = float;
@@ -174,7 +184,13 @@ __device__ __forceinline__ void collide_srt(typename ST<P>::C g[Q], typename ST<
     }
 }
 
-template <typename C> struct MatsT { C mc[361]; C mf[361]; };
+// the MRT matrices in the arithmetic type; sd: S_k / |row k|^2 of their
+// moment form (used when the host found one, MrtMats::diag)
+template <typename C> struct MatsT { C mc[361]; C mf[361]; C sd[Q]; };
+
+// internal model tag: MRT applied in moment space (the matrices have the
+// moment form M_COLLID = M^-1 S M, M_FORCE = I - M_COLLID/2)
+constexpr int CM_MRT_MOM = 103;
 
 // MRT (FluidDomain.f90:1236-1238): g += M_COLLID (feq - f) + M_FORCE Flb
 template <int P>
@@ -209,6 +225,118 @@ __device__ __forceinline__ void collide_mrt(typename ST<P>::C g[Q], typename ST<
             for (int j = 0; j < Q; j++) s += mm.mf[i + Q * j] * flb[j];
         }
         g[i] = s;
+    }
+}
+
+// The D3Q19 moment transform (rows mrow_) for one cell in any arithmetic
+// type, by velocity class: r0 the rest value, rs[k] = r_i + r_o and rd[k] =
+// r_i - r_o for the nine pairs in pr_ order (x, y, z axes; diagonals (1,1,0),
+// (-1,1,0), (1,0,1), (-1,0,1), (0,1,1), (0,-1,1)). t[k] = sd[k] m_k; the
+// conserved moments 0, 3, 5, 7 are not formed (their rates are zero).
+template <typename C>
+__device__ __forceinline__ void mrt_forward_c(C r0, const C rs[9], const C rd[9], const C sd[Q], C t[Q]) {
+    const C Ax = rs[0], Ay = rs[1], Az = rs[2];
+    const C Dxy = rs[3] + rs[4], Dxz = rs[5] + rs[6], Dyz = rs[7] + rs[8];
+    const C A = (Ax + Ay) + Az, D = (Dxy + Dxz) + Dyz;
+    const C m1 = C(-30) * r0 + (C(-11) * A + C(8) * D);
+    const C m2 = C(12) * r0 + (C(-4) * A + D);
+    const C U = Ay + Az, V = C(-2) * Dyz + (Dxy + Dxz);
+    const C m9 = C(2) * Ax + (V - U);
+    const C m10 = C(-4) * Ax + (C(2) * U + V);
+    const C W = Ay - Az, Xd = Dxy - Dxz;
+    const C m11 = W + Xd;
+    const C m12 = C(-2) * W + Xd;
+    const C m13 = rs[3] - rs[4], m14 = rs[7] - rs[8], m15 = rs[5] - rs[6];
+    const C p3 = rd[3] - rd[4], q3 = rd[3] + rd[4];
+    const C p5 = rd[5] - rd[6], q5 = rd[5] + rd[6];
+    const C p7 = rd[7] - rd[8], q7 = rd[7] + rd[8];
+    const C m4 = C(-4) * rd[0] + (p3 + p5);
+    const C m16 = p3 - p5;
+    const C m6 = C(-4) * rd[1] + (q3 + p7);
+    const C m17 = p7 - q3;
+    const C m8 = C(-4) * rd[2] + (q5 + q7);
+    const C m18 = q5 - q7;
+    t[0] = t[3] = t[5] = t[7] = C(0);
+    t[1] = sd[1] * m1; t[2] = sd[2] * m2; t[4] = sd[4] * m4; t[6] = sd[6] * m6; t[8] = sd[8] * m8;
+    t[9] = sd[9] * m9; t[10] = sd[10] * m10; t[11] = sd[11] * m11; t[12] = sd[12] * m12;
+    t[13] = sd[13] * m13; t[14] = sd[14] * m14; t[15] = sd[15] * m15;
+    t[16] = sd[16] * m16; t[17] = sd[17] * m17; t[18] = sd[18] * m18;
+}
+
+// Delta = M^T t split by parity: Delta_0 = E0; for pair k with representative
+// i: Delta_i = E[k] + O[k], Delta_opp(i) = E[k] - O[k]
+template <typename C>
+__device__ __forceinline__ void mrt_backward_c(const C t[Q], C &E0, C E[9], C O[9]) {
+    E0 = C(-30) * t[1] + C(12) * t[2];
+    const C Ca = C(-11) * t[1] + C(-4) * t[2];
+    const C G = C(2) * t[10] - t[9];
+    const C H = C(-2) * t[12] + t[11];
+    E[0] = C(-2) * G + Ca;
+    E[1] = (Ca + G) + H;
+    E[2] = (Ca + G) - H;
+    O[0] = C(-4) * t[4];
+    O[1] = C(-4) * t[6];
+    O[2] = C(-4) * t[8];
+    const C Cd = C(8) * t[1] + t[2];
+    const C J = t[9] + t[10], K = t[11] + t[12];
+    const C L = Cd + J;
+    const C b34 = L + K, b56 = L - K, b78 = C(-2) * J + Cd;
+    E[3] = b34 + t[13]; E[4] = b34 - t[13];
+    E[5] = b56 + t[15]; E[6] = b56 - t[15];
+    E[7] = b78 + t[14]; E[8] = b78 - t[14];
+    const C a = t[4] + t[16], b = t[6] - t[17];
+    const C c = t[4] - t[16], d = t[8] + t[18];
+    const C e = t[6] + t[17], f = t[8] - t[18];
+    O[3] = a + b; O[4] = b - a;
+    O[5] = c + d; O[6] = d - c;
+    O[7] = e + f; O[8] = f - e;
+}
+
+// MRT (FluidDomain.f90:1236-1238) in moment space for one cell:
+// g' = g + M^-1 S M (feq - g - Flb/2) + Flb, which is M_COLLID (feq - g) +
+// M_FORCE Flb for M_COLLID = M^-1 S M and M_FORCE = I - M_COLLID/2
+template <int P>
+__device__ __forceinline__ void collide_mrt_mom(typename ST<P>::C g[Q], typename ST<P>::C rho,
+                                                typename ST<P>::C drho, typename ST<P>::C u0,
+                                                typename ST<P>::C u1, typename ST<P>::C u2,
+                                                typename ST<P>::C F0, typename ST<P>::C F1,
+                                                typename ST<P>::C F2, bool forced, typename ST<P>::C dh3,
+                                                const typename ST<P>::C sd[Q]) {
+    using C = typename ST<P>::C;
+    constexpr bool OFF = ST<P>::OFF;
+    const C k15 = C(1.5) * (u0 * u0 + u1 * u1 + u2 * u2);
+    const C uF = u0 * F0 + u1 * F1 + u2 * F2;
+    C flb[Q], r[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const C w = C(wt_(i));
+        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eq = OFF ? w * drho + (w * rho) * ((C(3) + C(4.5) * eu) * eu - k15)
+                         : (w * rho) * ((C(1) - k15) + (C(3) + C(4.5) * eu) * eu);
+        if (forced) {
+            const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+            flb[i] = (dh3 * w) * ((eF - uF) + (C(3) * eu) * eF);
+            r[i] = (eq - g[i]) - C(0.5) * flb[i];
+        } else {
+            flb[i] = C(0);
+            r[i] = eq - g[i];
+        }
+    }
+    C rs[9], rd[9], t[Q], E0, E[9], O[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int i = pr_(k), o = opp_(i);
+        rs[k] = r[i] + r[o];
+        rd[k] = r[i] - r[o];
+    }
+    mrt_forward_c<C>(r[0], rs, rd, sd, t);
+    mrt_backward_c<C>(t, E0, E, O);
+    g[0] = g[0] + (E0 + flb[0]);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int i = pr_(k), o = opp_(i);
+        g[i] = g[i] + ((E[k] + O[k]) + flb[i]);
+        g[o] = g[o] + ((E[k] - O[k]) + flb[o]);
     }
 }
 
@@ -509,14 +637,16 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
         ((a.l2[0] && x == 1) || (a.l2[1] && x == X - 2) || (a.l2[2] && y == 1) || (a.l2[3] && y == Y - 2) ||
          (a.l2[4] && z == 1) || (a.l2[5] && z == Z - 2))) {
         a.den[c] = T::OFF ? 1.0 + (double)drho : (double)rho;
-        a.u[c] = u0; a.u[c + N] = u1; a.u[c + 2 * N] = u2;
+        a.u[c] = (double)u0; a.u[c + N] = (double)u1; a.u[c + 2 * N] = (double)u2;
     }
     const C om = sc.om, dh3 = sc.dh3;
-    if (MODEL == CM_SRT) {
+    if constexpr (MODEL == CM_SRT) {
         if (forced) collide_srt<P, true>(g, rho, drho, u0, u1, u2, F0, F1, F2, om, dh3);
         else collide_srt_free<P>(g, rho, drho, u0, u1, u2, om);
-    } else if (MODEL == CM_MRT) {
+    } else if constexpr (MODEL == CM_MRT) {
         collide_mrt<P>(g, rho, drho, u0, u1, u2, F0, F1, F2, forced, dh3, mm);
+    } else if constexpr (MODEL == CM_MRT_MOM) {
+        collide_mrt_mom<P>(g, rho, drho, u0, u1, u2, F0, F1, F2, forced, dh3, mm.sd);
     } else {
         collide_rate<P, MODEL>(g, rho, drho, u0, u1, u2, F0, F1, F2, sc, a, x, y, z, (long long)c);
     }
@@ -2028,18 +2158,45 @@ template <int P, int MODEL>
 cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     using C = typename ST<P>::C;
     MatsT<C> m{};
-    if (MODEL == 3)
+    if (MODEL == 3) {
         for (int i = 0; i < 361; i++) { m.mc[i] = (C)mm->mc[i]; m.mf[i] = (C)mm->mf[i]; }
+        for (int k = 0; k < Q; k++) m.sd[k] = (C)mm->sd[k];
+    }
     // the hook-free variant serves blocks without IB window, half-way faces
     // and non-equilibrium extrapolation faces
     bool hooks = a.win.x1 >= a.win.x0;
     for (int k = 0; k < 6; k++) hooks = hooks || a.hw[k] != nullptr || a.l2[k] != 0;
     // 32-bit byte offsets while all 19 populations span less than 4 GiB
     const bool small = (unsigned long long)Q * a.N * sizeof(typename ST<P>::S) < (1ULL << 32);
+    if constexpr (P == FSI_PREC_F64_DW) {
+        // double-word arithmetic: SRT, and MRT in moment space only
+        if constexpr (MODEL == CM_SRT) {
+            if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
+            return hooks ? step_launch<P, MODEL, true, long long>(a, m, st)
+                         : step_launch<P, MODEL, false, long long>(a, m, st);
+        } else if constexpr (MODEL == CM_MRT) {
+            if (!mm->diag) return cudaErrorInvalidValue;
+            if (small)
+                return hooks ? step_launch<P, CM_MRT_MOM, true, int>(a, m, st)
+                             : step_launch<P, CM_MRT_MOM, false, int>(a, m, st);
+            return hooks ? step_launch<P, CM_MRT_MOM, true, long long>(a, m, st)
+                         : step_launch<P, CM_MRT_MOM, false, long long>(a, m, st);
+        } else {
+            return cudaErrorInvalidValue;
+        }
+    } else {
     if (step_fast_paired(a, mm, P, MODEL))
         return pair_launch<P == FSI_PREC_F64_FAST ? FSI_PREC_F32 : P, MODEL>(a, mm, hooks, st);
+    if (MODEL == CM_MRT && mm->diag) {
+        // moment space: about 80 operations for the transform each way
+        // instead of two dense 19x19 products
+        constexpr int MM = MODEL == CM_MRT ? CM_MRT_MOM : MODEL;
+        if (small) return hooks ? step_launch<P, MM, true, int>(a, m, st) : step_launch<P, MM, false, int>(a, m, st);
+        return hooks ? step_launch<P, MM, true, long long>(a, m, st) : step_launch<P, MM, false, long long>(a, m, st);
+    }
     if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
     return hooks ? step_launch<P, MODEL, true, long long>(a, m, st) : step_launch<P, MODEL, false, long long>(a, m, st);
+    }
 }
 
 // Face kernels of the offset storage forms (FP32, FP16, BF16): the codes of
@@ -2311,7 +2468,7 @@ namespace FSI_FAST_NS {
 
 bool step_fast_paired(const StepArgs &a, const MrtMats *mm, int prec, int model) {
     const bool small = (long long)Q * a.N < (1LL << 31) - 1;
-    return prec != FSI_PREC_F64_FAST &&
+    return prec != FSI_PREC_F64_FAST && prec != FSI_PREC_F64_DW &&
            (model == CM_SRT || model == CM_TRT || model == CM_SMAG || model == CM_VREM || model == CM_WALE ||
             (model == CM_MRT && mm->diag)) && small &&
            a.Z % 2 == 0 && a.Z <= 512;
@@ -2328,6 +2485,8 @@ cudaError_t launch_step_fast(const StepArgs &a, const MrtMats *mm, int prec, int
     }
 }
 
+#if FSI_FAST_PREC != FSI_PREC_F64_DW
+// (the double-word unit defines the bulk step only)
 cudaError_t launch_step_macro_fast(const StepArgs &a, int prec, cudaStream_t st) {
     int bz = a.Z >= 256 ? 256 : ((a.Z + 31) / 32) * 32;
     dim3 g((a.Z + bz - 1) / bz, a.Y, a.X);
@@ -2465,6 +2624,8 @@ cudaError_t launch_win_macro_fast(const void *fs, int prec, double *wden, double
     FSI_DISPATCH(prec, k_win_macro_fast<PP><<<nb, 256, 0, st>>>(fs, wden, wu, g, N, Nw, vf[0], vf[1], vf[2]);
                  return cudaGetLastError())
 }
+
+#endif  // FSI_FAST_PREC != FSI_PREC_F64_DW
 
 }  // namespace FSI_FAST_NS
 }  // namespace fsi

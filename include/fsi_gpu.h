@@ -52,6 +52,10 @@ extern "C" {
 #define FSI_PREC_F32       2  /* FP32 storage of f - w_i, FP32 arithmetic        */
 #define FSI_PREC_F16       3  /* FP16 storage of f - w_i, FP32 arithmetic        */
 #define FSI_PREC_BF16      4  /* BF16 storage of f - w_i, FP32 arithmetic        */
+#define FSI_PREC_F64_DW    5  /* FP64 storage; the collide-stream step in double-word
+                                 FP32 arithmetic (pairs of FP32 values, about 48
+                                 significant bits) on the FP32 pipe; SRT and MRT
+                                 (moment form); everything else as FSI_PREC_F64_FAST */
 
 typedef struct fsi_block *fsi_block_t;
 
