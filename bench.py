@@ -90,7 +90,7 @@ def parse():
                    help="run one side section alone and print its result (profiling runs)")
     p.add_argument("--tgv-grid", type=int, default=256, help="edge of the periodic TGV cube")
     p.add_argument("--ib160-steps", type=int, default=2000, help="steps of the 160x96x96 plate case")
-    p.add_argument("--tgv-forms", default="f64,f64_fast,f32,f16,bf16", help="TGV storage forms")
+    p.add_argument("--tgv-forms", default="f64,f64_fast,f64_dw,f32,f16,bf16", help="TGV storage forms")
     p.add_argument("--tgv-models", default="1,3", help="TGV collision models (1 SRT, 3 MRT)")
     p.add_argument("--les-models", default="2,11,14,15", help="TRT and LES models of the models section")
     a = p.parse_args()
@@ -362,7 +362,7 @@ def model_bytes(model, s, form):
     return B
 
 
-def tgv_forms(F, steps, pk, forms=("f64", "f64_fast", "f32", "f16", "bf16"), models=(1, 3)):
+def tgv_forms(F, steps, pk, forms=("f64", "f64_fast", "f64_dw", "f32", "f16", "bf16"), models=(1, 3)):
     X, Y, Z = TGV_GRID
     N = X * Y * Z
     nu = (TAU - 0.5) / 3.0

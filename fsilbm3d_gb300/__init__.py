@@ -15,11 +15,11 @@ There is no CPU fallback: if the CUDA library cannot be loaded, or no GPU is
 present, every compute call raises.
 """
 from .abi import (FsiError, Block, Pair, Mlp, Batch, lib, load_library, library_path, PREC_F64, PREC_F64_FAST,
-                  PREC_F32, PREC_F16, PREC_BF16, PRECISIONS, device_info, FSI_OK, FSI_E_ARG, FSI_E_CUDA,
+                  PREC_F32, PREC_F16, PREC_BF16, PREC_F64_DW, PRECISIONS, device_info, FSI_OK, FSI_E_ARG, FSI_E_CUDA,
                   FSI_E_NAN, FSI_E_TIMEOUT, FSI_E_BC, FSI_E_RANGE, FSI_E_STATE, continue_write, continue_read)
 from .d3q19 import E, OPPO, WT, Q
 
 __all__ = ["FsiError", "Block", "Pair", "Mlp", "Batch", "lib", "load_library", "library_path", "PREC_F64", "PREC_F64_FAST",
-           "PREC_F32", "PREC_F16", "PREC_BF16", "PRECISIONS", "device_info", "E", "OPPO", "WT", "Q",
+           "PREC_F32", "PREC_F16", "PREC_BF16", "PREC_F64_DW", "PRECISIONS", "device_info", "E", "OPPO", "WT", "Q",
            "FSI_OK", "FSI_E_ARG", "FSI_E_CUDA", "FSI_E_NAN", "FSI_E_TIMEOUT", "FSI_E_BC", "FSI_E_RANGE", "FSI_E_STATE",
            "continue_write", "continue_read"]

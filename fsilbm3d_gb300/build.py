@@ -1,6 +1,6 @@
 """Build libfsi_gpu.so (sm_103a) in-tree with nvcc.
 
-Nine translation units, compiled in parallel:
+Ten translation units, compiled in parallel:
   k_f64_exact.cu  -fmad=false  FP64 kernels in the reference's operation order
   k_fast.cu       x5           FP64 regrouped, FP32/FP16/BF16 storage forms and
                                the double-word FP64 form's bulk step, one unit
@@ -8,6 +8,7 @@ Nine translation units, compiled in parallel:
   fast_route.cu                forwards the fast launchers to the unit of a form
   k_mlp.cu                     warm-start perceptron: inference, gradient, Adam
   fsi_abi.cu                   host implementation of include/fsi_gpu.h
+  beam_host.cpp                host structural solver of include/fsi_beam.h
 The library is linked with --no-undefined, so that a launcher missing from a
 unit fails the build rather than the first load.
 """
@@ -35,6 +36,8 @@ UNITS = [("k_fast.cu", "k_fast_p%d.o" % p, ["-DFSI_FAST_PREC=%d" % p, "-diag-sup
     ("fsi_abi.cu", "fsi_abi.o", ["-Xcompiler", "-ffp-contract=off"]),
     ("k_mlp.cu", "k_mlp.o", []),
     ("fast_route.cu", "fast_route.o", []),
+    # the host-side structural solver (no device code), without contraction
+    ("beam_host.cpp", "beam_host.o", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 HEADERS = ["fsi_common.cuh", "fsi_kernels.h", "store_acc.cuh", "bc_impl.cuh", "ib_impl.cuh", "mlp_impl.cuh",
            "dw.cuh"]
@@ -57,7 +60,8 @@ def _stale(target, deps):
 def build(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "fsi_gpu.h")]
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", h)
+                                                     for h in ("fsi_gpu.h", "fsi_beam.h")]
     jobs = []
     objs = []
     for src, obj, extra in UNITS:

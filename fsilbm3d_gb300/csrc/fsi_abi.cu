@@ -60,6 +60,18 @@ int fail(int code, const char *fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+// the message of fsi_last_error for the host-side units (beam_host.cpp)
+namespace fsi {
+int host_fail(int code, const char *msg) {
+    g_err = msg;
+    return code;
+}
+}  // namespace fsi
+
+namespace {
+
 #define CK(call)                                                                             \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \

@@ -2143,7 +2143,10 @@ cudaError_t step_launch(const StepArgs &a, const MatsT<typename ST<P>::C> &m, cu
     Scal<C> sc{};
     sc.om = (C)a.omega;
     sc.dh = (C)a.dh;
-    sc.dh3 = (C)3 * (C)a.dh;
+    // (host code: the double-word type's arithmetic is device-only, so its
+    // scalars are formed in FP64 and converted once)
+    if constexpr (P == FSI_PREC_F64_DW) sc.dh3 = (C)(3.0 * a.dh);
+    else sc.dh3 = (C)3 * (C)a.dh;
     for (int k = 0; k < 3; k++) sc.vf[k] = (C)a.vf[k];
     sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
     sc.om2 = (C)a.omega2;

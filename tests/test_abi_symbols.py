@@ -1,5 +1,6 @@
 """The C-ABI library builds for sm_103a, loads without a GPU and exports
-every function include/fsi_gpu.h declares (no compute calls here)."""
+every function include/fsi_gpu.h and include/fsi_beam.h declare (no compute
+calls here)."""
 import os
 import re
 import subprocess
@@ -9,8 +10,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "fsi_gpu.h")).read()
+def declared_symbols(header="fsi_gpu.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\bint\s+(fsi_\w+)\s*\(", src)))
 
@@ -33,6 +34,16 @@ def test_library_exports_every_declared_symbol(gpu_lib):
     assert sorted(SYMBOLS) == declared_symbols()
     for s in declared_symbols():
         assert hasattr(gpu_lib, s)
+
+
+def test_library_exports_the_beam_solver(gpu_lib):
+    import fsilbm3d_gb300 as F
+    syms = declared_symbols("fsi_beam.h")
+    assert "fsi_beam_structure" in syms and "fsi_beam_markers" in syms and len(syms) == 9
+    out = subprocess.run(["nm", "-D", "--defined-only", F.library_path()], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(line.split()[-1] for line in out.splitlines() if line.strip())
+    assert not [s for s in syms if s not in exported]
 
 
 def test_no_cpu_fallback_without_library(tmp_path, monkeypatch):
@@ -62,6 +73,7 @@ def test_binding_constants_match_header():
         "FSI_E_TIMEOUT": A.FSI_E_TIMEOUT, "FSI_E_BC": A.FSI_E_BC, "FSI_E_RANGE": A.FSI_E_RANGE,
         "FSI_E_STATE": A.FSI_E_STATE, "FSI_PREC_F64": A.PREC_F64, "FSI_PREC_F64_FAST": A.PREC_F64_FAST,
         "FSI_PREC_F32": A.PREC_F32, "FSI_PREC_F16": A.PREC_F16, "FSI_PREC_BF16": A.PREC_BF16,
+        "FSI_PREC_F64_DW": A.PREC_F64_DW,
         "FSI_KERNEL_AUTO": A.KERNEL_AUTO, "FSI_KERNEL_PAIRED": A.KERNEL_PAIRED,
         "FSI_KERNEL_PIPELINED": A.KERNEL_PIPELINED, "FSI_IB_AUTO": A.IB_AUTO, "FSI_IB_GRID": A.IB_GRID,
         "FSI_IB_CLUSTER": A.IB_CLUSTER, "FSI_IB_OVERLAP": A.IB_OVERLAP, "FSI_MLP_IN": A.MLP_IN,

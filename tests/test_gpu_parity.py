@@ -135,14 +135,61 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
-def test_f64_fast_within_1e12(gpu_lib):
-    c = Case((24, 20, 16), model=1, nu=0.02, precision=F.PREC_F64_FAST)
+F64_FORMS = [F.PREC_F64_FAST, F.PREC_F64_DW]
+
+
+@pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("prec", F64_FORMS)
+def test_f64_fast_within_1e12(gpu_lib, prec, model):
+    c = Case((24, 20, 16), model=model, nu=0.02, precision=prec)
     c.init_tgv(0.05)
     for s in range(10):
         c.step()
-    fo, fg = c.f_pair()
-    # FP64 with regrouped sums and FMA: relative error per step well below 1e-12
-    assert _rel(fg, fo) < 1e-12
+        fo, fg = c.f_pair()
+        # FP64 storage with regrouped FP64 arithmetic (F64_FAST) or double-word
+        # FP32 arithmetic (F64_DW, about 48 bits): the relative difference from
+        # the reference-order oracle stays below 1e-12 at every step
+        assert _rel(fg, fo) < 1e-12, s
+
+
+@pytest.mark.parametrize("name", sorted(BC_CASES))
+@pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("prec", F64_FORMS)
+def test_f64_fast_boundaries_within_1e12(gpu_lib, prec, name, model):
+    # every boundary-code set, both collision models, odd z extent (one cell
+    # per thread everywhere)
+    c = Case((14, 11, 9), model=model, nu=0.01, precision=prec, **BC_CASES[name])
+    c.init_equilibrium()
+    for s in range(8):
+        c.step()
+        fo, fg = c.f_pair()
+        assert _rel(fg, fo) < 1e-12, s
+
+
+@pytest.mark.parametrize("model", [1, 3])
+def test_f64_dw_plate_within_1e12(gpu_lib, model):
+    # the IB window cells take the IB stage's den/u/force (FP64) into the
+    # double-word collision; Lagrangian force and distributions against the oracle
+    dims = (40, 24, 20)
+    c = Case(dims, bnd=(101, 104, 101, 101, 101, 101), model=model, uvwIn=(0.05, 0.0, 0.0), nu=0.02,
+             plates=[plate_in(dims, n=5, heave=1.0, freq=0.02)], ntol=4, dtol=1e-12, Uref=0.05,
+             precision=F.PREC_F64_DW)
+    c.init_equilibrium()
+    for s in range(6):
+        r = c.step()
+        assert r["it_o"] == r["it_g"]
+        fo, fg = c.f_pair()
+        assert _rel(fg, fo) < 1e-12, s
+    Fo, Fg = r["ef_o"].sum(axis=0), r["ef_g"].sum(axis=0)
+    assert np.max(np.abs(Fg - Fo)) <= 1e-10 * np.max(np.abs(Fo))
+
+
+def test_f64_dw_refuses_other_models(gpu_lib):
+    # the double-word collision is built for SRT and MRT only
+    for model in (2, 11):
+        with pytest.raises(F.FsiError) as e:
+            F.Block(8, 8, 8, iCollidModel=model, precision=F.PREC_F64_DW, params=(0.1875,))
+        assert e.value.code == -1
 
 
 @pytest.mark.parametrize("model", [1, 3])
