@@ -19,10 +19,10 @@
 //   product   -- DWTimesDW3 (same paper, Algorithm 12) with fused
 //               multiply-add for the exact product of the high parts.
 //   reciprocal-- one Newton step r = y + y (1 - x y) from the FP32 reciprocal.
-// FP64 -> double word is integer bit work (FP64 -> FP32 conversion runs on
-// GB300's FP64 pipe, about 2 per clock per SM); double word -> FP64 is two
-// exact FP32 -> FP64 conversions (about 20 per clock per SM) and one FP64
-// addition per stored value, so that the step issues little FP64 work.
+// Conversions between FP32 and FP64 run on GB300's FP64 pipe (about two per
+// clock per SM), so both directions are integer bit work here: FP64 -> double
+// word splits the significand, double word -> FP64 builds the two exact FP64
+// parts and adds them with the one FP64 instruction per stored value.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -131,17 +131,127 @@ __host__ __device__ __forceinline__ dw dw_from_f64(double d) {
 #endif
 }
 
-// double word -> nearest FP64: the two parts converted exactly (FP32 -> FP64
-// conversion is not an FP64-pipe instruction on GB300), one FP64 addition
+// the exact FP64 value of an FP32 number by bit operations (subnormals -> 0):
+// GB300 runs FP32 -> FP64 conversion on its FP64 pipe
+__host__ __device__ __forceinline__ double f64_of_f32(float x) {
+#ifndef __CUDA_ARCH__
+    dw_arithmetic_is_device_only();
+    return double();
+#else
+    const unsigned b = __float_as_uint(x);
+    const unsigned sgn = b & 0x80000000u;
+    const bool nz = (b & 0x7F800000u) != 0u;
+    const unsigned hi = nz ? (((b & 0x7FFFFFFFu) >> 3) + (896u << 20)) | sgn : sgn;
+    const unsigned lo = nz ? (b << 29) : 0u;
+    return __hiloint2double((int)hi, (int)lo);
+#endif
+}
+
+// double word -> nearest FP64: the two parts made exact FP64 numbers by bit
+// operations, one FP64 addition (the only FP64-pipe instruction per value)
 __host__ __device__ __forceinline__ double dw_to_f64(dw x) {
 #ifndef __CUDA_ARCH__
     dw_arithmetic_is_device_only();
     return double();
 #else
-    return __dadd_rn((double)x.h, (double)x.l);
+    return __dadd_rn(f64_of_f32(x.h), f64_of_f32(x.l));
 #endif
 }
 
 __device__ __forceinline__ dw::operator double() const { return dw_to_f64(*this); }
+
+}  // namespace fsi
+
+// ---------------------------------------------------------------------------
+// dw2: two double words side by side (the same quantity of two cells), every
+// operation one packed FP32x2 instruction (FADD2 / FMUL2 / FFMA2) per step of
+// the single algorithms above, so that two cells cost the issue slots of one.
+// Subtraction is written out (TwoDiff) instead of adding a negated operand.
+namespace fsi {
+
+__device__ __forceinline__ float2 p2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, p2(-1.0f), a); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+struct dw2 {
+    float2 h, l;
+    __host__ __device__ constexpr dw2() : h{0.0f, 0.0f}, l{0.0f, 0.0f} {}
+    __host__ __device__ constexpr dw2(double d)
+        : h{(float)d, (float)d}, l{(float)(d - (double)(float)d), (float)(d - (double)(float)d)} {}
+    __host__ __device__ constexpr dw2(float2 hh, float2 ll, int) : h(hh), l(ll) {}
+};
+
+__host__ __device__ __forceinline__ dw2 dw2_fast2sum(float2 a, float2 b) {
+#ifndef __CUDA_ARCH__
+    dw_arithmetic_is_device_only();
+    return dw2();
+#else
+    const float2 s = padd(a, b);
+    return dw2(s, psub(b, psub(s, a)), 0);
+#endif
+}
+
+__host__ __device__ __forceinline__ dw2 operator+(dw2 x, dw2 y) {
+#ifndef __CUDA_ARCH__
+    dw_arithmetic_is_device_only();
+    return dw2();
+#else
+    const float2 s = padd(x.h, y.h);
+    const float2 bp = psub(s, x.h);
+    const float2 ap = psub(s, bp);
+    const float2 e = padd(psub(x.h, ap), psub(y.h, bp));
+    return dw2_fast2sum(s, padd(e, padd(x.l, y.l)));
+#endif
+}
+__host__ __device__ __forceinline__ dw2 operator-(dw2 x, dw2 y) {
+#ifndef __CUDA_ARCH__
+    dw_arithmetic_is_device_only();
+    return dw2();
+#else
+    // TwoDiff(a, b) = TwoSum(a, -b) with the negation folded in
+    const float2 s = psub(x.h, y.h);
+    const float2 bp = psub(s, x.h);
+    const float2 ap = psub(s, bp);
+    const float2 e = psub(psub(x.h, ap), padd(y.h, bp));
+    return dw2_fast2sum(s, padd(e, psub(x.l, y.l)));
+#endif
+}
+__host__ __device__ __forceinline__ dw2 operator-(dw2 x) {
+#ifndef __CUDA_ARCH__
+    dw_arithmetic_is_device_only();
+    return dw2();
+#else
+    return dw2(pmul(x.h, p2(-1.0f)), pmul(x.l, p2(-1.0f)), 0);
+#endif
+}
+__host__ __device__ __forceinline__ dw2 operator*(dw2 x, dw2 y) {
+#ifndef __CUDA_ARCH__
+    dw_arithmetic_is_device_only();
+    return dw2();
+#else
+    const float2 ch = pmul(x.h, y.h);
+    const float2 cl1 = pfma(x.h, y.h, pmul(ch, p2(-1.0f)));
+    const float2 cl2 = pfma(x.l, y.h, pfma(x.h, y.l, pmul(x.l, y.l)));
+    return dw2_fast2sum(ch, padd(cl1, cl2));
+#endif
+}
+__host__ __device__ __forceinline__ dw2 &operator+=(dw2 &x, dw2 y) { return x = x + y; }
+__host__ __device__ __forceinline__ dw2 &operator-=(dw2 &x, dw2 y) { return x = x - y; }
+__host__ __device__ __forceinline__ dw2 &operator*=(dw2 &x, dw2 y) { return x = x * y; }
+
+__host__ __device__ __forceinline__ dw2 rcp(dw2 x) {
+#ifndef __CUDA_ARCH__
+    dw_arithmetic_is_device_only();
+    return dw2();
+#else
+    const float2 y = make_float2(__frcp_rn(x.h.x), __frcp_rn(x.h.y));
+    const float2 ph = pmul(x.h, y);
+    const float2 pl = pfma(x.l, y, pfma(x.h, y, pmul(ph, p2(-1.0f))));
+    const float2 d = psub(psub(p2(1.0f), ph), pl);
+    return dw2_fast2sum(y, pmul(y, d));
+#endif
+}
 
 }  // namespace fsi

@@ -52,6 +52,12 @@ namespace {
 constexpr int TPB = 256;
 
 template <int P> struct ST;
+// internal: the double-word form with two cells per thread (dw2)
+constexpr int PDW2 = 105;
+template <> struct ST<PDW2> {
+    using S = double; using C = dw2;
+    static constexpr bool OFF = false;
+};
 template <> struct ST<FSI_PREC_F64_FAST> {
     using S = double; using C = double;
     static constexpr bool OFF = false;
@@ -107,6 +113,22 @@ __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
 // +v, -v or the additive identity -0 for lattice component e
 template <typename C> __device__ __forceinline__ C sel(int e, C v) { return e > 0 ? v : (e < 0 ? -v : C(-0.0)); }
 
+// e_i . (v0, v1, v2) summing only the nonzero components (i is a constant
+// after unrolling). Equal, bit for bit, to the three-term sum of sel():
+// x + (-0) is x in IEEE arithmetic; the double-word type is spared the
+// additions of zero.
+template <typename C> __device__ __forceinline__ C eacc(bool set, int e, C acc, C v) {
+    return set ? (e > 0 ? acc + v : acc - v) : sel(e, v);
+}
+template <typename C> __device__ __forceinline__ C edot3(int i, C v0, C v1, C v2) {
+    C acc = C(-0.0);
+    bool set = false;
+    if (ex_(i) != 0) { acc = sel(ex_(i), v0); set = true; }
+    if (ey_(i) != 0) { acc = eacc(set, ey_(i), acc, v1); set = true; }
+    if (ez_(i) != 0) { acc = eacc(set, ez_(i), acc, v2); }
+    return acc;
+}
+
 // offset equilibrium g_eq = w (rho - 1) + w rho (3 eu + 4.5 eu^2 - 1.5 u^2),
 // k15 = 1.5 u^2 (the face kernels and the fused z faces)
 __device__ __forceinline__ float geq_off(int q, float rho, float u0, float u1, float u2, float k15) {
@@ -129,9 +151,9 @@ __device__ __forceinline__ void macro_fast(const typename ST<P>::C g[Q], const t
         const int i = pr_(k), o = opp_(i);
         const C sk = g[i] + g[o], dk = g[i] - g[o];
         s += sk;
-        jx += sel(ex_(i), dk);
-        jy += sel(ey_(i), dk);
-        jz += sel(ez_(i), dk);
+        if (ex_(i) > 0) jx += dk; else if (ex_(i) < 0) jx -= dk;
+        if (ey_(i) > 0) jy += dk; else if (ey_(i) < 0) jy -= dk;
+        if (ez_(i) > 0) jz += dk; else if (ez_(i) < 0) jz -= dk;
     }
     if (ST<P>::OFF) { drho = s; rho = C(1) + s; }
     else { rho = s; drho = s - C(1); }
@@ -165,7 +187,7 @@ __device__ __forceinline__ void collide_srt(typename ST<P>::C g[Q], typename ST<
     for (int k = 0; k < 9; k++) {
         const int i = pr_(k), o = opp_(i);
         const C w = C(wt_(i));
-        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eu = edot3(i, u0, u1, u2);
         const C wr = w * rho;
         const C sym = OFF ? w * drho + wr * (C(4.5) * eu * eu - k15) : wr * ((C(1) - k15) + C(4.5) * eu * eu);
         const C asym = (C(3) * wr) * eu;
@@ -173,7 +195,7 @@ __device__ __forceinline__ void collide_srt(typename ST<P>::C g[Q], typename ST<
         C ni = gi + om * ((sym + asym) - gi);
         C no = go + om * ((sym - asym) - go);
         if (FORCED) {
-            const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+            const C eF = edot3(i, F0, F1, F2);
             const C cw = cf * w;
             const C Fs = cw * (C(3) * eu * eF - uF), Fa = cw * eF;
             ni += Fs + Fa;
@@ -208,11 +230,11 @@ __device__ __forceinline__ void collide_mrt(typename ST<P>::C g[Q], typename ST<
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const C w = C(wt_(i));
-        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eu = edot3(i, u0, u1, u2);
         const C eq = OFF ? w * drho + (w * rho) * ((C(3) + C(4.5) * eu) * eu - k15)
                          : (w * rho) * ((C(1) - k15) + (C(3) + C(4.5) * eu) * eu);
         neq[i] = eq - g[i];
-        const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+        const C eF = edot3(i, F0, F1, F2);
         flb[i] = (dh3 * w) * (eF - uF + C(3) * eu * eF);
     }
 #pragma unroll
@@ -310,11 +332,11 @@ __device__ __forceinline__ void collide_mrt_mom(typename ST<P>::C g[Q], typename
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const C w = C(wt_(i));
-        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eu = edot3(i, u0, u1, u2);
         const C eq = OFF ? w * drho + (w * rho) * ((C(3) + C(4.5) * eu) * eu - k15)
                          : (w * rho) * ((C(1) - k15) + (C(3) + C(4.5) * eu) * eu);
         if (forced) {
-            const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+            const C eF = edot3(i, F0, F1, F2);
             flb[i] = (dh3 * w) * ((eF - uF) + (C(3) * eu) * eF);
             r[i] = (eq - g[i]) - C(0.5) * flb[i];
         } else {
@@ -365,7 +387,7 @@ __device__ __forceinline__ void collide_srt_free(typename ST<P>::C g[Q], typenam
     for (int k = 0; k < 9; k++) {
         const int i = pr_(k), o = opp_(i);
         const bool cls1 = (i <= 6);
-        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eu = edot3(i, u0, u1, u2);
         const C Sm = (cls1 ? bc1 : bc2) * (eu * eu) + (cls1 ? ac1 : ac2);
         const C Am = (cls1 ? cc1 : cc2) * eu;
         const C gi = g[i], go = g[o];
@@ -563,11 +585,11 @@ __device__ __forceinline__ void collide_rate(typename ST<P>::C g[Q], typename ST
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const C w = C(wt_(i));
-        const C eu = sel(ex_(i), u0) + sel(ey_(i), u1) + sel(ez_(i), u2);
+        const C eu = edot3(i, u0, u1, u2);
         const C eq = OFF ? w * drho + (w * rho) * ((C(3) + C(4.5) * eu) * eu - k15)
                          : (w * rho) * ((C(1) - k15) + (C(3) + C(4.5) * eu) * eu);
         neq[i] = eq - g[i];
-        const C eF = sel(ex_(i), F0) + sel(ey_(i), F1) + sel(ez_(i), F2);
+        const C eF = edot3(i, F0, F1, F2);
         flb[i] = (sc.dh3 * w) * (eF - uF + C(3) * eu * eF);
     }
     if (MODEL == CM_TRT) {
@@ -683,6 +705,103 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
             __stcs((dp + corr) + of.st[i], T::enc(g[i]));
     }
 }
+
+#if FSI_FAST_PREC == FSI_PREC_F64_DW
+// ---------------------------------------------------------------------------
+// The double-word form's bulk step without hooks (no IB window, half-way or
+// 102 faces) and with an even z extent: each thread takes the cells z, z+1
+// (z even) in one dw2, so that every double-word operation serves two cells
+// with packed FP32x2 instructions. Loads are 16-byte pairs of FP64; a
+// population that streams along z lands on an odd offset and is stored as two
+// FP64 values. Same physics and step as k_step_fast (push scheme, periodic
+// wrap, uniform volume force).
+// ---------------------------------------------------------------------------
+constexpr int TPB_DW2 = 128;
+struct SdT { dw2 sd[Q]; };
+
+template <int MODEL, typename IT>
+__global__ void __launch_bounds__(TPB_DW2) k_step_dw2(StepArgs a, Offs<IT> of, Scal<dw2> sc, SdT sdt) {
+    const int zp = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = blockIdx.z;
+    const int X = a.X, Y = a.Y, Z = a.Z;
+    const int z = 2 * zp;
+    if (z >= Z || y >= Y) return;
+    const long long N = a.N;
+    const IT c = (IT)z + (IT)Z * ((IT)y + (IT)Y * (IT)x);
+    constexpr bool U32 = sizeof(IT) == 4;
+    dw2 g[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        double2 v;
+        if constexpr (U32)
+            v = __ldcs((const double2 *)((const char *)a.src + (unsigned)(c + of.ld[i]) * 8u));
+        else
+            v = __ldcs((const double2 *)((const double *)a.src + (c + of.ld[i])));
+        const dw d0 = dw_from_f64(v.x), d1 = dw_from_f64(v.y);
+        g[i] = dw2(make_float2(d0.h, d1.h), make_float2(d0.l, d1.l), 0);
+    }
+    dw2 rho, drho, u0, u1, u2;
+    macro_fast<PDW2>(g, sc.vf, sc.dh, rho, drho, u0, u1, u2);
+    if constexpr (MODEL == CM_SRT) {
+        if (sc.forced) collide_srt<PDW2, true>(g, rho, drho, u0, u1, u2, sc.vf[0], sc.vf[1], sc.vf[2], sc.om, sc.dh3);
+        else collide_srt_free<PDW2>(g, rho, drho, u0, u1, u2, sc.om);
+    } else {
+        collide_mrt_mom<PDW2>(g, rho, drho, u0, u1, u2, sc.vf[0], sc.vf[1], sc.vf[2], sc.forced != 0, sc.dh3, sdt.sd);
+    }
+    // push: destination = c + st[i] + the periodic wrap of each cell
+    const IT ZY = (IT)Z * (IT)Y, NN = (IT)N;
+    const IT cyp = (y == Y - 1) ? -ZY : 0, cym = (y == 0) ? ZY : 0;
+    const IT cxp = (x == X - 1) ? -NN : 0, cxm = (x == 0) ? NN : 0;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const double d0 = dw_to_f64(dw(g[i].h.x, g[i].l.x, 0)), d1 = dw_to_f64(dw(g[i].h.y, g[i].l.y, 0));
+        const IT cxy = wrap_corr(ey_(i), cyp, cym) + wrap_corr(ex_(i), cxp, cxm);
+        const IT o = c + cxy + of.st[i];
+        if (ez_(i) == 0) {
+            if constexpr (U32) __stcs((double2 *)((char *)a.dst + (unsigned)o * 8u), make_double2(d0, d1));
+            else __stcs((double2 *)((double *)a.dst + o), make_double2(d0, d1));
+        } else {
+            // cell z streams to z + ez, cell z+1 to z+1+ez; only z = 0 (ez < 0)
+            // and z+1 = Z-1 (ez > 0) wrap
+            const IT w0 = (ez_(i) < 0 && z == 0) ? (IT)Z : 0;
+            const IT w1 = (ez_(i) > 0 && z + 1 == Z - 1) ? -(IT)Z : 0;
+            if constexpr (U32) {
+                __stcs((double *)((char *)a.dst + (unsigned)(o + w0) * 8u), d0);
+                __stcs((double *)((char *)a.dst + (unsigned)(o + 1 + w1) * 8u), d1);
+            } else {
+                __stcs((double *)a.dst + (o + w0), d0);
+                __stcs((double *)a.dst + (o + 1 + w1), d1);
+            }
+        }
+    }
+}
+
+template <int MODEL, typename IT>
+cudaError_t dw2_launch(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
+    Offs<IT> of{};
+    const long long ZY = (long long)a.Z * a.Y;
+    for (int i = 0; i < Q; i++) {
+        of.ld[i] = (IT)((long long)i * a.N);
+        of.st[i] = (IT)((long long)i * a.N + ez_(i) + (long long)a.Z * ey_(i) + ZY * ex_(i));
+    }
+    const int Zp = a.Z / 2;
+    int bz = Zp >= TPB_DW2 ? TPB_DW2 : ((Zp + 31) / 32) * 32;
+    int by = TPB_DW2 / bz;
+    if (by < 1) by = 1;
+    dim3 blk(bz, by), grd((Zp + bz - 1) / bz, (a.Y + by - 1) / by, a.X);
+    Scal<dw2> sc{};
+    sc.om = dw2(a.omega);
+    sc.dh = dw2(a.dh);
+    sc.dh3 = dw2(3.0 * a.dh);
+    for (int k = 0; k < 3; k++) sc.vf[k] = dw2(a.vf[k]);
+    sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
+    SdT sdt{};
+    for (int k = 0; k < Q; k++) sdt.sd[k] = dw2(mm->sd[k]);
+    k_step_dw2<MODEL, IT><<<grd, blk, 0, st>>>(a, of, sc, sdt);
+    return cudaGetLastError();
+}
+#endif
 
 // ---------------------------------------------------------------------------
 // Paired-cell form of the step for the offset storage forms (FP32, FP16,
@@ -2172,7 +2291,16 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     // 32-bit byte offsets while all 19 populations span less than 4 GiB
     const bool small = (unsigned long long)Q * a.N * sizeof(typename ST<P>::S) < (1ULL << 32);
     if constexpr (P == FSI_PREC_F64_DW) {
-        // double-word arithmetic: SRT, and MRT in moment space only
+        // double-word arithmetic: SRT, and MRT in moment space only; two
+        // cells per thread when the block needs no hooks and z is even
+#if FSI_FAST_PREC == FSI_PREC_F64_DW
+        if constexpr (MODEL == CM_SRT || MODEL == CM_MRT) {
+            if (!hooks && a.Z % 2 == 0 && (MODEL == CM_SRT || mm->diag)) {
+                constexpr int MM = MODEL == CM_MRT ? CM_MRT_MOM : MODEL;
+                return small ? dw2_launch<MM, int>(a, mm, st) : dw2_launch<MM, long long>(a, mm, st);
+            }
+        }
+#endif
         if constexpr (MODEL == CM_SRT) {
             if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
             return hooks ? step_launch<P, MODEL, true, long long>(a, m, st)

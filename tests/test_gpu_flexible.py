@@ -95,7 +95,7 @@ def test_flexible_plate_fp64_bitwise(gpu_lib, model):
 
 # The FP64-storage forms differ from the reference-order run by about 1e-14
 # per step in the fluid, but the beam's conjugate-gradient solve stops at an
-# absolute residual of 1e-6 (Beam_CG_Solve, SolidSolver.f90:1969-1970): loads
+# absolute residual of 1e-6 (Beam_CG_Solve, SolidSolver.f90:1975-1976): loads
 # that differ in their last bits can stop it an iteration apart, which moves
 # the displacement by far more than the load's difference. Measured over 60
 # steps: 1.5e-9 (F64_FAST) and 3e-9 (F64_DW) of the tip's largest bending

@@ -167,6 +167,19 @@ def test_f64_fast_boundaries_within_1e12(gpu_lib, prec, name, model):
 
 
 @pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("dims", [(14, 9, 22), (14, 9, 21), (7, 5, 64)])
+def test_f64_dw_forced_periodic_within_1e12(gpu_lib, dims, model):
+    # even z extent without hooks: two cells per thread (packed FP32x2 double
+    # words); odd: one cell per thread
+    c = Case(dims, model=model, nu=0.02, precision=F.PREC_F64_DW, volumeForceIn=(3e-5, -1e-5, 2e-5))
+    c.init_tgv(0.04)
+    for s in range(12):
+        c.step()
+        fo, fg = c.f_pair()
+        assert _rel(fg, fo) < 1e-12, s
+
+
+@pytest.mark.parametrize("model", [1, 3])
 def test_f64_dw_plate_within_1e12(gpu_lib, model):
     # the IB window cells take the IB stage's den/u/force (FP64) into the
     # double-word collision; Lagrangian force and distributions against the oracle
