@@ -66,8 +66,14 @@ RE = 1000.0
 # the flexible plate: bending and stretching stiffness (KB, KS), mass ratio;
 # KS is not given by the case and is chosen stiff in stretching
 PLATE_KB, PLATE_KS, PLATE_DENR = 0.5, 1000.0, 1.0
-# Newmark-beta (average acceleration), Newton-Raphson stop and limit, no damping
-BEAM_SOLVER = dict(dampK=0.0, dampM=0.0, GeoGamma=1.0, NewmarkGamma=0.5, NewmarkBeta=0.25, dtolFEM=1e-10,
+# Newmark-beta with numerical dissipation of the highest beam modes (gamma =
+# 0.6, beta = (gamma + 1/2)^2 / 4; the reference reads both from inFlow.dat),
+# Newton-Raphson stop and limit, no damping. With the non-dissipative
+# gamma = 1/2, beta = 1/4 the explicitly coupled plate of this case diverges
+# after about 1,200 steps (the penalty force grows at the beam's highest
+# modes); with gamma = 0.6 it runs a heave period with the same mean forces
+# as with damping or a softer beam.
+BEAM_SOLVER = dict(dampK=0.0, dampM=0.0, GeoGamma=1.0, NewmarkGamma=0.6, NewmarkBeta=0.3025, dtolFEM=1e-10,
                    ntolFEM=20, isKB=1, g=(0.0, 0.0, 0.0))
 NTOL, DTOL = 5, 1e-4
 BND = (101, 104, 101, 101, 101, 101)
@@ -859,13 +865,22 @@ def main():
 
     extra = {}
     if not a.no_extra and rank == 0:
-        extra["tgv256"] = tgv_forms(F, max(20, min(a.steps, 100)), pk)
-        extra["tgv256_models"] = tgv_forms(F, max(20, min(a.steps, 100)), pk, forms=("f64", "f32", "f16"),
-                                           models=tuple(int(m) for m in a.les_models.split(",")))
-        extra["ib160"] = ib160_case(F, a.ib160_steps)
-        extra["fsi384_period"] = fsi_period_case(F)
-        extra["batched_sweep"] = batched_sweep(F, max(10, min(a.steps, 50)))
-        extra["warm_start"] = warm_start_case(F)
+        sections = [
+            ("tgv256", lambda: tgv_forms(F, max(20, min(a.steps, 100)), pk)),
+            ("tgv256_models", lambda: tgv_forms(F, max(20, min(a.steps, 100)), pk, forms=("f64", "f32", "f16"),
+                                                models=tuple(int(m) for m in a.les_models.split(",")))),
+            ("ib160", lambda: ib160_case(F, a.ib160_steps)),
+            ("fsi384_period", lambda: fsi_period_case(F)),
+            ("batched_sweep", lambda: batched_sweep(F, max(10, min(a.steps, 50)))),
+            ("warm_start", lambda: warm_start_case(F)),
+        ]
+        for name, run in sections:
+            # a side section that fails is reported in its place; the headline
+            # line is still printed
+            try:
+                extra[name] = run()
+            except Exception as e:  # noqa: BLE001
+                extra[name] = {"error": "%s: %s" % (type(e).__name__, e)}
 
     cpu = None
     if not a.no_cpu and rank == 0 and world == 1:
