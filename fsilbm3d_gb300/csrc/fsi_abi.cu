@@ -199,6 +199,8 @@ struct fsi_block {
     double *d_tolm = nullptr, *d_tol = nullptr;
     int16_t *d_ei = nullptr;
     float *d_ew = nullptr;
+    int *d_c64 = nullptr;       // fast forms: window cell and weight product of every stencil point
+    double *d_w64 = nullptr;
     double *h_tol = nullptr;  // pinned
     int *h_err = nullptr;     // pinned
     // cooperative IB solve of the fast forms
@@ -440,7 +442,7 @@ void free_block(fsi_block *h) {
     void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
                     h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
-                    h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf, h->og, h->tauf2};
+                    h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf, h->og, h->tauf2, h->d_c64, h->d_w64};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 6; k++)
@@ -1055,7 +1057,7 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     if ((long long)h->Mtot * 64 > 0x7fffffffLL) return fail(FSI_E_ARG, "too many markers");
     for (int k = 0; k < 6; k++) h->ibbc[k] = bc ? bc[k] : h->d.bndConds[k];
     void *ptrs[] = {h->d_offs, h->d_xyz, h->d_vel, h->d_area, h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew,
-                    h->d_aux, h->d_feat};
+                    h->d_aux, h->d_feat, h->d_c64, h->d_w64};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     h->d_aux = nullptr;
@@ -1072,6 +1074,8 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     CK(cudaMalloc((void **)&h->d_tol, sizeof(double) * 64));
     CK(cudaMalloc((void **)&h->d_ei, sizeof(int16_t) * 12 * Mt));
     CK(cudaMalloc((void **)&h->d_ew, sizeof(float) * 12 * Mt));
+    CK(cudaMalloc((void **)&h->d_c64, sizeof(int) * 64 * Mt));
+    CK(cudaMalloc((void **)&h->d_w64, sizeof(double) * 64 * Mt));
     CK(cudaMemcpyAsync(h->d_offs, h->offs.data(), sizeof(int) * (nbodies + 1), cudaMemcpyHostToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
     return FSI_OK;
@@ -1185,6 +1189,7 @@ void fill_ib(fsi_block *h, const double vf[3], double denIn, double dt, double U
     a.offs = h->d_offs;
     a.xyz = h->d_xyz; a.vel = h->d_vel; a.area = h->d_area;
     a.ei = h->d_ei; a.ew = h->d_ew;
+    a.c64 = h->d_c64; a.w64 = h->d_w64;
     a.eforce = h->d_eforce; a.fet = h->d_fet;
     a.wden = h->wden; a.wu = h->wu; a.wforce = h->wforce;
     a.ntol = ntol;

@@ -59,6 +59,10 @@ struct IbCoop {
     const double *xyz, *vel, *area;
     int16_t *ei;
     float *ew;
+    // per marker and stencil point (64 each): window cell and weight product
+    // rx ry rz, formed once per solve with the stencil
+    int *c64;
+    double *w64;
     double *eforce, *fet;
     double *wden, *wu, *wforce;
     int ntol;

@@ -1990,10 +1990,6 @@ __device__ __forceinline__ long long ib_wcell(const IbGeom &g, const int16_t *s,
            (long long)g.WZ * ((long long)(s[4 + ((p >> 2) & 3)] - 1 - g.wy0) + (long long)g.WY * (s[p >> 4] - 1 - g.wx0));
 }
 
-__device__ __forceinline__ double ib_weight(const float *w, int p) {
-    return ((double)w[p >> 4] * (double)w[4 + ((p >> 2) & 3)]) * (double)w[8 + (p & 3)];
-}
-
 // The IB stage of one block, by nth threads (tid = 0..nth-1) that meet at
 // bar(): the whole grid of a cooperative launch (k_ib_coop, grid barrier) or
 // one CTA (k_ib_batch, one block per CTA, __syncthreads).
@@ -2023,12 +2019,25 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
         a.wu[wc] = u0; a.wu[wc + Nw] = u1; a.wu[wc + 2 * Nw] = u2;
         a.wforce[wc] = a.vf[0]; a.wforce[wc + Nw] = a.vf[1]; a.wforce[wc + 2 * Nw] = a.vf[2];
     }
-    // UpdateElmtInterp_ and v_Eforce = 0 (Solidbody.f90:886-889)
+    // UpdateElmtInterp_ and v_Eforce = 0 (Solidbody.f90:886-889); with the
+    // stencil, the window cell and the weight product rx ry rz of each of its
+    // 64 points, which every phase below reads instead of forming them again
     for (long long m = tid; m < a.Mtot; m += nth) {
         int b = 0;
         while (b + 1 < a.nb && m >= a.offs[b + 1]) b++;
-        const int st = ib_stencil_one(a.xyz + 3LL * a.offs[b], a.xyz + 3 * m, g, a.ei + 12 * m, a.ew + 12 * m);
+        int16_t e[12];
+        float w[12];
+        const int st = ib_stencil_one(a.xyz + 3LL * a.offs[b], a.xyz + 3 * m, g, e, w);
         if (st) atomicOr(a.status, st);
+#pragma unroll
+        for (int k = 0; k < 12; k++) { a.ei[12 * m + k] = e[k]; a.ew[12 * m + k] = w[k]; }
+        double wd[12];
+#pragma unroll
+        for (int k = 0; k < 12; k++) wd[k] = (double)w[k];
+        for (int p = 0; p < 64; p++) {
+            a.c64[64 * m + p] = (int)ib_wcell(g, e, p);
+            a.w64[64 * m + p] = (wd[p >> 4] * wd[4 + ((p >> 2) & 3)]) * wd[8 + (p & 3)];
+        }
         a.eforce[3 * m] = 0.0; a.eforce[3 * m + 1] = 0.0; a.eforce[3 * m + 2] = 0.0;
     }
     for (long long i = tid; i < a.ntol; i += nth) a.tol_acc[i] = 0.0;
@@ -2042,12 +2051,10 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
     if (a.mlp || a.feat) {
         const float iU = (float)(1.0 / a.Uref);
         for (long long m = gw; m < a.Mtot; m += nw) {
-            const int16_t *s = a.ei + 12 * m;
-            const float *w = a.ew + 12 * m;
             double v0 = 0.0, v1 = 0.0, v2 = 0.0;
             for (int p = lane; p < 64; p += 32) {
-                const long long wc = ib_wcell(g, s, p);
-                const double wt = ib_weight(w, p);
+                const long long wc = __ldcg(a.c64 + 64 * m + p);
+                const double wt = __ldcg(a.w64 + 64 * m + p);
                 v0 += __ldcg(a.wu + wc) * wt;
                 v1 += __ldcg(a.wu + wc + Nw) * wt;
                 v2 += __ldcg(a.wu + wc + 2 * Nw) * wt;
@@ -2091,12 +2098,10 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
         if (a.mlp) {
             if (!bar()) return;
             for (long long m = gw; m < a.Mtot; m += nw) {
-                const int16_t *s = a.ei + 12 * m;
-                const float *w = a.ew + 12 * m;
                 const double f0 = __ldcg(a.fet + 3 * m), f1 = __ldcg(a.fet + 3 * m + 1), f2 = __ldcg(a.fet + 3 * m + 2);
                 for (int p = lane; p < 64; p += 32) {
-                    const long long wc = ib_wcell(g, s, p);
-                    const double wt = ib_weight(w, p);
+                    const long long wc = __ldcg(a.c64 + 64 * m + p);
+                    const double wt = __ldcg(a.w64 + 64 * m + p);
                     atomicAdd(a.wu + wc, -(f0 * wt));
                     atomicAdd(a.wu + wc + Nw, -(f1 * wt));
                     atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
@@ -2106,30 +2111,40 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
         }
     }
 
-    // the PenaltyForce_ loop, Solidbody.f90:893-906 (bodies one after another)
+    // the PenaltyForce_ loop, Solidbody.f90:893-906 (bodies one after another).
+    // A group of IB_GL lanes serves one marker (64 / IB_GL stencil points per
+    // lane), so that a warp has 32 / IB_GL markers in flight: the phases are
+    // chains of dependent L2 accesses, and more markers per warp shorten the
+    // number of chains a warp runs one after another.
+    constexpr int IB_GL = 8, IB_PTS = 64 / IB_GL, IB_MPW = 32 / IB_GL;
+    const int sub = lane / IB_GL, gl = lane % IB_GL;
     int it = 0;
     double dmax = 1e10;
     while (it < a.ntol && dmax > a.dtol) {
         for (int b = 0; b < a.nb; b++) {
             const int m0 = a.offs[b], m1 = a.offs[b + 1];
-            for (long long m = m0 + gw; m < m1; m += nw) {
-                const int16_t *s = a.ei + 12 * m;
-                const float *w = a.ew + 12 * m;
+            for (long long mb = m0 + gw * IB_MPW; mb < m1; mb += nw * IB_MPW) {
+                const long long m = mb + sub;
+                const bool act = m < m1;
                 double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-                for (int p = lane; p < 64; p += 32) {
-                    const long long wc = ib_wcell(g, s, p);
-                    const double wt = ib_weight(w, p);
-                    v0 += __ldcg(a.wu + wc) * wt;
-                    v1 += __ldcg(a.wu + wc + Nw) * wt;
-                    v2 += __ldcg(a.wu + wc + 2 * Nw) * wt;
+                if (act) {
+#pragma unroll
+                    for (int j = 0; j < IB_PTS; j++) {
+                        const int p = gl + IB_GL * j;
+                        const long long wc = __ldcg(a.c64 + 64 * m + p);
+                        const double wt = __ldcg(a.w64 + 64 * m + p);
+                        v0 += __ldcg(a.wu + wc) * wt;
+                        v1 += __ldcg(a.wu + wc + Nw) * wt;
+                        v2 += __ldcg(a.wu + wc + 2 * Nw) * wt;
+                    }
                 }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
+                for (int o = IB_GL / 2; o > 0; o >>= 1) {
                     v0 += __shfl_xor_sync(0xffffffffu, v0, o);
                     v1 += __shfl_xor_sync(0xffffffffu, v1, o);
                     v2 += __shfl_xor_sync(0xffffffffu, v2, o);
                 }
-                if (lane == 0) {
+                if (act && gl == 0) {
                     const double d0 = a.vel[3 * m] - v0, d1 = a.vel[3 * m + 1] - v1, d2 = a.vel[3 * m + 2] - v2;
                     const double ar = a.area[m];
                     const double F0 = d0 * ar, F1 = d1 * ar, F2 = d2 * ar;
@@ -2142,13 +2157,13 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
             }
             if (!bar()) return;
             // the velocity correction of the support (Solidbody.f90:1034-1048)
-            for (long long m = m0 + gw; m < m1; m += nw) {
-                const int16_t *s = a.ei + 12 * m;
-                const float *w = a.ew + 12 * m;
+            for (long long m = m0 + gw * IB_MPW + sub; m < m1; m += nw * IB_MPW) {
                 const double f0 = __ldcg(a.fet + 3 * m), f1 = __ldcg(a.fet + 3 * m + 1), f2 = __ldcg(a.fet + 3 * m + 2);
-                for (int p = lane; p < 64; p += 32) {
-                    const long long wc = ib_wcell(g, s, p);
-                    const double wt = ib_weight(w, p);
+#pragma unroll
+                for (int j = 0; j < IB_PTS; j++) {
+                    const int p = gl + IB_GL * j;
+                    const long long wc = __ldcg(a.c64 + 64 * m + p);
+                    const double wt = __ldcg(a.w64 + 64 * m + p);
                     atomicAdd(a.wu + wc, -(f0 * wt));
                     atomicAdd(a.wu + wc + Nw, -(f1 * wt));
                     atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
@@ -2165,14 +2180,14 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
         it = it + 1;
     }
     // FluidVolumeForce_ spreading (Solidbody.f90:968-977) onto vf
-    for (long long m = gw; m < a.Mtot; m += nw) {
-        const int16_t *s = a.ei + 12 * m;
-        const float *w = a.ew + 12 * m;
+    for (long long m = gw * IB_MPW + sub; m < a.Mtot; m += nw * IB_MPW) {
         const double f0 = __ldcg(a.eforce + 3 * m) * a.invh3s, f1 = __ldcg(a.eforce + 3 * m + 1) * a.invh3s,
                      f2 = __ldcg(a.eforce + 3 * m + 2) * a.invh3s;
-        for (int p = lane; p < 64; p += 32) {
-            const long long wc = ib_wcell(g, s, p);
-            const double wt = ib_weight(w, p);
+#pragma unroll
+        for (int j = 0; j < IB_PTS; j++) {
+            const int p = gl + IB_GL * j;
+            const long long wc = __ldcg(a.c64 + 64 * m + p);
+            const double wt = __ldcg(a.w64 + 64 * m + p);
             atomicAdd(a.wforce + wc, -(f0 * wt));
             atomicAdd(a.wforce + wc + Nw, -(f1 * wt));
             atomicAdd(a.wforce + wc + 2 * Nw, -(f2 * wt));
