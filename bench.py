@@ -749,8 +749,8 @@ DATA = "synthetic (uniform inflow initial field; flexible plate from rest, leadi
 def headline_config(world):
     """the line's config, the same on both arms"""
     return {"workload": WORKLOAD, "grid": list(FSI_GRID), "collision": "MRT", "markers": FSI_NODES * FSI_NODES,
-            "plate": "33 beam elements, KB=%g KS=%g mass ratio %g, Newmark beta=0.25 gamma=0.5" %
-                     (PLATE_KB, PLATE_KS, PLATE_DENR),
+            "plate": "33 beam elements, KB=%g KS=%g mass ratio %g, Newmark beta=%g gamma=%g" %
+                     (PLATE_KB, PLATE_KS, PLATE_DENR, BEAM_SOLVER["NewmarkBeta"], BEAM_SOLVER["NewmarkGamma"]),
             "ib": "ntol=%d dtol=%g" % (NTOL, DTOL), "parallelism": "replicas" if world > 1 else "1 GPU",
             "l2": "inputs larger than L2 (two 1.9 GB distribution buffers)"}
 

@@ -46,6 +46,7 @@ class RigidPlate:
         self.Lspan = 0.5 * self.span
         self.spanlen = 0.5 * self.span + self.Lspan
         self.dirc = np.array([0.0, 0.0, 1.0])
+        self._span_off = None  # dirc * span station of every marker, formed on first use
 
     @property
     def M(self):
@@ -67,11 +68,15 @@ class RigidPlate:
         pos = self.x00 + XYZ  # MapReferencePosToCurrent with TTT = I
         beta = -self.alpha * 2.0 * self.denIn
         mid = 0.5 * (pos[:-1] + pos[1:])                            # element centres
-        len1 = np.sqrt(np.sum((pos[1:] - pos[:-1]) ** 2, axis=1))   # element lengths
+        e = pos[1:] - pos[:-1]
+        len1 = np.sqrt((e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1]) + e[:, 2] * e[:, 2])  # element lengths
         dl = self.spanlen / self.n_span
-        ls = dl * (0.5 + np.arange(self.n_span)) - self.Lspan       # span stations
-        xyz = (mid[:, None, :] + self.dirc[None, None, :] * ls[None, :, None]).reshape(self.M, 3)
-        vel = np.broadcast_to(UVW, (self.M, 3)).copy()
+        if self._span_off is None:
+            ls = dl * (0.5 + np.arange(self.n_span)) - self.Lspan   # span stations
+            self._span_off = self.dirc[None, None, :] * ls[None, :, None]
+        xyz = (mid[:, None, :] + self._span_off).reshape(self.M, 3)
+        vel = np.empty((self.M, 3))
+        vel[:] = UVW
         area = np.repeat(dl * len1 * beta, self.n_span)
         return xyz, vel, area
 

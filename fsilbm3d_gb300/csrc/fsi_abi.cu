@@ -156,6 +156,9 @@ void mrt_moment_form(MrtMats &m) {
     m.diag = ok ? 1 : 0;
 }
 
+// the device status words (8 ints) followed by the IB residual (a double)
+constexpr size_t STAT_BYTES = sizeof(int) * 8 + sizeof(double);
+
 }  // namespace
 
 struct fsi_block {
@@ -195,7 +198,10 @@ struct fsi_block {
     std::vector<int> M, offs;
     int ibbc[6] = {0, 0, 0, 0, 0, 0};
     int *d_offs = nullptr, *d_err = nullptr;
+    // d_vel and d_area point into the d_xyz allocation ([xyz 3M][vel 3M][area M]);
+    // h_mk is its pinned mirror, so that one copy uploads the markers
     double *d_xyz = nullptr, *d_vel = nullptr, *d_area = nullptr, *d_eforce = nullptr, *d_fet = nullptr;
+    double *h_mk = nullptr;
     double *d_tolm = nullptr, *d_tol = nullptr;
     int16_t *d_ei = nullptr;
     float *d_ew = nullptr;
@@ -208,7 +214,7 @@ struct fsi_block {
     // 8 ints: IB flags, iterations, barrier count, generation; [4] the step
     // kernel's error word (bit 1: a bounded wait ran out)
     int *d_status = nullptr;
-    int *h_stat = nullptr;  // pinned copy of d_status[0..5)
+    int *h_stat = nullptr;  // pinned copy of d_status (STAT_BYTES: 8 status words, the IB residual)
     double *d_res = nullptr, *d_tolacc = nullptr;
     int tolacc_cap = 0;
     // warm start: per-marker auxiliary inputs and logged features
@@ -218,7 +224,7 @@ struct fsi_block {
     // IB window
     IbGeom geom{};
     long long Nw = 0, Nw_cap = 0;
-    double *wden = nullptr, *wu = nullptr, *wforce = nullptr;
+    double *wden = nullptr, *wu = nullptr, *wforce = nullptr, *wu2 = nullptr, *dlt = nullptr;
     int *cnt = nullptr, *start = nullptr, *fillc = nullptr, *list = nullptr;
     long long list_cap = 0;
     bool win_valid = false;
@@ -439,9 +445,9 @@ int check_kerr(fsi_block *h) {
 void free_block(fsi_block *h) {
     if (!h) return;
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
-    void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz, h->d_vel, h->d_area,
+    void *ptrs[] = {h->fa, h->fb, h->den, h->u, h->stage, h->d_offs, h->d_err, h->d_xyz,
                     h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew, h->wden, h->wu, h->wforce,
-                    h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_res, h->d_tolacc, h->d_aux,
+                    h->wu2, h->dlt, h->cnt, h->start, h->fillc, h->list, h->d_status, h->d_tolacc, h->d_aux,
                     h->d_feat, h->d_out, h->tau_all, h->tauf, h->uf, h->og, h->tauf2, h->d_c64, h->d_w64};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -450,6 +456,7 @@ void free_block(fsi_block *h) {
     if (h->h_tol) cudaFreeHost(h->h_tol);
     if (h->h_err) cudaFreeHost(h->h_err);
     if (h->h_stat) cudaFreeHost(h->h_stat);
+    if (h->h_mk) cudaFreeHost(h->h_mk);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->ev_ib) cudaEventDestroy(h->ev_ib);
@@ -612,9 +619,11 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     chk(cudaHostAlloc((void **)&h->h_tol, sizeof(double) * 64, cudaHostAllocDefault));
     chk(cudaHostAlloc((void **)&h->h_err, sizeof(int), cudaHostAllocDefault));
     chk(cudaMalloc((void **)&h->d_err, sizeof(int)));
-    chk(cudaMalloc((void **)&h->d_status, sizeof(int) * 8));
-    chk(cudaMalloc((void **)&h->d_res, sizeof(double)));
-    chk(cudaHostAlloc((void **)&h->h_stat, sizeof(int) * 8, cudaHostAllocDefault));
+    // the status words and the IB residual in one allocation (and one pinned
+    // mirror), so that one copy brings both back
+    chk(cudaMalloc((void **)&h->d_status, STAT_BYTES));
+    if (h->d_status) h->d_res = (double *)(h->d_status + 8);
+    chk(cudaHostAlloc((void **)&h->h_stat, STAT_BYTES, cudaHostAllocDefault));
     // every device operation of a block goes to its own (non-blocking)
     // stream: work on the legacy default stream would not be ordered with it
     if (e == cudaSuccess) chk(cudaMemsetAsync(h->den, 0, sizeof(double) * h->N, h->st));
@@ -1056,18 +1065,22 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     h->Mtot = h->offs[nbodies];
     if ((long long)h->Mtot * 64 > 0x7fffffffLL) return fail(FSI_E_ARG, "too many markers");
     for (int k = 0; k < 6; k++) h->ibbc[k] = bc ? bc[k] : h->d.bndConds[k];
-    void *ptrs[] = {h->d_offs, h->d_xyz, h->d_vel, h->d_area, h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew,
+    void *ptrs[] = {h->d_offs, h->d_xyz, h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew,
                     h->d_aux, h->d_feat, h->d_c64, h->d_w64};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (h->h_mk) cudaFreeHost(h->h_mk);
+    h->h_mk = nullptr;
+    h->d_xyz = h->d_vel = h->d_area = nullptr;
     h->d_aux = nullptr;
     h->d_feat = nullptr;
     h->warm_cap = 0;
     int Mt = std::max(1, h->Mtot);
     CK(cudaMalloc((void **)&h->d_offs, sizeof(int) * (nbodies + 1)));
-    CK(cudaMalloc((void **)&h->d_xyz, sizeof(double) * 3 * Mt));
-    CK(cudaMalloc((void **)&h->d_vel, sizeof(double) * 3 * Mt));
-    CK(cudaMalloc((void **)&h->d_area, sizeof(double) * Mt));
+    CK(cudaMalloc((void **)&h->d_xyz, sizeof(double) * 7 * Mt));
+    h->d_vel = h->d_xyz + 3 * Mt;
+    h->d_area = h->d_xyz + 6 * Mt;
+    CK(cudaHostAlloc((void **)&h->h_mk, sizeof(double) * 7 * Mt, cudaHostAllocDefault));
     CK(cudaMalloc((void **)&h->d_eforce, sizeof(double) * 3 * Mt));
     CK(cudaMalloc((void **)&h->d_fet, sizeof(double) * 3 * Mt));
     CK(cudaMalloc((void **)&h->d_tolm, sizeof(double) * Mt));
@@ -1116,19 +1129,22 @@ int compute_window(fsi_block *h, const double *xyz) {
     IbGeom &g = h->geom;
     g.X = h->X; g.Y = h->Y; g.Z = h->Z;
     g.dh = h->d.dh; g.xmin = h->d.xmin; g.ymin = h->d.ymin; g.zmin = h->d.zmin;
+    g.invdh = 1.0 / h->d.dh;
     for (int k = 0; k < 6; k++) g.bc[k] = h->ibbc[k];
     g.wx0 = box[0]; g.wx1 = box[1]; g.wy0 = box[2]; g.wy1 = box[3]; g.wz0 = box[4]; g.wz1 = box[5];
     g.WY = box[3] - box[2] + 1;
     g.WZ = box[5] - box[4] + 1;
     h->Nw = (long long)(box[1] - box[0] + 1) * g.WY * g.WZ;
     if (h->Nw > h->Nw_cap) {
-        void *ptrs[] = {h->wden, h->wu, h->wforce, h->cnt, h->start, h->fillc};
+        void *ptrs[] = {h->wden, h->wu, h->wforce, h->wu2, h->dlt, h->cnt, h->start, h->fillc};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         long long cap = h->Nw + h->Nw / 2 + 1024;
         CK(cudaMalloc((void **)&h->wden, sizeof(double) * cap));
         CK(cudaMalloc((void **)&h->wu, sizeof(double) * 3 * cap));
         CK(cudaMalloc((void **)&h->wforce, sizeof(double) * 3 * cap));
+        CK(cudaMalloc((void **)&h->wu2, sizeof(double) * 3 * cap));
+        CK(cudaMalloc((void **)&h->dlt, sizeof(double) * 9 * cap));
         CK(cudaMalloc((void **)&h->cnt, sizeof(int) * cap));
         CK(cudaMalloc((void **)&h->start, sizeof(int) * (cap + 1)));
         CK(cudaMalloc((void **)&h->fillc, sizeof(int) * cap));
@@ -1192,6 +1208,7 @@ void fill_ib(fsi_block *h, const double vf[3], double denIn, double dt, double U
     a.c64 = h->d_c64; a.w64 = h->d_w64;
     a.eforce = h->d_eforce; a.fet = h->d_fet;
     a.wden = h->wden; a.wu = h->wu; a.wforce = h->wforce;
+    a.wu2 = h->wu2; a.dlt = h->dlt;
     a.ntol = ntol;
     a.dtol = dtol;
     a.dsumU = (double)h->Mtot * Uref;
@@ -1246,8 +1263,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
             CK(launch_ib_cluster(a, h->prec, h->st2));
         }
         CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st2));
-        CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st2));
-        CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st2));
+        CK(cudaMemcpyAsync(h->h_stat, h->d_status, STAT_BYTES, cudaMemcpyDeviceToHost, h->st2));
         CK(cudaEventRecord(h->ev_ib, h->st2));
         h->win_valid = true;
         int rc = enqueue_step(h, wm.step_vf, wm.step_time, true, h->ev_ib);
@@ -1273,8 +1289,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
             h->h_ef_cap = h->Mtot;
         }
         CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->h_stat, h->d_status, STAT_BYTES, cudaMemcpyDeviceToHost, h->st));
         CK(cudaEventRecord(h->ev_ib, h->st));
         h->win_valid = true;
         int rc = enqueue_step(h, wm.step_vf, wm.step_time, true);
@@ -1286,8 +1301,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
         if (wm.features)
             CK(cudaMemcpyAsync(wm.features, h->d_feat, sizeof(float) * 12 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(h->h_stat, h->d_status, sizeof(int) * 5, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(h->h_tol, h->d_res, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->h_stat, h->d_status, STAT_BYTES, cudaMemcpyDeviceToHost, h->st));
         CK(cudaStreamSynchronize(h->st));
     }
     }
@@ -1299,7 +1313,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     if (st & 8) return fail(FSI_E_TIMEOUT, "IB grid barrier timed out");
     const int it = h->h_stat[1];
     if (iters) *iters = it;
-    if (residual) *residual = h->h_tol[0];
+    if (residual) *residual = *(const double *)(h->h_stat + 8);
     h->win_valid = !wm.step;
     return FSI_OK;
 }
@@ -1310,9 +1324,13 @@ int ib_upload(fsi_block *h, const double *xyz, const double *vel, const double *
     if (rc) return rc;
     const int Mt = h->Mtot;
     if (!st) st = h->st;
-    CK(cudaMemcpyAsync(h->d_xyz, xyz, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(h->d_vel, vel, sizeof(double) * 3 * Mt, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(h->d_area, area, sizeof(double) * Mt, cudaMemcpyHostToDevice, st));
+    // through the pinned mirror: every caller waits for its IB stage (which
+    // follows this copy on the stream) before it returns, so the mirror is
+    // free again when the next call fills it
+    memcpy(h->h_mk, xyz, sizeof(double) * 3 * Mt);
+    memcpy(h->h_mk + 3 * Mt, vel, sizeof(double) * 3 * Mt);
+    memcpy(h->h_mk + 6 * Mt, area, sizeof(double) * Mt);
+    CK(cudaMemcpyAsync(h->d_xyz, h->h_mk, sizeof(double) * 7 * Mt, cudaMemcpyHostToDevice, st));
     return FSI_OK;
 }
 

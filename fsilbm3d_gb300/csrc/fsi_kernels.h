@@ -25,6 +25,7 @@ cudaError_t launch_halfway_f64(const double *f, double *hw, int X, int Y, int Z,
 struct IbGeom {
     int X, Y, Z;
     double dh, xmin, ymin, zmin;
+    double invdh;  // 1 / dh, correctly rounded (formed on the host)
     int bc[6];
     int wx0, wx1, wy0, wy1, wz0, wz1, WY, WZ;
 };
@@ -65,6 +66,9 @@ struct IbCoop {
     double *w64;
     double *eforce, *fet;
     double *wden, *wu, *wforce;
+    // the fast forms' penalty loop: the second window-velocity buffer (3 Nw)
+    // and three slots of velocity corrections (9 Nw)
+    double *wu2, *dlt;
     int ntol;
     double dtol, dsumU, invh3p, invh3s;
     double *tol_acc;  // ntol sums

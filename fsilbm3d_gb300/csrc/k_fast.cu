@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <mutex>
+#include <type_traits>
 
 #include "bc_impl.cuh"
 #include "dw.cuh"
@@ -1959,111 +1960,197 @@ __global__ void k_win_macro_fast(const void *__restrict__ fs, double *wden, doub
 // (__ldcg): L1 is not coherent across SMs.
 // ---------------------------------------------------------------------------
 
-// grid barrier with an iteration limit: on timeout the status gets bit 8 and
-// every CTA returns
-__device__ __forceinline__ bool gbar(int *status, unsigned nblk) {
+// grid barrier with an iteration limit. The arrival counter (status[2],
+// zeroed by the host before each launch) only grows: the k-th barrier of a
+// launch waits for k * nblk arrivals, one release-add and acquire polls of a
+// single word. On timeout the status gets bit 8 and the CTA returns false;
+// the other CTAs then time out at their next barrier.
+__device__ __forceinline__ bool gbar(int *status, unsigned nblk, unsigned &target) {
+    __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned *cnt = (unsigned *)(status + 2);
-        volatile unsigned *gen = (volatile unsigned *)(status + 3);
-        const unsigned g0 = *gen;
-        __threadfence();
-        if (atomicAdd(cnt, 1u) == nblk - 1) {
-            *cnt = 0;
-            __threadfence();
-            atomicAdd((unsigned *)(status + 3), 1u);
-        } else {
-            long long it = 0;
-            while (*gen == g0) {
-                if (++it > (1LL << 24)) { atomicOr(status, 8); break; }
-                __nanosleep(64);
+        target += nblk;
+        unsigned v;
+        asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(v) : "l"(cnt) : "memory");
+        v += 1u;
+        int good = 1;
+        for (long long it = 0; (int)(v - target) < 0; it++) {
+            if (it > (1LL << 21)) {
+                atomicOr(status, 8);
+                good = 0;
+                break;
             }
+            asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
         }
-        __threadfence();
+        ok = good;
     }
     __syncthreads();
-    return (*(volatile int *)status & 8) == 0;
+    return ok != 0;
 }
 
-__device__ __forceinline__ long long ib_wcell(const IbGeom &g, const int16_t *s, int p) {
-    return (long long)(s[8 + (p & 3)] - 1 - g.wz0) +
-           (long long)g.WZ * ((long long)(s[4 + ((p >> 2) & 3)] - 1 - g.wy0) + (long long)g.WY * (s[p >> 4] - 1 - g.wx0));
-}
-
-// The IB stage of one block, by nth threads (tid = 0..nth-1) that meet at
-// bar(): the whole grid of a cooperative launch (k_ib_coop, grid barrier) or
-// one CTA (k_ib_batch, one block per CTA, __syncthreads).
+// The IB stage of one block, by nth threads (tid = 0..nth-1, tid = CTA *
+// blockDim.x + thread) that meet at bar(): the whole grid of a cooperative
+// launch (k_ib_coop, grid barrier) or one cluster (k_ib_cluster, k_ib_batch).
+//
+// The penalty loop runs one barrier per stage (a stage = one body in one
+// iteration, Solidbody.f90:893-906): stage s interpolates the window velocity
+// V_s = P_s + D_{s-1} and scatters its velocity corrections into D_s, where
+// P_s (two ping-pong buffers) holds V_{s-1} and D (three rotating slots) the
+// corrections of one stage each. The stage's owner pass writes P_{s+1} =
+// P_s + D_{s-1} and clears D_{s-2}, the slot that D_{s+1} reuses. No stage
+// writes what it reads, so the interpolation and the correction of a stage
+// need no barrier between them.
+//
+// Arithmetic of the loop (R): FP32 for the offset forms, whose distributions
+// carry FP32 arithmetic (GB300 runs FP64 at a small fraction of the FP32
+// rate, and every FP64 warp instruction of a phase is on its critical path);
+// FP64 for the FP64-storage forms. With R = FP32 the two P buffers live in
+// wu2 and the correction slots, the spreading sums and the Lagrangian-force
+// sums in dlt, w64 and fet (each sized for FP64); the window's den, u and
+// force (read by the step's window fix-up) and the Lagrangian force stay FP64.
 template <int P, class BAR>
 __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long long nth, BAR &&bar) {
     using T = ST<P>;
     using C = typename T::C;
+    constexpr bool F32IB = std::is_same<C, float>::value;
+    using R = typename std::conditional<F32IB, float, double>::type;
+    constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const long long gw = tid >> 5, nw = nth >> 5;
+    // warps numbered across the CTAs first (warp w of CTA b is w * nblk + b),
+    // so that the few warps that hold markers are spread over all the CTAs'
+    // SMs; window cells (own) go to the CTAs' last threads first, which hold
+    // no marker unless the markers fill the grid
+    const long long bd = blockDim.x, nblk = nth / bd, t = tid % bd;
+    const long long gw = (t >> 5) * nblk + tid / bd, nw = nth >> 5;
+    const long long own = (bd - 1 - t) * nblk + tid / bd;
     const IbGeom &g = a.g;
     const long long Nw = a.Nw;
+    R *const P0 = F32IB ? (R *)a.wu2 : (R *)a.wu;
+    R *const P1 = F32IB ? (R *)a.wu2 + 3 * Nw : (R *)a.wu2;
+    R *const D = (R *)a.dlt;
+    float *const Sp = (float *)a.dlt + 9 * Nw;  // R = FP32: spreading sums (3 Nw)
+    R *const W64 = (R *)a.w64;
+    float *const efs = (float *)a.fet;          // R = FP32: Lagrangian-force sums (3 Mtot)
+    // a group of IB_GL lanes serves one marker, IB_PTS of its 64 stencil
+    // points each: point p = gl + IB_GL j has z offset gl & 3, y offset
+    // ((gl >> 2) & 1) + 2 (j & 1) and x offset j >> 1
+    constexpr int IB_GL = 8, IB_PTS = 64 / IB_GL, IB_MPW = 32 / IB_GL;
+    const int sub = lane / IB_GL, gl = lane % IB_GL;
 
-    // calculate_macro_quantities_ and the force reset + add_volume_force_ on the window
+    // calculate_macro_quantities_ and the force reset + add_volume_force_ on
+    // the window; the correction slots (and spreading sums) cleared
     const C vf[3] = {(C)a.vf[0], (C)a.vf[1], (C)a.vf[2]};
-    for (long long wc = tid; wc < Nw; wc += nth) {
+    for (long long wc = own; wc < Nw; wc += nth) {
         const int wz = (int)(wc % g.WZ);
-        const long long t = wc / g.WZ;
-        const int wy = (int)(t % g.WY), wx = (int)(t / g.WY);
+        const long long r = wc / g.WZ;
+        const int wy = (int)(r % g.WY), wx = (int)(r / g.WY);
         const long long c = cidx(wz + g.wz0, wy + g.wy0, wx + g.wx0, g.Z, g.Y);
         const typename T::S *src = (const typename T::S *)a.f;
-        C gl[Q];
+        C fl[Q];
 #pragma unroll
-        for (int i = 0; i < Q; i++) gl[i] = T::dec(src[c + a.N * i]);
+        for (int i = 0; i < Q; i++) fl[i] = T::dec(src[c + a.N * i]);
         C rho, drho, u0, u1, u2;
-        macro_fast<P>(gl, vf, (C)g.dh, rho, drho, u0, u1, u2);
+        macro_fast<P>(fl, vf, (C)g.dh, rho, drho, u0, u1, u2);
         a.wden[wc] = T::OFF ? 1.0 + (double)drho : (double)rho;
-        a.wu[wc] = u0; a.wu[wc + Nw] = u1; a.wu[wc + 2 * Nw] = u2;
+        P0[wc] = (R)u0; P0[wc + Nw] = (R)u1; P0[wc + 2 * Nw] = (R)u2;
         a.wforce[wc] = a.vf[0]; a.wforce[wc + Nw] = a.vf[1]; a.wforce[wc + 2 * Nw] = a.vf[2];
-    }
-    // UpdateElmtInterp_ and v_Eforce = 0 (Solidbody.f90:886-889); with the
-    // stencil, the window cell and the weight product rx ry rz of each of its
-    // 64 points, which every phase below reads instead of forming them again
-    for (long long m = tid; m < a.Mtot; m += nth) {
-        int b = 0;
-        while (b + 1 < a.nb && m >= a.offs[b + 1]) b++;
-        int16_t e[12];
-        float w[12];
-        const int st = ib_stencil_one(a.xyz + 3LL * a.offs[b], a.xyz + 3 * m, g, e, w);
-        if (st) atomicOr(a.status, st);
 #pragma unroll
-        for (int k = 0; k < 12; k++) { a.ei[12 * m + k] = e[k]; a.ew[12 * m + k] = w[k]; }
-        double wd[12];
+        for (int k = 0; k < 9; k++) D[wc + k * Nw] = (R)0;
+        if (F32IB) {
 #pragma unroll
-        for (int k = 0; k < 12; k++) wd[k] = (double)w[k];
-        for (int p = 0; p < 64; p++) {
-            a.c64[64 * m + p] = (int)ib_wcell(g, e, p);
-            a.w64[64 * m + p] = (wd[p >> 4] * wd[4 + ((p >> 2) & 3)]) * wd[8 + (p & 3)];
+            for (int k = 0; k < 3; k++) Sp[wc + k * Nw] = 0.0f;
         }
-        a.eforce[3 * m] = 0.0; a.eforce[3 * m + 1] = 0.0; a.eforce[3 * m + 2] = 0.0;
+    }
+    // UpdateElmtInterp_ and v_Eforce = 0 (Solidbody.f90:886-889): the group
+    // forms the stencil and writes the window cell and the weight product
+    // rx ry rz of each of its 64 points, which every phase below reads
+    // instead of forming them again. The registers rwc/rwt (and the marker's
+    // velocity ub and area ar) hold those of marker cm, the last marker this
+    // lane group read.
+    long long cm = -1;
+    int rwc[IB_PTS];
+    R rwt[IB_PTS];
+    R ub[3] = {(R)0, (R)0, (R)0}, ar = (R)0;
+    for (long long mb = gw * IB_MPW; mb < a.Mtot; mb += nw * IB_MPW) {
+        const long long m = mb + sub;
+        const bool act = m < a.Mtot;
+        int b = 0;
+        if (act)
+            while (b + 1 < a.nb && m >= a.offs[b + 1]) b++;
+        int e[12];
+        float w[12];
+        const long long mm = act ? m : 0;
+        const int st = ib_stencil_group(a.xyz + 3LL * a.offs[b], a.xyz + 3 * mm, g, gl, act, e, w);
+        if (st && gl == 0) atomicOr(a.status, st);
+        if (act) {
+#pragma unroll
+            for (int k = 0; k < 12; k++)
+                if (k % IB_GL == gl) { a.ei[12 * m + k] = (int16_t)e[k]; a.ew[12 * m + k] = w[k]; }
+            const int zi = gl & 3, yi = (gl >> 2) & 1;
+            const int ez = zi == 0 ? e[8] : (zi == 1 ? e[9] : (zi == 2 ? e[10] : e[11]));
+            const float wz = zi == 0 ? w[8] : (zi == 1 ? w[9] : (zi == 2 ? w[10] : w[11]));
+            const int ey0 = yi ? e[5] : e[4], ey1 = yi ? e[7] : e[6];
+            const float wy0 = yi ? w[5] : w[4], wy1 = yi ? w[7] : w[6];
+            const long long cz = (long long)(ez - 1 - g.wz0);
+#pragma unroll
+            for (int j = 0; j < IB_PTS; j++) {
+                const int ey = (j & 1) ? ey1 : ey0;
+                const float wy = (j & 1) ? wy1 : wy0;
+                rwc[j] = (int)(cz + (long long)g.WZ * ((long long)(ey - 1 - g.wy0) +
+                                                       (long long)g.WY * (long long)(e[j >> 1] - 1 - g.wx0)));
+                rwt[j] = ((R)w[j >> 1] * (R)wy) * (R)wz;
+                a.c64[64 * m + gl + IB_GL * j] = rwc[j];
+                W64[64 * m + gl + IB_GL * j] = rwt[j];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) ub[k] = (R)a.vel[3 * m + k];
+            ar = (R)a.area[m];
+            cm = m;
+            if (gl < 3) {
+                a.eforce[3 * m + gl] = 0.0;
+                if (F32IB) efs[3 * m + gl] = 0.0f;
+            }
+        }
     }
     for (long long i = tid; i < a.ntol; i += nth) a.tol_acc[i] = 0.0;
     if (!bar()) return;
     if (*(volatile int *)a.status & 3) return;
+    // the points, velocity and area of marker m in the registers
+    auto points = [&](long long m) {
+        if (m == cm) return;
+#pragma unroll
+        for (int j = 0; j < IB_PTS; j++) {
+            rwc[j] = __ldcg(a.c64 + 64 * m + gl + IB_GL * j);
+            rwt[j] = __ldcg(W64 + 64 * m + gl + IB_GL * j);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) ub[k] = (R)a.vel[3 * m + k];
+        ar = (R)a.area[m];
+        cm = m;
+    };
 
     // learned warm start (no counterpart in the reference): features of every
     // marker from the uncorrected window velocity; with a network, its
-    // predicted force becomes the first correction, applied to all bodies at
-    // once, and the penalty loop below continues from it
+    // predicted force becomes the first correction (into D_{-1}, the slot the
+    // first stage reads), applied to all bodies at once, and the penalty loop
+    // below continues from it
     if (a.mlp || a.feat) {
         const float iU = (float)(1.0 / a.Uref);
         for (long long m = gw; m < a.Mtot; m += nw) {
             double v0 = 0.0, v1 = 0.0, v2 = 0.0;
             for (int p = lane; p < 64; p += 32) {
                 const long long wc = __ldcg(a.c64 + 64 * m + p);
-                const double wt = __ldcg(a.w64 + 64 * m + p);
-                v0 += __ldcg(a.wu + wc) * wt;
-                v1 += __ldcg(a.wu + wc + Nw) * wt;
-                v2 += __ldcg(a.wu + wc + 2 * Nw) * wt;
+                const double wt = (double)__ldcg(W64 + 64 * m + p);
+                v0 += (double)__ldcg(P0 + wc) * wt;
+                v1 += (double)__ldcg(P0 + wc + Nw) * wt;
+                v2 += (double)__ldcg(P0 + wc + 2 * Nw) * wt;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                v0 += __shfl_xor_sync(0xffffffffu, v0, o);
-                v1 += __shfl_xor_sync(0xffffffffu, v1, o);
-                v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+                v0 += __shfl_xor_sync(FULL, v0, o);
+                v1 += __shfl_xor_sync(FULL, v1, o);
+                v2 += __shfl_xor_sync(FULL, v2, o);
             }
             float x[MLP_IN];
             x[0] = (float)(a.vel[3 * m] - v0) * iU;
@@ -2084,126 +2171,242 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
             if (a.mlp) {
                 float y[MLP_OUT];
                 mlp_forward_warp(a.mlp, a.mlp_nrm, x, lane, y);
+                const double sc = a.area[m] * a.Uref;
+                double F[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) F[k] = (double)__shfl_sync(FULL, y[k], 0) * sc;
                 if (lane == 0) {
-                    const double sc = a.area[m] * a.Uref;
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
-                        const double F = (double)y[k] * sc;
-                        a.eforce[3 * m + k] = F;
-                        a.fet[3 * m + k] = F * a.invh3p;
+                        a.eforce[3 * m + k] = F[k];
+                        if (F32IB) efs[3 * m + k] = (float)F[k];
                     }
                 }
-            }
-        }
-        if (a.mlp) {
-            if (!bar()) return;
-            for (long long m = gw; m < a.Mtot; m += nw) {
-                const double f0 = __ldcg(a.fet + 3 * m), f1 = __ldcg(a.fet + 3 * m + 1), f2 = __ldcg(a.fet + 3 * m + 2);
+                const R f0 = (R)(F[0] * a.invh3p), f1 = (R)(F[1] * a.invh3p), f2 = (R)(F[2] * a.invh3p);
+                R *Dm = D + 6 * Nw;
                 for (int p = lane; p < 64; p += 32) {
                     const long long wc = __ldcg(a.c64 + 64 * m + p);
-                    const double wt = __ldcg(a.w64 + 64 * m + p);
-                    atomicAdd(a.wu + wc, -(f0 * wt));
-                    atomicAdd(a.wu + wc + Nw, -(f1 * wt));
-                    atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
+                    const R wt = __ldcg(W64 + 64 * m + p);
+                    atomicAdd(Dm + wc, -(f0 * wt));
+                    atomicAdd(Dm + wc + Nw, -(f1 * wt));
+                    atomicAdd(Dm + wc + 2 * Nw, -(f2 * wt));
                 }
             }
-            if (!bar()) return;
         }
+        if (a.mlp && !bar()) return;
     }
 
-    // the PenaltyForce_ loop, Solidbody.f90:893-906 (bodies one after another).
-    // A group of IB_GL lanes serves one marker (64 / IB_GL stencil points per
-    // lane), so that a warp has 32 / IB_GL markers in flight: the phases are
-    // chains of dependent L2 accesses, and more markers per warp shorten the
-    // number of chains a warp runs one after another.
-    constexpr int IB_GL = 8, IB_PTS = 64 / IB_GL, IB_MPW = 32 / IB_GL;
-    const int sub = lane / IB_GL, gl = lane % IB_GL;
+    // the PenaltyForce_ loop, Solidbody.f90:893-906 (bodies one after another,
+    // one stage each); in the last iteration the cap allows, each stage also
+    // spreads its markers' final force (FluidVolumeForce_, Solidbody.f90:968-977)
+    const R ih3p = (R)a.invh3p, ih3s = (R)a.invh3s;
+    const float stopf = (float)(a.dtol * a.dsumU);  // R = FP32: the residual test tol > dtol M U
     int it = 0;
+    long long s = 0;
     double dmax = 1e10;
-    while (it < a.ntol && dmax > a.dtol) {
-        for (int b = 0; b < a.nb; b++) {
+    R tol = (R)0;
+    bool stop = !(dmax > a.dtol), nan = false;
+    // the residual test of iteration it - 1 (tol_acc complete after the
+    // barrier); false: the loop stops
+    auto test = [&](R tl) {
+        tol = tl;
+        if (!isfinite(tol)) {
+            nan = true;
+            return false;
+        }
+        if (F32IB) {
+            stop = !((float)tol > stopf);
+        } else {
+            dmax = (double)tol / a.dsumU;
+            stop = !(dmax > a.dtol);
+        }
+        return !stop;
+    };
+    while (it < a.ntol && !stop) {
+        const bool last = it == a.ntol - 1;
+        for (int b = 0; b < a.nb; b++, s++) {
+            const R *Pk = (s & 1) ? P1 : P0;
+            R *Pn = (s & 1) ? P0 : P1;
+            const R *Dr = D + 3 * Nw * ((s + 2) % 3);
+            R *Dw = D + 3 * Nw * (s % 3);
+            R *Dz = D + 3 * Nw * ((s + 1) % 3);
             const int m0 = a.offs[b], m1 = a.offs[b + 1];
+            // the first stage of an iteration reads the previous iteration's
+            // residual beside its own loads (its first window cell and
+            // marker) and writes nothing before the test
+            bool decided = !(b == 0 && it > 0);
+            R tprev = (R)0;
+            if (!decided) tprev = F32IB ? (R)__ldcg((const float *)a.tol_acc + it - 1) : (R)__ldcg(a.tol_acc + it - 1);
+            R ow[3] = {(R)0, (R)0, (R)0};
+            if (own < Nw) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) ow[k] = __ldcg(Pk + own + k * Nw) + __ldcg(Dr + own + k * Nw);
+            }
+            bool go = true;
             for (long long mb = m0 + gw * IB_MPW; mb < m1; mb += nw * IB_MPW) {
                 const long long m = mb + sub;
                 const bool act = m < m1;
-                double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+                R v0 = (R)0, v1 = (R)0, v2 = (R)0, ef[3] = {(R)0, (R)0, (R)0};
                 if (act) {
+                    points(m);
+#pragma unroll
+                    for (int k = 0; k < 3; k++) ef[k] = F32IB ? (R)__ldcg(efs + 3 * m + k) : (R)__ldcg(a.eforce + 3 * m + k);
 #pragma unroll
                     for (int j = 0; j < IB_PTS; j++) {
-                        const int p = gl + IB_GL * j;
-                        const long long wc = __ldcg(a.c64 + 64 * m + p);
-                        const double wt = __ldcg(a.w64 + 64 * m + p);
-                        v0 += __ldcg(a.wu + wc) * wt;
-                        v1 += __ldcg(a.wu + wc + Nw) * wt;
-                        v2 += __ldcg(a.wu + wc + 2 * Nw) * wt;
+                        const long long c = rwc[j];
+                        const R wt = rwt[j];
+                        v0 += (__ldcg(Pk + c) + __ldcg(Dr + c)) * wt;
+                        v1 += (__ldcg(Pk + c + Nw) + __ldcg(Dr + c + Nw)) * wt;
+                        v2 += (__ldcg(Pk + c + 2 * Nw) + __ldcg(Dr + c + 2 * Nw)) * wt;
                     }
                 }
 #pragma unroll
                 for (int o = IB_GL / 2; o > 0; o >>= 1) {
-                    v0 += __shfl_xor_sync(0xffffffffu, v0, o);
-                    v1 += __shfl_xor_sync(0xffffffffu, v1, o);
-                    v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+                    v0 += __shfl_xor_sync(FULL, v0, o);
+                    v1 += __shfl_xor_sync(FULL, v1, o);
+                    v2 += __shfl_xor_sync(FULL, v2, o);
                 }
-                if (act && gl == 0) {
-                    const double d0 = a.vel[3 * m] - v0, d1 = a.vel[3 * m + 1] - v1, d2 = a.vel[3 * m + 2] - v2;
-                    const double ar = a.area[m];
-                    const double F0 = d0 * ar, F1 = d1 * ar, F2 = d2 * ar;
-                    a.eforce[3 * m] = __ldcg(a.eforce + 3 * m) + F0;
-                    a.eforce[3 * m + 1] = __ldcg(a.eforce + 3 * m + 1) + F1;
-                    a.eforce[3 * m + 2] = __ldcg(a.eforce + 3 * m + 2) + F2;
-                    a.fet[3 * m] = F0 * a.invh3p; a.fet[3 * m + 1] = F1 * a.invh3p; a.fet[3 * m + 2] = F2 * a.invh3p;
-                    atomicAdd(a.tol_acc + it, (fabs(d0) + fabs(d1)) + fabs(d2));
+                if (!decided) {
+                    decided = true;
+                    if (!test(tprev)) {
+                        go = false;
+                        break;
+                    }
                 }
-            }
-            if (!bar()) return;
-            // the velocity correction of the support (Solidbody.f90:1034-1048)
-            for (long long m = m0 + gw * IB_MPW + sub; m < m1; m += nw * IB_MPW) {
-                const double f0 = __ldcg(a.fet + 3 * m), f1 = __ldcg(a.fet + 3 * m + 1), f2 = __ldcg(a.fet + 3 * m + 2);
+                R tsum = (R)0;
+                if (act) {
+                    const R d0 = ub[0] - v0, d1 = ub[1] - v1, d2 = ub[2] - v2;
+                    const R F0 = d0 * ar, F1 = d1 * ar, F2 = d2 * ar;
+                    const R e0 = ef[0] + F0, e1 = ef[1] + F1, e2 = ef[2] + F2;
+                    tsum = (fabs(d0) + fabs(d1)) + fabs(d2);
+                    if (gl == 0) {
+                        if (F32IB) {
+                            efs[3 * m] = (float)e0; efs[3 * m + 1] = (float)e1; efs[3 * m + 2] = (float)e2;
+                        } else {
+                            a.eforce[3 * m] = (double)e0; a.eforce[3 * m + 1] = (double)e1;
+                            a.eforce[3 * m + 2] = (double)e2;
+                        }
+                    }
+                    // the velocity correction of the support (Solidbody.f90:1034-1048)
+                    const R f0 = F0 * ih3p, f1 = F1 * ih3p, f2 = F2 * ih3p;
 #pragma unroll
-                for (int j = 0; j < IB_PTS; j++) {
-                    const int p = gl + IB_GL * j;
-                    const long long wc = __ldcg(a.c64 + 64 * m + p);
-                    const double wt = __ldcg(a.w64 + 64 * m + p);
-                    atomicAdd(a.wu + wc, -(f0 * wt));
-                    atomicAdd(a.wu + wc + Nw, -(f1 * wt));
-                    atomicAdd(a.wu + wc + 2 * Nw, -(f2 * wt));
+                    for (int j = 0; j < IB_PTS; j++) {
+                        const long long c = rwc[j];
+                        const R wt = rwt[j];
+                        atomicAdd(Dw + c, -(f0 * wt));
+                        atomicAdd(Dw + c + Nw, -(f1 * wt));
+                        atomicAdd(Dw + c + 2 * Nw, -(f2 * wt));
+                    }
+                    if (last) {
+                        const R s0 = e0 * ih3s, s1 = e1 * ih3s, s2 = e2 * ih3s;
+                        if (F32IB) {
+                            if (gl < 3) a.eforce[3 * m + gl] = (double)(gl == 0 ? e0 : (gl == 1 ? e1 : e2));
+#pragma unroll
+                            for (int j = 0; j < IB_PTS; j++) {
+                                const long long c = rwc[j];
+                                const float wt = (float)rwt[j];
+                                atomicAdd(Sp + c, -((float)s0 * wt));
+                                atomicAdd(Sp + c + Nw, -((float)s1 * wt));
+                                atomicAdd(Sp + c + 2 * Nw, -((float)s2 * wt));
+                            }
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < IB_PTS; j++) {
+                                const long long c = rwc[j];
+                                const double wt = (double)rwt[j];
+                                atomicAdd(a.wforce + c, -((double)s0 * wt));
+                                atomicAdd(a.wforce + c + Nw, -((double)s1 * wt));
+                                atomicAdd(a.wforce + c + 2 * Nw, -((double)s2 * wt));
+                            }
+                        }
+                    }
+                }
+                // the residual sum: one term per marker (its group's first
+                // lane), one atomic per warp
+                if (gl != 0) tsum = (R)0;
+#pragma unroll
+                for (int o = IB_GL; o < 32; o <<= 1) tsum += __shfl_xor_sync(FULL, tsum, o);
+                if (lane == 0) {
+                    if (F32IB) atomicAdd((float *)a.tol_acc + it, (float)tsum);
+                    else atomicAdd(a.tol_acc + it, (double)tsum);
+                }
+            }
+            if (go && !decided) go = test(tprev);
+            if (nan) {
+                if (tid == 0) atomicOr(a.status, 4);
+                return;
+            }
+            if (!go) break;
+            // owner pass: P_{s+1} = P_s + D_{s-1}, D_{s-2} cleared
+            for (long long wc = own; wc < Nw; wc += nth) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    Pn[wc + k * Nw] = wc == own ? ow[k] : __ldcg(Pk + wc + k * Nw) + __ldcg(Dr + wc + k * Nw);
+                    Dz[wc + k * Nw] = (R)0;
                 }
             }
             if (!bar()) return;
         }
-        const double tol = __ldcg(a.tol_acc + it);
-        if (!isfinite(tol)) {
-            if (tid == 0) atomicOr(a.status, 4);
-            return;
-        }
-        dmax = tol / a.dsumU;
+        if (stop) break;
         it = it + 1;
     }
-    // FluidVolumeForce_ spreading (Solidbody.f90:968-977) onto vf
-    for (long long m = gw * IB_MPW + sub; m < a.Mtot; m += nw * IB_MPW) {
-        const double f0 = __ldcg(a.eforce + 3 * m) * a.invh3s, f1 = __ldcg(a.eforce + 3 * m + 1) * a.invh3s,
-                     f2 = __ldcg(a.eforce + 3 * m + 2) * a.invh3s;
+    // the residual of the last iteration the cap allowed (a stop by the test
+    // has read it already)
+    if (!stop && it > 0) {
+        if (!test(F32IB ? (R)__ldcg((const float *)a.tol_acc + it - 1) : (R)__ldcg(a.tol_acc + it - 1))) {
+            if (nan) {
+                if (tid == 0) atomicOr(a.status, 4);
+                return;
+            }
+        }
+    }
+    const bool spread_done = a.ntol > 0 && it == a.ntol;
+    // the window velocity after the loop, V_s = P_s + D_{s-1}, into wu (the
+    // window fix-up of the fluid step reads it); with R = FP32 also the
+    // spreading sums onto the window force
+    {
+        const R *Pk = (s & 1) ? P1 : P0;
+        const R *Dr = D + 3 * Nw * ((s + 2) % 3);
+        for (long long wc = own; wc < Nw; wc += nth) {
 #pragma unroll
-        for (int j = 0; j < IB_PTS; j++) {
-            const int p = gl + IB_GL * j;
-            const long long wc = __ldcg(a.c64 + 64 * m + p);
-            const double wt = __ldcg(a.w64 + 64 * m + p);
-            atomicAdd(a.wforce + wc, -(f0 * wt));
-            atomicAdd(a.wforce + wc + Nw, -(f1 * wt));
-            atomicAdd(a.wforce + wc + 2 * Nw, -(f2 * wt));
+            for (int k = 0; k < 3; k++) {
+                a.wu[wc + k * Nw] = (double)(__ldcg(Pk + wc + k * Nw) + __ldcg(Dr + wc + k * Nw));
+                if (F32IB && spread_done) a.wforce[wc + k * Nw] += (double)__ldcg(Sp + wc + k * Nw);
+            }
+        }
+    }
+    // FluidVolumeForce_ spreading (Solidbody.f90:968-977) onto vf, where the
+    // loop stopped before its last iteration
+    if (!spread_done) {
+        for (long long m = gw * IB_MPW + sub; m < a.Mtot; m += nw * IB_MPW) {
+            points(m);
+            double ef[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) ef[k] = F32IB ? (double)__ldcg(efs + 3 * m + k) : __ldcg(a.eforce + 3 * m + k);
+            if (F32IB && gl < 3) a.eforce[3 * m + gl] = gl == 0 ? ef[0] : (gl == 1 ? ef[1] : ef[2]);
+            const double f0 = ef[0] * a.invh3s, f1 = ef[1] * a.invh3s, f2 = ef[2] * a.invh3s;
+#pragma unroll
+            for (int j = 0; j < IB_PTS; j++) {
+                const long long c = rwc[j];
+                const double wt = (double)rwt[j];
+                atomicAdd(a.wforce + c, -(f0 * wt));
+                atomicAdd(a.wforce + c + Nw, -(f1 * wt));
+                atomicAdd(a.wforce + c + 2 * Nw, -(f2 * wt));
+            }
         }
     }
     if (tid == 0) {
         a.status[1] = it;
-        *a.res = dmax;
+        *a.res = F32IB ? (it > 0 ? (double)tol / a.dsumU : dmax) : dmax;
     }
 }
 
 template <int P>
 __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
     const unsigned nblk = gridDim.x;
+    unsigned target = 0;
     ib_body<P>(a, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x,
-               [&]() { return gbar(a.status, nblk); });
+               [&]() { return gbar(a.status, nblk, target); });
 }
 
 // the IB stage of many blocks, one thread-block cluster of IB_CLUSTER CTAs
