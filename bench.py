@@ -664,35 +664,40 @@ def batched_sweep(F, steps, ncase=32, seed=7):
 
 # ------------------------------------------------ learned IB warm start
 
-def warm_start_case(F, dtols=(0.005, 0.002), gen_steps=306, eval_steps=20, epochs=10, grid=(320, 192, 192)):
-    out = {}
-    for d in dtols:
-        out["dtol_%g" % d] = warm_start_run(F, d, gen_steps, eval_steps, epochs, grid)
-    return out
+# stopping rules the warm start is measured at: the headline's (the
+# iteration cap reached first) and two residuals the plain loop reaches
+WARM_RULES = (("headline_ntol5_dtol1e-4", NTOL, DTOL), ("dtol_2e-3", 3000, 2e-3), ("dtol_5e-4", 3000, 5e-4))
 
 
-def warm_start_run(F, dtol, gen_steps, eval_steps, epochs, grid):
-    """Three plates in tandem (spacing 1.5L, phases 0/90/180 deg, 33x33
-    markers, prescribed heave A = 0.3L, f* = 0.2) in a 320x192x192 block at
-    Re = 500 (dh = L/32, FP16 MRT). Training pairs are logged from the plain
-    solver (gen_steps x 3267 pairs, ~1e6), the network is trained on the GPU,
-    then plain and warm-started solves run from the same states to the same
-    residual; the warm result advances the flow."""
+def warm_start_case(F, gen_steps=306, eval_steps=20, epochs=10, grid=(320, 192, 192)):
+    """The learned IB warm start, trained on one tandem case and evaluated on
+    it and on an unseen one. Two plates in tandem (spacing 1.5L, 33x33
+    markers, prescribed heave A = 0.3L, f* = 0.2, phases 0/90 deg) in a
+    320x192x192 block at Re = 500 (dh = L/32, FP16 MRT): training pairs are
+    logged from the plain solver converged to dtol 2e-3 (gen_steps x 2178
+    pairs), the network is trained on the GPU, then plain and warm-started
+    solves run from the same states under each stopping rule, beside the
+    seeded start from the previous step's force (fsi_ib_solve_seeded; the
+    flow advances with the seeded solve under the headline rule). The unseen
+    case has other phases and another amplitude (45/135 deg, A = 0.4L); its
+    flow develops for gen_steps plain steps before the same evaluation."""
     from fsilbm3d_gb300.bodies import RigidPlate
     X, Y, Z = grid
     L = 32
     dh = 1.0 / L
     nu = U / 500.0
-    b = F.Block(X, Y, Z, dh=dh, bndConds=BND, iCollidModel=3, nu=nu, precision=F.PREC_F16, uvwIn=(U, 0, 0))
-    b.initialise(0.0)
-    b.set_boundary_conditions(0.0)
-    plates = [RigidPlate(n_chord=33, n_span=33, chord=1.0, span=1.0, le=(2.0 + 1.5 * k, 0.5 * Y * dh, 0.5 * Z * dh),
-                         heave_ampl=(0.0, 0.3, 0.0), heave_phase_deg=(0.0, 90.0 * k, 0.0), freq=0.2 * U)
-              for k in range(3)]
-    b.ib_set_bodies([p.M for p in plates])
-    ntol = 400
 
-    def markers(t):
+    def case(phases, ampl):
+        b = F.Block(X, Y, Z, dh=dh, bndConds=BND, iCollidModel=3, nu=nu, precision=F.PREC_F16, uvwIn=(U, 0, 0))
+        b.initialise(0.0)
+        b.set_boundary_conditions(0.0)
+        plates = [RigidPlate(n_chord=33, n_span=33, chord=1.0, span=1.0,
+                             le=(2.0 + 1.5 * k, 0.5 * Y * dh, 0.5 * Z * dh), heave_ampl=(0.0, ampl, 0.0),
+                             heave_phase_deg=(0.0, ph, 0.0), freq=0.2 * U) for k, ph in enumerate(phases)]
+        b.ib_set_bodies([p.M for p in plates])
+        return b, plates
+
+    def markers(plates, t):
         xs, vs, ar, ax = [], [], [], []
         for p in plates:
             xyz, vel, area = p.markers(t)
@@ -704,12 +709,50 @@ def warm_start_run(F, dtol, gen_steps, eval_steps, epochs, grid):
             xs.append(xyz); vs.append(vel); ar.append(area); ax.append(a)
         return np.concatenate(xs), np.concatenate(vs), np.concatenate(ar), np.concatenate(ax)
 
+    def evaluate(b, plates, t, m):
+        keys = ("plain", "warm", "seeded")
+        rec = {name: {k: ([], []) for k in keys} for name, _, _ in WARM_RULES}
+        prev = {name: None for name, _, _ in WARM_RULES}
+        for s in range(eval_steps):
+            xyz, vel, area, aux = markers(plates, t)
+            for name, ntol, dtol in WARM_RULES[::-1]:  # the headline rule last: its seeded solve advances the flow
+                e0, i0, r0 = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol)
+                e1, i1, r1 = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol, warm=m)
+                g = prev[name] if prev[name] is not None else np.zeros_like(e0)
+                e2, i2, r2 = b.ib_solve_seeded(xyz, vel, area, g, dt=dh, Uref=U, ntol=ntol, dtol=dtol)
+                prev[name] = e2
+                for k, (i, r) in zip(keys, ((i0, r0), (i1, r1), (i2, r2))):
+                    rec[name][k][0].append(i)
+                    rec[name][k][1].append(r)
+            t += dh
+            b.step(blktime=t)
+        out = {}
+        for name, ntol, dtol in WARM_RULES:
+            o = {"ntol": ntol, "dtol": dtol}
+            ip = np.array(rec[name]["plain"][0], dtype=np.float64)
+            rp = np.array(rec[name]["plain"][1])
+            for k in keys:
+                ik = np.array(rec[name][k][0], dtype=np.float64)
+                rk = np.array(rec[name][k][1])
+                o[k] = {"subiters_per_step": float(ik.mean()), "residual_mean": float(rk.mean())}
+                if k != "plain":
+                    o[k]["subiter_reduction"] = round(float(ip.sum()) / max(1.0, float(ik.sum())), 2)
+                    o[k]["residual_reduction"] = round(float(rp.mean()) / max(1e-30, float(rk.mean())), 2)
+            out[name] = o
+        return out
+
+    # labels at the looser residual: the converged force at 2e-4 (about 1,400
+    # penalty iterations a step) depends on the flow far from the marker and
+    # its fit from the local features stalls (normalised loss 0.85 -> 0.75)
+    gen_ntol, gen_dtol = 3000, 2e-3
+    b, plates = case((0.0, 90.0), 0.3)
     t = 0.0
     Xf, Yf, gen_it = [], [], []
     w0 = time.perf_counter()
     for s in range(gen_steps):
-        xyz, vel, area, aux = markers(t)
-        ef, it, res, ft = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol, features=True)
+        xyz, vel, area, aux = markers(plates, t)
+        ef, it, res, ft = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=gen_ntol, dtol=gen_dtol,
+                                          features=True)
         Xf.append(ft)
         Yf.append(ef / (area[:, None] * U))
         gen_it.append(it)
@@ -722,23 +765,25 @@ def warm_start_run(F, dtol, gen_steps, eval_steps, epochs, grid):
     w0 = time.perf_counter()
     hist = m.train(Xf, Yf, epochs=epochs, batch=512, lr=2e-3, seed=2)
     train_s = time.perf_counter() - w0
-    plain, warm, rp, rw = [], [], [], []
-    for s in range(eval_steps):
-        xyz, vel, area, aux = markers(t)
-        e0, i0, r0 = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol)
-        e1, i1, r1 = b.ib_solve_warm(xyz, vel, area, aux=aux, dt=dh, Uref=U, ntol=ntol, dtol=dtol, warm=m)
-        plain.append(i0); warm.append(i1); rp.append(r0); rw.append(r1)
-        t += dh
-        b.step(blktime=t)
+    seen = evaluate(b, plates, t, m)
     b.close()
-    return {"pairs": int(Xf.shape[0]), "gen_steps": gen_steps, "gen_s": round(gen_s, 2), "epochs": epochs,
-            "train_s": round(train_s, 2), "train_samples_per_s": round(Xf.shape[0] * epochs / train_s, 0),
-            "loss_first_last": [float(hist[0]), float(hist[-1])], "eval_steps": eval_steps, "dtol": dtol,
-            "plain_subiters_per_step": float(np.mean(plain)), "warm_subiters_per_step": float(np.mean(warm)),
-            "subiter_reduction": round(float(np.sum(plain)) / max(1.0, float(np.sum(warm))), 2),
-            "plain_residual_mean": float(np.mean(rp)), "warm_residual_mean": float(np.mean(rw)),
-            "workload": "3 rigid plates in tandem (1.5L, phases 0/90/180), 33x33 markers each, 320x192x192 FP16 "
-                        "MRT, Re=500, heave A=0.3L f*=0.2 (prescribed)"}
+    b, plates = case((45.0, 135.0), 0.4)
+    t = 0.0
+    for s in range(gen_steps):
+        xyz, vel, area, aux = markers(plates, t)
+        b.ib_step(xyz, vel, area, dt=dh, Uref=U, ntol=NTOL, dtol=DTOL, blktime=t + dh)
+        t += dh
+    unseen = evaluate(b, plates, t, m)
+    b.close()
+    return {"pairs": int(Xf.shape[0]), "gen_steps": gen_steps, "gen_s": round(gen_s, 2),
+            "gen_rule": {"ntol": gen_ntol, "dtol": gen_dtol, "subiters_per_step": float(np.mean(gen_it))},
+            "epochs": epochs, "train_s": round(train_s, 2),
+            "train_samples_per_s": round(Xf.shape[0] * epochs / train_s, 0),
+            "loss_first_last": [float(hist[0]), float(hist[-1])], "eval_steps": eval_steps,
+            "trained_case": seen, "unseen_case": unseen,
+            "workload": "2 rigid plates in tandem (1.5L), 33x33 markers each, 320x192x192 FP16 MRT, Re=500, "
+                        "prescribed heave f*=0.2; trained on phases 0/90 A=0.3L, evaluated there and on the "
+                        "unseen phases 45/135 A=0.4L"}
 
 
 # ------------------------------------------------------------------ main

@@ -57,7 +57,7 @@ SYMBOLS = [
     "fsi_ib_get_stencil", "fsi_ib_get_window", "fsi_pair_create", "fsi_pair_destroy", "fsi_pair_extract",
     "fsi_pair_father_to_son", "fsi_pair_son_to_father", "fsi_pair_father_to_son_static",
     "fsi_mlp_create", "fsi_mlp_destroy", "fsi_mlp_set_params", "fsi_mlp_get_params", "fsi_mlp_set_norm",
-    "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_block_timer",
+    "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_ib_solve_seeded", "fsi_block_timer",
     "fsi_block_set_kernel", "fsi_block_ib_step",
     "fsi_batch_create", "fsi_batch_destroy", "fsi_batch_ib_step", "fsi_batch_tune", "fsi_batch_set_threads",
     "fsi_block_set_ib_mode", "fsi_block_pack_flow", "fsi_block_flux", "fsi_block_probes",
@@ -138,6 +138,8 @@ def load_library():
     L.fsi_mlp_train.argtypes = [VP, FP, FP, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, FP]
     L.fsi_ib_solve_warm.argtypes = [VP, DP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int,
                                     C.c_double, VP, FP, DP, IP, DP]
+    L.fsi_ib_solve_seeded.argtypes = [VP, DP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int,
+                                      C.c_double, DP, IP, DP]
     for s in SYMBOLS:
         getattr(L, s).restype = C.c_int
     _lib = L
@@ -419,6 +421,26 @@ class Block:
                                                 _dp(eforce), C.byref(it), C.byref(res)))
         out = (eforce.reshape(-1, 3), it.value, res.value)
         return out + (feat,) if features else out
+
+    def ib_solve_seeded(self, xyz, vel, area, guess, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0,
+                        ntol=3, dtol=1e-5):
+        """ib_solve started from guess (Mtot,3), e.g. the previous step's
+        Lagrangian force (fast forms only); returns (eforce, iterations, residual)"""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        area = np.ascontiguousarray(area, dtype=np.float64).reshape(-1)
+        guess = np.ascontiguousarray(guess, dtype=np.float64).reshape(-1)
+        if area.size != self.Mtot or xyz.size != 3 * self.Mtot or vel.size != 3 * self.Mtot or \
+                guess.size != 3 * self.Mtot:
+            raise ValueError("marker arrays do not match the bodies set with ib_set_bodies")
+        eforce = np.empty(3 * self.Mtot)
+        vf = _vec3(volumeForce)
+        it = C.c_int()
+        res = C.c_double()
+        _check(load_library().fsi_ib_solve_seeded(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(guess), _dp(vf), denIn,
+                                                  self.dh if dt is None else dt, Uref, int(ntol), dtol,
+                                                  _dp(eforce), C.byref(it), C.byref(res)))
+        return eforce.reshape(-1, 3), it.value, res.value
 
     def ib_stencil(self):
         ei = np.empty(12 * self.Mtot, dtype=np.int16)

@@ -1166,6 +1166,7 @@ struct Warm {
     const fsi_mlp *mlp = nullptr;  // network of the warm start, or null
     bool aux = false;              // d_aux holds this call's auxiliary inputs
     float *features = nullptr;     // host (12,Mtot) out, or null
+    bool seed = false;             // d_eforce holds the caller's initial force
     // queue the fluid step right behind the IB stage (fsi_block_ib_step)
     bool step = false;
     const double *step_vf = nullptr;
@@ -1240,6 +1241,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     a.aux = wm.aux ? h->d_aux : nullptr;
     a.feat = wm.features ? h->d_feat : nullptr;
     a.Uref = Uref;
+    a.seed = wm.seed ? 1 : 0;
     // the IB stage beside the bulk step (fsi_block_ib_step forked it onto the
     // second stream); the window fix-up and the face hooks wait for it
     const int mode = wm.forked;
@@ -1435,6 +1437,28 @@ int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const
     wm.mlp = warm;
     wm.aux = aux != nullptr;
     wm.features = features;
+    return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
+}
+
+int fsi_ib_solve_seeded(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double *guess,
+                        const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol, double *eforce,
+                        int *iters, double *residual) {
+    FSI_CALL_RANGE();
+    if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    if (h->prec == FSI_PREC_F64)
+        return fail(FSI_E_ARG, "the seeded start needs a fast form; FSI_PREC_F64 keeps the reference's iteration");
+    h->win_valid = false;
+    if (iters) *iters = 0;
+    if (residual) *residual = 0.0;
+    if (h->nb == 0 || h->Mtot == 0) return FSI_OK;
+    if (!xyz || !vel || !area || !guess || !eforce) return fail(FSI_E_ARG, "null marker array");
+    for (long long k = 0; k < 3LL * h->Mtot; k++)
+        if (!std::isfinite(guess[k])) return fail(FSI_E_NAN, "non-finite initial force");
+    int rc = ib_upload(h, xyz, vel, area);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->d_eforce, guess, sizeof(double) * 3 * h->Mtot, cudaMemcpyHostToDevice, h->st));
+    Warm wm;
+    wm.seed = true;
     return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
 }
 

@@ -79,6 +79,7 @@ struct IbCoop {
     const double *aux;           // (6,Mtot): acceleration, normal; or null
     float *feat;                 // (12,Mtot) features out, or null
     double Uref;
+    int seed;                    // 1: eforce holds the caller's initial force
 };
 
 // ---- output packing (k_f64_exact.cu, reference operation order) ----

@@ -2108,8 +2108,9 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
             ar = (R)a.area[m];
             cm = m;
             if (gl < 3) {
-                a.eforce[3 * m + gl] = 0.0;
-                if (F32IB) efs[3 * m + gl] = 0.0f;
+                // a seeded start keeps the caller's initial force
+                if (!a.seed) a.eforce[3 * m + gl] = 0.0;
+                if (F32IB) efs[3 * m + gl] = a.seed ? (float)a.eforce[3 * m + gl] : 0.0f;
             }
         }
     }
@@ -2135,6 +2136,24 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
     // predicted force becomes the first correction (into D_{-1}, the slot the
     // first stage reads), applied to all bodies at once, and the penalty loop
     // below continues from it
+    // seeded start (no counterpart in the reference): the caller's force
+    // (3,Mtot) in eforce becomes the first correction, as the network's
+    // prediction does below
+    if (a.seed) {
+        for (long long m = gw; m < a.Mtot; m += nw) {
+            const R f0 = (R)(a.eforce[3 * m] * a.invh3p), f1 = (R)(a.eforce[3 * m + 1] * a.invh3p),
+                    f2 = (R)(a.eforce[3 * m + 2] * a.invh3p);
+            R *Dm = D + 6 * Nw;
+            for (int p = lane; p < 64; p += 32) {
+                const long long wc = __ldcg(a.c64 + 64 * m + p);
+                const R wt = __ldcg(W64 + 64 * m + p);
+                atomicAdd(Dm + wc, -(f0 * wt));
+                atomicAdd(Dm + wc + Nw, -(f1 * wt));
+                atomicAdd(Dm + wc + 2 * Nw, -(f2 * wt));
+            }
+        }
+        if (!bar()) return;
+    }
     if (a.mlp || a.feat) {
         const float iU = (float)(1.0 / a.Uref);
         for (long long m = gw; m < a.Mtot; m += nw) {

@@ -281,6 +281,16 @@ int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const
                       int ntol, double dtol, fsi_mlp_t warm, float *features, double *eforce,
                       int *iters, double *residual);
 
+/* Seeded start of the penalty loop (fast forms only). No counterpart in the
+ * reference, whose loop starts every time step from v_Eforce = 0: guess
+ * (3,Mtot) is applied as the first velocity correction and becomes the
+ * starting v_Eforce, e.g. the previous time step's converged force; the
+ * unchanged loop then runs to the same ntol/dtol test. A zero guess gives
+ * the result of fsi_ib_solve. FSI_E_NAN for a non-finite guess. */
+int fsi_ib_solve_seeded(fsi_block_t h, const double *xyz, const double *vel, const double *area,
+                        const double *guess, const double vf[3], double denIn, double dt, double Uref,
+                        int ntol, double dtol, double *eforce, int *iters, double *residual);
+
 /* No counterpart in the reference: many independent blocks stepped together
  * (a parameter sweep of cases on one GPU). The blocks keep their handles and
  * state; while batched they are stepped only through fsi_batch_ib_step (the

@@ -131,8 +131,10 @@ def test_fast_ib_step(gpu_lib, model, prec):
         xyz, vel, area = c.plates[0].markers(t)
         ef1, it1, _ = other.ib_step(xyz, vel, area, Uref=0.05, ntol=4, dtol=1e-12, blktime=t + 1.0)
         c.step()
-        assert np.max(np.abs(ef1 - c.last["ef_g"])) <= 1e-6 * np.max(np.abs(c.last["ef_g"]))
-    # the IB stage's FP64 atomics sum in any order: agreement to rounding
+        # the offset forms run the penalty loop in FP32 with FP32 atomics,
+        # which sum in any order: agreement to FP32 rounding over the loop
+        assert np.max(np.abs(ef1 - c.last["ef_g"])) <= 1e-5 * np.max(np.abs(c.last["ef_g"]))
+    # the IB stage's atomics sum in any order: agreement to rounding
     fa, fb = other.download_f(), c.gb.download_f()
     assert np.max(np.abs(fa - fb)) <= (1e-6 if prec == F.PREC_F32 else 1e-3) * np.max(np.abs(fb))
     ta, tb = other.tau_all(), c.gb.tau_all()
