@@ -58,7 +58,7 @@ SYMBOLS = [
     "fsi_pair_father_to_son", "fsi_pair_son_to_father", "fsi_pair_father_to_son_static",
     "fsi_mlp_create", "fsi_mlp_destroy", "fsi_mlp_set_params", "fsi_mlp_get_params", "fsi_mlp_set_norm",
     "fsi_mlp_forward", "fsi_mlp_grad", "fsi_mlp_train", "fsi_ib_solve_warm", "fsi_ib_solve_seeded", "fsi_block_timer",
-    "fsi_block_set_kernel", "fsi_block_ib_step",
+    "fsi_block_set_kernel", "fsi_block_ib_step", "fsi_block_ib_step_async", "fsi_block_ib_wait",
     "fsi_batch_create", "fsi_batch_destroy", "fsi_batch_ib_step", "fsi_batch_tune", "fsi_batch_set_threads",
     "fsi_block_set_ib_mode", "fsi_block_pack_flow", "fsi_block_flux", "fsi_block_probes",
     "fsi_block_get_omega2", "fsi_block_get_tau_all", "fsi_continue_write", "fsi_continue_read",
@@ -116,6 +116,9 @@ def load_library():
     L.fsi_batch_set_threads.argtypes = [VP, C.c_int]
     L.fsi_block_ib_step.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                     C.c_double, DP, IP, DP]
+    L.fsi_block_ib_step_async.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int,
+                                          C.c_double, C.c_double]
+    L.fsi_block_ib_wait.argtypes = [VP, DP, IP, DP]
     L.fsi_ib_set_bodies.argtypes = [VP, C.c_int, IP, IP]
     L.fsi_ib_solve.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                DP, IP, DP]
@@ -391,6 +394,27 @@ class Block:
                                                 self.dh if dt is None else dt, Uref, int(ntol), dtol, blktime,
                                                 _dp(eforce), C.byref(it), C.byref(res)))
         return eforce.reshape(-1, 3), it.value, res.value
+
+    def ib_step_async(self, xyz, vel, area, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0, ntol=3,
+                      dtol=1e-5, blktime=0.0):
+        """ib_step's first half: queues the IB stage and the fluid step and
+        returns at once; ib_wait() returns (eforce (Mtot,3), iterations, residual)"""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        area = np.ascontiguousarray(area, dtype=np.float64).reshape(-1)
+        if area.size != self.Mtot or xyz.size != 3 * self.Mtot or vel.size != 3 * self.Mtot:
+            raise ValueError("marker arrays do not match the bodies set with ib_set_bodies")
+        vf = _vec3(volumeForce)
+        _check(load_library().fsi_block_ib_step_async(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(vf), denIn,
+                                                      self.dh if dt is None else dt, Uref, int(ntol), dtol,
+                                                      blktime))
+
+    def ib_wait(self):
+        eforce = np.empty(3 * max(self.Mtot, 1))
+        it = C.c_int()
+        res = C.c_double()
+        _check(load_library().fsi_block_ib_wait(self.h, _dp(eforce), C.byref(it), C.byref(res)))
+        return eforce[:3 * self.Mtot].reshape(-1, 3), it.value, res.value
 
     def ib_solve_warm(self, xyz, vel, area, aux=None, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0,
                       ntol=3, dtol=1e-5, warm=None, features=False):

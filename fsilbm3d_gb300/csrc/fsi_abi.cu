@@ -228,6 +228,11 @@ struct fsi_block {
     int *cnt = nullptr, *start = nullptr, *fillc = nullptr, *list = nullptr;
     long long list_cap = 0;
     bool win_valid = false;
+    // fsi_block_ib_step_async: 1 the IB stage and step are queued, 2 (exact
+    // form) the force waits in h_ef with pend_iters / pend_res
+    int ib_pending = 0;
+    int pend_iters = 0;
+    double pend_res = 0.0;
     // captured graph of two steps (A->B, B->A)
     int kernel = FSI_KERNEL_AUTO;  // bulk step kernel of the offset forms
     cudaGraphExec_t gexec = nullptr;
@@ -1055,6 +1060,7 @@ int fsi_block_run(fsi_block_t h, const double vf[3], double blktime0, int nsteps
 int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6]) {
     if (!h || nbodies < 0 || (nbodies > 0 && !M)) return fail(FSI_E_ARG, "invalid argument");
     if (nbodies > 64) return fail(FSI_E_ARG, "at most 64 bodies per block");
+    if (h->ib_pending) return fail(FSI_E_STATE, "an IB step is pending: fsi_block_ib_wait first");
     h->nb = nbodies;
     h->M.assign(M, M + nbodies);
     h->offs.assign(nbodies + 1, 0);
@@ -1167,6 +1173,7 @@ struct Warm {
     bool aux = false;              // d_aux holds this call's auxiliary inputs
     float *features = nullptr;     // host (12,Mtot) out, or null
     bool seed = false;             // d_eforce holds the caller's initial force
+    bool async = false;            // return once queued (fsi_block_ib_wait finishes)
     // queue the fluid step right behind the IB stage (fsi_block_ib_step)
     bool step = false;
     const double *step_vf = nullptr;
@@ -1221,6 +1228,15 @@ void fill_ib(fsi_block *h, const double vf[3], double denIn, double dt, double U
     a.Uref = Uref;
 }
 
+int ib_check_status(fsi_block *h, int *iters, double *residual, bool keep_window);
+
+// the end of a queued IB step: wait for its force and status copies
+int ib_step_finish(fsi_block *h, double *eforce, int *iters, double *residual) {
+    CK(cudaEventSynchronize(h->ev_ib));
+    if (eforce) memcpy(eforce, h->h_ef, sizeof(double) * 3 * h->Mtot);
+    return ib_check_status(h, iters, residual, false);
+}
+
 int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol,
                   const Warm &wm, double *eforce, int *iters, double *residual) {
     if (!h->coop_grid) {
@@ -1271,8 +1287,6 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         int rc = enqueue_step(h, wm.step_vf, wm.step_time, true, h->ev_ib);
         h->win_valid = false;
         if (rc) return rc;
-        CK(cudaEventSynchronize(h->ev_ib));
-        memcpy(eforce, h->h_ef, sizeof(double) * 3 * h->Mtot);
     } else {
     // one warp per marker in the penalty loop and a thread per window cell in
     // the macro phase are all the parallelism there is; a smaller grid makes
@@ -1297,8 +1311,6 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         int rc = enqueue_step(h, wm.step_vf, wm.step_time, true);
         h->win_valid = false;
         if (rc) return rc;
-        CK(cudaEventSynchronize(h->ev_ib));
-        memcpy(eforce, h->h_ef, sizeof(double) * 3 * h->Mtot);
     } else {
         CK(cudaMemcpyAsync(eforce, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
         if (wm.features)
@@ -1307,6 +1319,19 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         CK(cudaStreamSynchronize(h->st));
     }
     }
+    if (wm.step) {
+        if (wm.async) {
+            h->ib_pending = 1;
+            return FSI_OK;
+        }
+        return ib_step_finish(h, eforce, iters, residual);
+    }
+    return ib_check_status(h, iters, residual, true);
+}
+
+// the status of the last IB stage (its copy in h_stat): error codes, the
+// iteration count and the residual
+int ib_check_status(fsi_block *h, int *iters, double *residual, bool keep_window) {
     if (h->h_stat[4]) return fail(FSI_E_TIMEOUT, "step kernel: a bounded wait ran out");
     const int st = h->h_stat[0];
     if (st & 1) return fail(FSI_E_RANGE, "index out of block bounds in IB stencil");
@@ -1316,7 +1341,7 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     const int it = h->h_stat[1];
     if (iters) *iters = it;
     if (residual) *residual = *(const double *)(h->h_stat + 8);
-    h->win_valid = !wm.step;
+    h->win_valid = keep_window;
     return FSI_OK;
 }
 
@@ -1343,6 +1368,7 @@ int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const doub
                  double *residual) {
     FSI_CALL_RANGE();
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    if (h->ib_pending) return fail(FSI_E_STATE, "an IB step is pending: fsi_block_ib_wait first");
     h->win_valid = false;
     if (iters) *iters = 0;
     if (residual) *residual = 0.0;
@@ -1406,6 +1432,7 @@ int fsi_ib_solve_warm(fsi_block_t h, const double *xyz, const double *vel, const
                       float *features, double *eforce, int *iters, double *residual) {
     FSI_CALL_RANGE();
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    if (h->ib_pending) return fail(FSI_E_STATE, "an IB step is pending: fsi_block_ib_wait first");
     if (h->prec == FSI_PREC_F64)
         return fail(FSI_E_ARG, "the warm start needs a fast form; FSI_PREC_F64 keeps the reference's iteration");
     if (warm && !warm->norm_set) return fail(FSI_E_STATE, "network statistics not set (fsi_mlp_set_norm)");
@@ -1445,6 +1472,7 @@ int fsi_ib_solve_seeded(fsi_block_t h, const double *xyz, const double *vel, con
                         int *iters, double *residual) {
     FSI_CALL_RANGE();
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    if (h->ib_pending) return fail(FSI_E_STATE, "an IB step is pending: fsi_block_ib_wait first");
     if (h->prec == FSI_PREC_F64)
         return fail(FSI_E_ARG, "the seeded start needs a fast form; FSI_PREC_F64 keeps the reference's iteration");
     h->win_valid = false;
@@ -1462,22 +1490,49 @@ int fsi_ib_solve_seeded(fsi_block_t h, const double *xyz, const double *vel, con
     return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
 }
 
-int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
-                      double denIn, double dt, double Uref, int ntol, double dtol, double blktime, double *eforce,
-                      int *iters, double *residual) {
-    FSI_CALL_RANGE();
+}  // extern "C"
+
+namespace {
+
+// fsi_block_ib_step and its queued form
+int ib_step_impl(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
+                 double denIn, double dt, double Uref, int ntol, double dtol, double blktime, double *eforce,
+                 int *iters, double *residual, bool async) {
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
+    if (h->ib_pending) return fail(FSI_E_STATE, "an IB step is pending: fsi_block_ib_wait first");
     if (h->prec == FSI_PREC_F64 || h->nb == 0 || h->Mtot == 0) {
-        int rc = fsi_ib_solve(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, eforce, iters, residual);
+        if (!async) {
+            int rc = fsi_ib_solve(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, eforce, iters, residual);
+            if (rc) return rc;
+            return fsi_block_step(h, vf, blktime);
+        }
+        // the exact form runs the two calls one after the other; the force
+        // waits in the staging buffer for fsi_block_ib_wait
+        if (h->h_ef_cap < h->Mtot) {
+            if (h->h_ef) cudaFreeHost(h->h_ef);
+            h->h_ef = nullptr;
+            h->h_ef_cap = 0;
+            CK(cudaHostAlloc((void **)&h->h_ef, sizeof(double) * 3 * h->Mtot, cudaHostAllocDefault));
+            h->h_ef_cap = h->Mtot;
+        }
+        int it = 0;
+        double res = 0.0;
+        int rc = fsi_ib_solve(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, h->h_ef, &it, &res);
         if (rc) return rc;
-        return fsi_block_step(h, vf, blktime);
+        rc = fsi_block_step(h, vf, blktime);
+        if (rc) return rc;
+        h->pend_iters = it;
+        h->pend_res = res;
+        h->ib_pending = 2;
+        return FSI_OK;
     }
     h->win_valid = false;
     if (iters) *iters = 0;
     if (residual) *residual = 0.0;
-    if (!xyz || !vel || !area || !eforce) return fail(FSI_E_ARG, "null marker array");
+    if (!xyz || !vel || !area || (!eforce && !async)) return fail(FSI_E_ARG, "null marker array");
     Warm wm;
     wm.step = true;
+    wm.async = async;
     wm.step_vf = vf;
     wm.step_time = blktime;
     const int mode = resolve_ib_mode(h, vf, blktime);
@@ -1493,6 +1548,40 @@ int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const
     int rc = ib_upload(h, xyz, vel, area, ust);
     if (rc) return rc;
     return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, wm, eforce, iters, residual);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const double *area, const double vf[3],
+                      double denIn, double dt, double Uref, int ntol, double dtol, double blktime, double *eforce,
+                      int *iters, double *residual) {
+    FSI_CALL_RANGE();
+    return ib_step_impl(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, blktime, eforce, iters, residual, false);
+}
+
+int fsi_block_ib_step_async(fsi_block_t h, const double *xyz, const double *vel, const double *area,
+                            const double vf[3], double denIn, double dt, double Uref, int ntol, double dtol,
+                            double blktime) {
+    FSI_CALL_RANGE();
+    return ib_step_impl(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, blktime, nullptr, nullptr, nullptr,
+                        true);
+}
+
+int fsi_block_ib_wait(fsi_block_t h, double *eforce, int *iters, double *residual) {
+    FSI_CALL_RANGE();
+    if (!h) return fail(FSI_E_ARG, "null handle");
+    const int mode = h->ib_pending;
+    if (!mode) return fail(FSI_E_STATE, "no IB step pending (fsi_block_ib_step_async)");
+    h->ib_pending = 0;
+    if (mode == 2) {
+        if (eforce && h->Mtot) memcpy(eforce, h->h_ef, sizeof(double) * 3 * h->Mtot);
+        if (iters) *iters = h->pend_iters;
+        if (residual) *residual = h->pend_res;
+        return FSI_OK;
+    }
+    return ib_step_finish(h, eforce, iters, residual);
 }
 
 int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew) {

@@ -222,6 +222,20 @@ int fsi_block_ib_step(fsi_block_t h, const double *xyz, const double *vel, const
                       const double vf[3], double denIn, double dt, double Uref, int ntol,
                       double dtol, double blktime, double *eforce, int *iters, double *residual);
 
+/* fsi_block_ib_step in two calls (no counterpart in the reference): the
+ * first queues the IB stage and the fluid step and returns at once (the
+ * marker arrays may be reused on return); the second waits for the IB stage
+ * and returns its force, iteration count and residual (errors of the IB
+ * stage come back here). A host with prescribed body motion can prepare the
+ * next step's markers in between. While a step is pending, the IB calls of
+ * the block (fsi_ib_solve*, fsi_block_ib_step*, fsi_ib_set_bodies) return
+ * FSI_E_STATE; the other calls queue behind it on the block's stream.
+ * fsi_block_ib_wait without a pending step returns FSI_E_STATE. */
+int fsi_block_ib_step_async(fsi_block_t h, const double *xyz, const double *vel, const double *area,
+                            const double vf[3], double denIn, double dt, double Uref, int ntol,
+                            double dtol, double blktime);
+int fsi_block_ib_wait(fsi_block_t h, double *eforce, int *iters, double *residual);
+
 /* the stencil of the last fsi_ib_solve: v_Ei (12,Mtot) 1-based, v_Ew (12,Mtot) */
 int fsi_ib_get_stencil(fsi_block_t h, int16_t *ei, float *ew);
 
