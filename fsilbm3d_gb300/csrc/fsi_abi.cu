@@ -158,6 +158,8 @@ void mrt_moment_form(MrtMats &m) {
 
 // the device status words (8 ints) followed by the IB residual (a double)
 constexpr size_t STAT_BYTES = sizeof(int) * 8 + sizeof(double);
+// streams the per-case form of a batch's bulk step fans out over
+constexpr int BATCH_FAN = 16;
 
 }  // namespace
 
@@ -2015,7 +2017,18 @@ struct fsi_batch {
     int prec = 0, model = 1;
     cudaStream_t st = nullptr, st2 = nullptr;  // st2: the IB stage, beside the bulk step
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evf = nullptr, evj = nullptr;
-    int threads = BATCH_THREADS[0];  // bulk kernel CTA size (the autotuner's choice)
+    int threads = BATCH_THREADS[0];  // bulk kernel CTA size (the autotuner's choice; 0: per-case form)
+    // the per-case form of the bulk step (threads == 0): each block's own
+    // single-block bulk kernel, its arguments in the launch, fanned out over
+    // streams inside the captured graph; those arguments are baked in, so
+    // there is one graph per buffer parity (gexec: the buffers as captured,
+    // gexec_odd: swapped) and a recapture when a block's bulk arguments change
+    cudaStream_t fan[BATCH_FAN] = {};
+    cudaEvent_t evfan[BATCH_FAN] = {};
+    cudaEvent_t evfork = nullptr;
+    cudaGraphExec_t gexec_odd = nullptr;
+    int parity = 0;
+    std::vector<StepArgs> cap_args;  // the blocks' bulk arguments at capture
     std::vector<int> moff;           // first packed marker of each block (n+1)
     int Mall = 0;
     int ntol_cap = 0;
@@ -2050,6 +2063,12 @@ int thread_slot(int T) {
 void free_batch(fsi_batch *b) {
     if (!b) return;
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->gexec_odd) cudaGraphExecDestroy(b->gexec_odd);
+    for (int k = 0; k < BATCH_FAN; k++) {
+        if (b->evfan[k]) cudaEventDestroy(b->evfan[k]);
+        if (b->fan[k]) cudaStreamDestroy(b->fan[k]);
+    }
+    if (b->evfork) cudaEventDestroy(b->evfork);
     void *dp[] = {b->d_in, b->d_ef, b->d_stat, b->d_res, b->d_tol, b->d_gcase[0], b->d_gcase[1], b->d_gcase[2]};
     for (void *p : dp)
         if (p) cudaFree(p);
@@ -2090,11 +2109,41 @@ void batch_fill_steps(fsi_batch *b, const double *vf, const double *blktime, boo
     }
 }
 
-int batch_capture(fsi_batch *b, int G, long long wmax, bool forced) {
-    if (b->gexec) {
-        cudaGraphExecDestroy(b->gexec);
-        b->gexec = nullptr;
+// the bulk arguments of block c for the per-case form: the bulk kernel
+// alone (the window fix-up runs batched), buffers swapped for odd parity
+StepArgs percase_args(const fsi_batch *b, int c, int parity) {
+    StepArgs a = ((const BatchCase *)b->h_in)[c].a;
+    a.win = Win{};
+    a.win.x1 = a.win.x0 - 1;
+    a.win.n = 0;
+    a.join = nullptr;
+    if (parity) {
+        const void *t = a.src;
+        a.src = a.dst;
+        a.dst = const_cast<void *>(t);
     }
+    return a;
+}
+
+// the per-case bulk kernels, fanned out from st over the fan streams and
+// joined back into st (inside a capture, or for the autotuner)
+cudaError_t percase_launch(fsi_batch *b, int parity) {
+    const int nf = std::min(b->n, BATCH_FAN);
+    cudaError_t e = cudaEventRecord(b->evfork, b->st);
+    for (int k = 0; k < nf && e == cudaSuccess; k++) e = cudaStreamWaitEvent(b->fan[k], b->evfork, 0);
+    for (int c = 0; c < b->n && e == cudaSuccess; c++) {
+        const fsi_block *h = b->blk[c];
+        e = launch_step_fast(percase_args(b, c, parity), &h->mm, b->prec, b->model, b->fan[c % nf]);
+    }
+    for (int k = 0; k < nf && e == cudaSuccess; k++) {
+        e = cudaEventRecord(b->evfan[k], b->fan[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->evfan[k], 0);
+    }
+    return e;
+}
+
+// one step's graph; parity < 0: the table-driven bulk kernel
+int batch_capture_one(fsi_batch *b, int G, long long wmax, bool forced, int parity, cudaGraphExec_t *out) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemcpyAsync(b->d_in, b->h_in, b->in_bytes, cudaMemcpyHostToDevice, b->st);
@@ -2105,9 +2154,13 @@ int batch_capture(fsi_batch *b, int G, long long wmax, bool forced) {
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st2, b->evf, 0);
     if (e == cudaSuccess) e = launch_batch_ib((const IbCoop *)(b->d_in + b->off_ib), b->n, 512, b->prec, b->st2);
     if (e == cudaSuccess) e = cudaEventRecord(b->evj, b->st2);
-    if (e == cudaSuccess)
-        e = launch_batch_step((const BatchCase *)b->d_in, b->d_gcase[thread_slot(b->threads)], b->n, G, b->threads, 0,
-                              b->prec, b->model, forced, b->st);
+    if (e == cudaSuccess) {
+        if (parity < 0)
+            e = launch_batch_step((const BatchCase *)b->d_in, b->d_gcase[thread_slot(b->threads)], b->n, G, b->threads,
+                                  0, b->prec, b->model, forced, b->st);
+        else
+            e = percase_launch(b, parity);
+    }
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->evj, 0);
     if (e == cudaSuccess) e = launch_batch_winfix((const BatchCase *)b->d_in, b->n, wmax, b->prec, b->model, b->st);
     for (int k = 0; k < 6 && e == cudaSuccess; k++)
@@ -2122,14 +2175,58 @@ int batch_capture(fsi_batch *b, int G, long long wmax, bool forced) {
     cudaError_t ce = cudaStreamEndCapture(b->st, &g);
     if (e != cudaSuccess) return fail(FSI_E_CUDA, "batch capture: %s", cudaGetErrorString(e));
     if (ce != cudaSuccess) return fail(FSI_E_CUDA, "batch capture: %s", cudaGetErrorString(ce));
-    e = cudaGraphInstantiate(&b->gexec, g, 0);
+    e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(FSI_E_CUDA, "batch graph: %s", cudaGetErrorString(e));
+    return FSI_OK;
+}
+
+int batch_capture(fsi_batch *b, int G, long long wmax, bool forced) {
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    if (b->gexec_odd) {
+        cudaGraphExecDestroy(b->gexec_odd);
+        b->gexec_odd = nullptr;
+    }
+    if (b->threads == 0) {
+        int rc = batch_capture_one(b, G, wmax, forced, 0, &b->gexec);
+        if (!rc) rc = batch_capture_one(b, G, wmax, forced, 1, &b->gexec_odd);
+        if (rc) return rc;
+        b->cap_args.resize(b->n);
+        for (int c = 0; c < b->n; c++) b->cap_args[c] = ((const BatchCase *)b->h_in)[c].a;
+        b->parity = 0;
+    } else {
+        int rc = batch_capture_one(b, G, wmax, forced, -1, &b->gexec);
+        if (rc) return rc;
+    }
     b->g_threads = b->threads;
     b->g_wmax = wmax;
     b->g_forced = forced;
     b->g_ntol = b->ntol_cap;
     return FSI_OK;
+}
+
+// the per-case graphs still hold this step's bulk arguments: the buffers of
+// the current parity, the same volume force and z-face populations
+bool percase_current(const fsi_batch *b) {
+    if ((int)b->cap_args.size() != b->n) return false;
+    const BatchCase *cs = (const BatchCase *)b->h_in;
+    for (int c = 0; c < b->n; c++) {
+        const StepArgs &x = cs[c].a, &y = b->cap_args[c];
+        const bool swapped = b->parity != 0;
+        if (x.src != (swapped ? (const void *)y.dst : y.src) || x.dst != (swapped ? const_cast<void *>(y.src) : y.dst))
+            return false;
+        for (int k = 0; k < 3; k++)
+            if (x.vf[k] != y.vf[k]) return false;
+        for (int k = 0; k < 2; k++) {
+            if (x.zeq[k] != y.zeq[k]) return false;
+            for (int q = 0; q < 19; q++)
+                if (x.zg[k][q] != y.zg[k][q]) return false;
+        }
+    }
+    return true;
 }
 
 }  // namespace
@@ -2204,6 +2301,11 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
     }
     if ((e = cudaEventCreateWithFlags(&b->evf, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreateWithFlags(&b->evj, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreateWithFlags(&b->evfork, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+    for (int k = 0; k < std::min(n, BATCH_FAN); k++) {
+        if ((e = cudaStreamCreateWithFlags(&b->fan[k], cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+        if ((e = cudaEventCreateWithFlags(&b->evfan[k], cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+    }
     if ((e = cudaMalloc((void **)&b->d_in, b->in_bytes)) != cudaSuccess) return bail(e);
     if ((e = cudaHostAlloc((void **)&b->h_in, b->in_bytes, cudaHostAllocDefault)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc((void **)&b->d_ef, sizeof(double) * 3 * Mt)) != cudaSuccess) return bail(e);
@@ -2309,12 +2411,14 @@ int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const
         memcpy(mk + 3LL * Mt, vel, sizeof(double) * 3 * b->Mall);
         memcpy(mk + 6LL * Mt, area, sizeof(double) * b->Mall);
     }
-    if (!b->gexec || b->g_threads != b->threads || b->g_wmax < wmax || b->g_forced != forced || b->g_ntol != b->ntol_cap) {
+    if (!b->gexec || b->g_threads != b->threads || b->g_wmax < wmax || b->g_forced != forced ||
+        b->g_ntol != b->ntol_cap || (b->threads == 0 && !percase_current(b))) {
         int rc = batch_capture(b, G, wmax, forced);
         if (rc) return rc;
     }
-    CK(cudaGraphLaunch(b->gexec, b->st));
+    CK(cudaGraphLaunch(b->threads == 0 && b->parity ? b->gexec_odd : b->gexec, b->st));
     CK(cudaStreamSynchronize(b->st));
+    b->parity ^= 1;
     for (int c = 0; c < n; c++) {
         fsi_block *h = b->blk[c];
         std::swap(h->fa, h->fb);
@@ -2366,6 +2470,33 @@ int fsi_batch_tune(fsi_batch_t b, int reps, int *threads, float *ms_per_step) {
             best_t = T;
         }
     }
+    // the per-case form: a graph of the blocks' own bulk kernels, fanned out
+    {
+        cudaGraph_t g;
+        cudaGraphExec_t ge = nullptr;
+        CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = percase_launch(b, 0);
+        cudaError_t ce = cudaStreamEndCapture(b->st, &g);
+        if (e != cudaSuccess || ce != cudaSuccess)
+            return fail(FSI_E_CUDA, "batch tune capture: %s", cudaGetErrorString(e != cudaSuccess ? e : ce));
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(FSI_E_CUDA, "batch tune graph: %s", cudaGetErrorString(e));
+        for (int w = 0; w < 2 && e == cudaSuccess; w++) e = cudaGraphLaunch(ge, b->st);
+        if (e == cudaSuccess) e = cudaEventRecord(b->ev0, b->st);
+        for (int r = 0; r < reps && e == cudaSuccess; r++) e = cudaGraphLaunch(ge, b->st);
+        if (e == cudaSuccess) e = cudaEventRecord(b->ev1, b->st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b->ev1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        cudaGraphExecDestroy(ge);
+        if (e != cudaSuccess) return fail(FSI_E_CUDA, "batch tune: %s", cudaGetErrorString(e));
+        ms /= (float)reps;
+        if (ms < best) {
+            best = ms;
+            best_t = 0;
+        }
+    }
     b->threads = best_t;
     if (threads) *threads = best_t;
     if (ms_per_step) *ms_per_step = best;
@@ -2374,6 +2505,10 @@ int fsi_batch_tune(fsi_batch_t b, int reps, int *threads, float *ms_per_step) {
 
 int fsi_batch_set_threads(fsi_batch_t b, int threads) {
     if (!b) return fail(FSI_E_ARG, "null handle");
+    if (threads == 0) {
+        b->threads = 0;
+        return FSI_OK;
+    }
     for (int T : BATCH_THREADS)
         if (T == threads) {
             b->threads = threads;

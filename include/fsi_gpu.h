@@ -327,11 +327,15 @@ int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const
                       const double *vf, const double *denIn, const double *dt, const double *Uref,
                       int ntol, double dtol, const double *blktime, double *eforce, int *iters,
                       double *residual);
-/* Autotuner: times the bulk step of all blocks with each CTA size the kernel
- * is built for (reps launches each, reading the current state and writing the
- * spare buffer, so the state does not change) and keeps the fastest. */
+/* Autotuner: times the bulk step of all blocks in each form it can take
+ * (reps launches each, reading the current state and writing the spare
+ * buffer, so the state does not change) and keeps the fastest: the one
+ * table-driven kernel over every block's row groups at each CTA size it is
+ * built for (*threads = 128, 256, 512), or every block's own single-block
+ * bulk kernel, launched side by side inside the step's graph (*threads = 0). */
 int fsi_batch_tune(fsi_batch_t b, int reps, int *threads, float *ms_per_step);
-/* the bulk kernel's CTA size by hand (128, 256 or 512) */
+/* the bulk step's form by hand: 128, 256 or 512 (the table-driven kernel's
+ * CTA size) or 0 (each block's own kernel) */
 int fsi_batch_set_threads(fsi_batch_t b, int threads);
 
 /* Block refinement, LBMBlockComm.f90:340-979. A pair links a father and a

@@ -48,7 +48,8 @@ def test_batch_fluid_equals_single(gpu_lib, prec, model):
             assert np.array_equal(a.tau_all().view(np.uint64), b.tau_all().view(np.uint64))
 
 
-@pytest.mark.parametrize("threads", [128, 256, 512])
+# 0: the per-case form (each block's own bulk kernel inside the step's graph)
+@pytest.mark.parametrize("threads", [128, 256, 512, 0])
 def test_batch_cta_sizes_agree(gpu_lib, threads):
     solo, _ = _blocks(F.PREC_F16, 3)
     grouped, _ = _blocks(F.PREC_F16, 3)
@@ -98,12 +99,29 @@ def test_batch_tune_keeps_state(gpu_lib):
     batch = F.Batch(grouped)
     before = [b.download_f() for b in grouped]
     threads, ms = batch.tune(reps=3)
-    assert threads in (128, 256, 512) and ms > 0
+    assert threads in (0, 128, 256, 512) and ms > 0
     for b, f in zip(grouped, before):
         assert np.array_equal(b.download_f().view(np.uint64), f.view(np.uint64))
     mk = [p.markers(0.0) if p is not None else None for p in plates]
     efs, its, res = batch.ib_step(mk, Uref=[0.04] * 4, ntol=3, dtol=0.0, blktime=[1.0] * 4)
     assert all(np.all(np.isfinite(e)) for e in efs)
+
+
+def test_batch_per_case_form_follows_changed_arguments(gpu_lib):
+    # the per-case graphs hold each block's bulk arguments: two buffer
+    # parities, and a new capture when a block's volume force changes
+    solo, _ = _blocks(F.PREC_F16, 3)
+    grouped, _ = _blocks(F.PREC_F16, 3)
+    batch = F.Batch(grouped)
+    batch.set_threads(0)
+    n = len(grouped)
+    for s in range(7):
+        vf = [(0.0, 0.0, 0.0) if s < 3 else (1e-6 * (c + 1), 0.0, -2e-7) for c in range(n)]
+        for b, v in zip(solo, vf):
+            b.step(volumeForce=v, blktime=s + 1.0)
+        batch.ib_step([None] * n, vf=np.array(vf), blktime=[s + 1.0] * n)
+    for a, b in zip(solo, grouped):
+        assert np.array_equal(a.download_f().view(np.uint64), b.download_f().view(np.uint64))
 
 
 def test_batch_refusals(gpu_lib):
