@@ -63,7 +63,7 @@ SYMBOLS = [
     "fsi_block_set_ib_mode", "fsi_block_pack_flow", "fsi_block_flux", "fsi_block_probes",
     "fsi_block_get_omega2", "fsi_block_get_tau_all", "fsi_continue_write", "fsi_continue_read",
 ]
-IB_AUTO, IB_GRID, IB_CLUSTER, IB_OVERLAP = 0, 1, 2, 3
+IB_AUTO, IB_GRID, IB_CLUSTER, IB_OVERLAP, IB_GATHER = 0, 1, 2, 3, 4
 KERNEL_AUTO, KERNEL_PAIRED, KERNEL_PIPELINED = 0, 1, 2
 # the warm-start perceptron (FSI_MLP_* in the header)
 MLP_IN, MLP_OUT, MLP_NPARAM, MLP_NNORM = 12, 3, 5187, 30

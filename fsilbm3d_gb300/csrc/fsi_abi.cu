@@ -217,6 +217,10 @@ struct fsi_block {
     // kernel's error word (bit 1: a bounded wait ran out)
     int *d_status = nullptr;
     int *h_stat = nullptr;  // pinned copy of d_status (STAT_BYTES: 8 status words, the IB residual)
+    // the last cooperative IB stage ended cleanly and h_stat holds its status
+    // (error word 0, the barrier counter in h_stat[2]): the next one starts
+    // from that counter without clearing the status words
+    bool ib_clean = false;
     double *d_res = nullptr, *d_tolacc = nullptr;
     int tolacc_cap = 0;
     // warm start: per-marker auxiliary inputs and logged features
@@ -988,7 +992,7 @@ int fsi_block_set_kernel(fsi_block_t h, int kernel) {
 
 int fsi_block_set_ib_mode(fsi_block_t h, int mode) {
     if (!h) return fail(FSI_E_ARG, "null handle");
-    if (mode < FSI_IB_AUTO || mode > FSI_IB_OVERLAP) return fail(FSI_E_ARG, "unknown IB mode %d", mode);
+    if (mode < FSI_IB_AUTO || mode > FSI_IB_GATHER) return fail(FSI_E_ARG, "unknown IB mode %d", mode);
     h->ib_mode = mode;
     return FSI_OK;
 }
@@ -1250,10 +1254,14 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         h->tolacc_cap = std::max(ntol, 64);
         CK(cudaMalloc((void **)&h->d_tolacc, sizeof(double) * h->tolacc_cap));
     }
-    // a forked IB stage zeroes its status on the second stream, ahead of it
-    CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 4, wm.forked ? h->st2 : h->st));
+    // after a stage that did not end cleanly the status words are cleared (a
+    // forked stage on the second stream, ahead of it)
+    const unsigned bar_base = h->ib_clean ? (unsigned)h->h_stat[2] : 0u;
+    if (!h->ib_clean) CK(cudaMemsetAsync(h->d_status, 0, sizeof(int) * 4, wm.forked ? h->st2 : h->st));
+    h->ib_clean = false;
     IbCoop a;
     fill_ib(h, vf, denIn, dt, Uref, ntol, dtol, a);
+    a.bar_base = bar_base;
     a.mlp = wm.mlp ? wm.mlp->P : nullptr;
     a.mlp_nrm = wm.mlp ? wm.mlp->nrm : nullptr;
     a.aux = wm.aux ? h->d_aux : nullptr;
@@ -1344,6 +1352,7 @@ int ib_check_status(fsi_block *h, int *iters, double *residual, bool keep_window
     if (iters) *iters = it;
     if (residual) *residual = *(const double *)(h->h_stat + 8);
     h->win_valid = keep_window;
+    h->ib_clean = st == 0;
     return FSI_OK;
 }
 
@@ -1379,7 +1388,9 @@ int fsi_ib_solve(fsi_block_t h, const double *xyz, const double *vel, const doub
     int rc = ib_upload(h, xyz, vel, area);
     if (rc) return rc;
     const int Mt = h->Mtot;
-    if (h->prec != FSI_PREC_F64) return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, Warm{}, eforce, iters, residual);
+    // the fast forms' cooperative stage, unless the gather kernels are asked for
+    if (h->prec != FSI_PREC_F64 && h->ib_mode != FSI_IB_GATHER)
+        return ib_solve_coop(h, vf, denIn, dt, Uref, ntol, dtol, Warm{}, eforce, iters, residual);
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
     CK(cudaMemsetAsync(h->d_eforce, 0, sizeof(double) * 3 * Mt, h->st));
     // calculate_macro_quantities_ + ResetVolumeForce_ restricted to the window
@@ -1502,7 +1513,7 @@ int ib_step_impl(fsi_block_t h, const double *xyz, const double *vel, const doub
                  int *iters, double *residual, bool async) {
     if (!h || !vf) return fail(FSI_E_ARG, "null argument");
     if (h->ib_pending) return fail(FSI_E_STATE, "an IB step is pending: fsi_block_ib_wait first");
-    if (h->prec == FSI_PREC_F64 || h->nb == 0 || h->Mtot == 0) {
+    if (h->prec == FSI_PREC_F64 || h->ib_mode == FSI_IB_GATHER || h->nb == 0 || h->Mtot == 0) {
         if (!async) {
             int rc = fsi_ib_solve(h, xyz, vel, area, vf, denIn, dt, Uref, ntol, dtol, eforce, iters, residual);
             if (rc) return rc;

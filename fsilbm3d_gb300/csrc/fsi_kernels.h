@@ -80,6 +80,7 @@ struct IbCoop {
     float *feat;                 // (12,Mtot) features out, or null
     double Uref;
     int seed;                    // 1: eforce holds the caller's initial force
+    unsigned bar_base;           // the grid barrier's arrival counter (status[2]) at launch
 };
 
 // ---- output packing (k_f64_exact.cu, reference operation order) ----

@@ -1960,9 +1960,10 @@ __global__ void k_win_macro_fast(const void *__restrict__ fs, double *wden, doub
 // (__ldcg): L1 is not coherent across SMs.
 // ---------------------------------------------------------------------------
 
-// grid barrier with an iteration limit. The arrival counter (status[2],
-// zeroed by the host before each launch) only grows: the k-th barrier of a
-// launch waits for k * nblk arrivals, one release-add and acquire polls of a
+// grid barrier with an iteration limit. The arrival counter (status[2])
+// only grows, from launch to launch: the k-th barrier of a launch waits for
+// base + k * nblk arrivals (base: the counter at launch, which the host keeps
+// from the previous launch's status), one release-add and acquire polls of a
 // single word. On timeout the status gets bit 8 and the CTA returns false;
 // the other CTAs then time out at their next barrier.
 __device__ __forceinline__ bool gbar(int *status, unsigned nblk, unsigned &target) {
@@ -2423,7 +2424,7 @@ __device__ __forceinline__ void ib_body(const IbCoop &a, long long tid, long lon
 template <int P>
 __global__ void __launch_bounds__(256) k_ib_coop(IbCoop a) {
     const unsigned nblk = gridDim.x;
-    unsigned target = 0;
+    unsigned target = a.bar_base;
     ib_body<P>(a, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x,
                [&]() { return gbar(a.status, nblk, target); });
 }

@@ -184,11 +184,16 @@ int fsi_block_set_kernel(fsi_block_t h, int kernel);
  * IB-window fix-up and face hooks after both. FSI_IB_CLUSTER: as OVERLAP with
  * the IB stage on one thread-block cluster. FSI_IB_AUTO: OVERLAP for the
  * offset forms when the paired kernels run the step, else GRID. Same
- * stopping rule and results to rounding. */
+ * stopping rule and results to rounding (their sums are atomics, in any
+ * order). FSI_IB_GATHER: the kernels FSI_PREC_F64 uses (each window cell
+ * gathers its stencil entries in the reference's serial order, FP64; the
+ * residual test on the host between iterations), on the fast forms' window
+ * velocity: the same force from run to run, for comparisons. */
 #define FSI_IB_AUTO    0
 #define FSI_IB_GRID    1
 #define FSI_IB_CLUSTER 2
 #define FSI_IB_OVERLAP 3
+#define FSI_IB_GATHER  4
 int fsi_block_set_ib_mode(fsi_block_t h, int mode);
 
 /* No counterpart in the reference: device time of the work a host loop

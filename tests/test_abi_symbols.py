@@ -76,7 +76,8 @@ def test_binding_constants_match_header():
         "FSI_PREC_F64_DW": A.PREC_F64_DW,
         "FSI_KERNEL_AUTO": A.KERNEL_AUTO, "FSI_KERNEL_PAIRED": A.KERNEL_PAIRED,
         "FSI_KERNEL_PIPELINED": A.KERNEL_PIPELINED, "FSI_IB_AUTO": A.IB_AUTO, "FSI_IB_GRID": A.IB_GRID,
-        "FSI_IB_CLUSTER": A.IB_CLUSTER, "FSI_IB_OVERLAP": A.IB_OVERLAP, "FSI_MLP_IN": A.MLP_IN,
+        "FSI_IB_CLUSTER": A.IB_CLUSTER, "FSI_IB_OVERLAP": A.IB_OVERLAP, "FSI_IB_GATHER": A.IB_GATHER,
+        "FSI_MLP_IN": A.MLP_IN,
         "FSI_MLP_OUT": A.MLP_OUT, "FSI_MLP_NPARAM": A.MLP_NPARAM, "FSI_MLP_NNORM": A.MLP_NNORM,
         "FSI_STATIC_FACE_CELLS": A.STATIC_FACE_CELLS,
     }

@@ -82,3 +82,27 @@ def test_async_state_rules(gpu_lib):
     # after the wait the block takes IB calls again
     ef2, it2, _ = b.ib_step(xyz, vel, area, Uref=U, ntol=3, dtol=1e-6, blktime=2.0)
     assert it2 == 3
+
+
+@pytest.mark.parametrize("prec", [F.PREC_F64_FAST, F.PREC_F16])
+def test_gather_mode_is_deterministic(gpu_lib, prec):
+    # FSI_IB_GATHER: the same force and state from run to run on the fast
+    # forms, and the cooperative stage's result to its rounding
+    p = plate_in(DIMS, n=6, heave=2.0, freq=0.01)
+    runs = []
+    for mode in (F.abi.IB_GATHER, F.abi.IB_GATHER, F.abi.IB_GRID):
+        b = _block(prec)
+        b.ib_set_bodies([p.M], bc=list(BND))
+        b.set_ib_mode(mode)
+        t, efs = 0.0, []
+        for s in range(6):
+            xyz, vel, area = p.markers(t)
+            ef, it, res = b.ib_step(xyz, vel, area, Uref=U, ntol=5, dtol=1e-6, blktime=t + 1.0)
+            efs.append(ef)
+            t += 1.0
+        runs.append((np.array(efs), b.download_f()))
+    (e0, f0), (e1, f1), (e2, f2) = runs
+    assert np.array_equal(e0.view(np.uint64), e1.view(np.uint64))
+    assert np.array_equal(f0.view(np.uint64), f1.view(np.uint64))
+    tol = 1e-10 if prec == F.PREC_F64_FAST else 3e-4
+    assert np.max(np.abs(e2 - e0)) <= tol * np.max(np.abs(e0))
