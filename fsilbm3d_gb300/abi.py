@@ -101,7 +101,8 @@ def load_library():
     L.fsi_block_initialise.argtypes = [VP, C.c_double]
     L.fsi_block_set_boundary_conditions.argtypes = [VP, C.c_double]
     L.fsi_block_macro.argtypes = [VP, DP, DP, DP]
-    L.fsi_block_step.argtypes = [VP, DP, C.c_double]
+    # the calls of a time loop take plain addresses (see _vp)
+    L.fsi_block_step.argtypes = [VP, VP, C.c_double]
     L.fsi_block_run.argtypes = [VP, DP, C.c_double, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_timer.argtypes = [VP, C.c_int, C.POINTER(C.c_float)]
     L.fsi_block_set_kernel.argtypes = [VP, C.c_int]
@@ -114,11 +115,11 @@ def load_library():
     L.fsi_batch_ib_step.argtypes = [VP, DP, DP, DP, DP, DP, DP, DP, C.c_int, C.c_double, DP, DP, IP, DP]
     L.fsi_batch_tune.argtypes = [VP, C.c_int, IP, C.POINTER(C.c_float)]
     L.fsi_batch_set_threads.argtypes = [VP, C.c_int]
-    L.fsi_block_ib_step.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
-                                    C.c_double, DP, IP, DP]
-    L.fsi_block_ib_step_async.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int,
+    L.fsi_block_ib_step.argtypes = [VP, VP, VP, VP, VP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
+                                    C.c_double, VP, IP, DP]
+    L.fsi_block_ib_step_async.argtypes = [VP, VP, VP, VP, VP, C.c_double, C.c_double, C.c_double, C.c_int,
                                           C.c_double, C.c_double]
-    L.fsi_block_ib_wait.argtypes = [VP, DP, IP, DP]
+    L.fsi_block_ib_wait.argtypes = [VP, VP, IP, DP]
     L.fsi_ib_set_bodies.argtypes = [VP, C.c_int, IP, IP]
     L.fsi_ib_solve.argtypes = [VP, DP, DP, DP, DP, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
                                DP, IP, DP]
@@ -173,6 +174,18 @@ def _f32(a, cols):
 
 def _vec3(v):
     return np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(3))
+
+
+def _vp(a):
+    """the address of a contiguous array, for the calls of a time loop
+    (declared with void pointers): a third of the cost of a typed pointer"""
+    return a.ctypes.data
+
+
+def _v3(v):
+    """three doubles as a ctypes array"""
+    x, y, z = v
+    return (C.c_double * 3)(x, y, z)
 
 
 def device_info():
@@ -292,8 +305,7 @@ class Block:
     def step(self, volumeForce=(0.0, 0.0, 0.0), blktime=0.0):
         """add_volume_force_, collision_, halfwayBCset_, streaming_,
         set_boundary_conditions_ (LBMBlockComm.f90:288-303)"""
-        vf = _vec3(volumeForce)
-        _check(load_library().fsi_block_step(self.h, _dp(vf), blktime))
+        _check(load_library().fsi_block_step(self.h, _v3(volumeForce), blktime))
 
     def run(self, nsteps, volumeForce=(0.0, 0.0, 0.0), blktime0=0.0):
         """nsteps fluid steps from a captured CUDA graph; returns device ms"""
@@ -387,12 +399,11 @@ class Block:
         if area.size != self.Mtot or xyz.size != 3 * self.Mtot or vel.size != 3 * self.Mtot:
             raise ValueError("marker arrays do not match the bodies set with ib_set_bodies")
         eforce = np.empty(3 * self.Mtot)
-        vf = _vec3(volumeForce)
         it = C.c_int()
         res = C.c_double()
-        _check(load_library().fsi_block_ib_step(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(vf), denIn,
+        _check(load_library().fsi_block_ib_step(self.h, _vp(xyz), _vp(vel), _vp(area), _v3(volumeForce), denIn,
                                                 self.dh if dt is None else dt, Uref, int(ntol), dtol, blktime,
-                                                _dp(eforce), C.byref(it), C.byref(res)))
+                                                _vp(eforce), C.byref(it), C.byref(res)))
         return eforce.reshape(-1, 3), it.value, res.value
 
     def ib_step_async(self, xyz, vel, area, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0, ntol=3,
@@ -404,16 +415,15 @@ class Block:
         area = np.ascontiguousarray(area, dtype=np.float64).reshape(-1)
         if area.size != self.Mtot or xyz.size != 3 * self.Mtot or vel.size != 3 * self.Mtot:
             raise ValueError("marker arrays do not match the bodies set with ib_set_bodies")
-        vf = _vec3(volumeForce)
-        _check(load_library().fsi_block_ib_step_async(self.h, _dp(xyz), _dp(vel), _dp(area), _dp(vf), denIn,
-                                                      self.dh if dt is None else dt, Uref, int(ntol), dtol,
+        _check(load_library().fsi_block_ib_step_async(self.h, _vp(xyz), _vp(vel), _vp(area), _v3(volumeForce),
+                                                      denIn, self.dh if dt is None else dt, Uref, int(ntol), dtol,
                                                       blktime))
 
     def ib_wait(self):
         eforce = np.empty(3 * max(self.Mtot, 1))
         it = C.c_int()
         res = C.c_double()
-        _check(load_library().fsi_block_ib_wait(self.h, _dp(eforce), C.byref(it), C.byref(res)))
+        _check(load_library().fsi_block_ib_wait(self.h, _vp(eforce), C.byref(it), C.byref(res)))
         return eforce[:3 * self.Mtot].reshape(-1, 3), it.value, res.value
 
     def ib_solve_warm(self, xyz, vel, area, aux=None, volumeForce=(0.0, 0.0, 0.0), denIn=1.0, dt=None, Uref=1.0,
