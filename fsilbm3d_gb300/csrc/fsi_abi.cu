@@ -325,6 +325,36 @@ bool fill_bc(fsi_block *h, int k, void *f, double blktime, const int zdone[2], B
     a.u = h->u;
     a.zlo = zd0 ? 1 : 0;
     a.zhi = h->Z - 1 - (zd1 ? 1 : 0);
+    // offset forms, code 101: a face velocity uniform over the face (no shear
+    // along the face's own coordinates) gives one set of face populations
+    const bool off = h->prec == FSI_PREC_F32 || h->prec == FSI_PREC_F16 || h->prec == FSI_PREC_BF16;
+    const int ax = k >> 1;
+    const Vel &v = a.vel;
+    const bool uniform = v.kind == 2 || (ax == 0 ? (v.sr[1] == 0.0 && v.sr[2] == 0.0)
+                                                 : ax == 1 ? (v.sr[0] == 0.0 && v.sr[2] == 0.0)
+                                                           : (v.sr[0] == 0.0 && v.sr[1] == 0.0));
+    if (off && code == BC_EQ && uniform) {
+        // evaluate_velocity at the face (FluidDomain.f90:1791-1824)
+        const double xc = ax == 0 ? ((k & 1) ? h->xmax : h->d.xmin) : h->d.xmin;
+        const double yc = ax == 1 ? ((k & 1) ? h->ymax : h->d.ymin) : h->d.ymin;
+        const double zc = ax == 2 ? ((k & 1) ? h->zmax : h->d.zmin) : h->d.zmin;
+        double u[3];
+        if (v.kind == 2) {
+            u[0] = v.osc[0]; u[1] = v.osc[1]; u[2] = v.osc[2];
+        } else {
+            u[0] = ((v.vin[0] + 0.0 * v.sr[0]) + yc * v.sr[1]) + zc * v.sr[2];
+            u[1] = ((v.vin[1] + xc * v.sr[0]) + 0.0 * v.sr[1]) + zc * v.sr[2];
+            u[2] = ((v.vin[2] + xc * v.sr[0]) + yc * v.sr[1]) + 0.0 * v.sr[2];
+        }
+        // the offset equilibrium (calculate_distribution_funcion,
+        // FluidDomain.f90:1827-1834, minus the weight), as for the z faces
+        const double rho = h->d.denIn, usq = (u[0] * u[0] + u[1] * u[1]) + u[2] * u[2];
+        for (int q = 0; q < 19; q++) {
+            const double eu = (u[0] * ex_(q) + u[1] * ey_(q)) + u[2] * ez_(q);
+            a.gq[q] = (float)(wt_(q) * (rho - 1.0) + (wt_(q) * rho) * ((3.0 + 4.5 * eu) * eu - 1.5 * usq));
+        }
+        a.uni = 1;
+    }
     return true;
 }
 

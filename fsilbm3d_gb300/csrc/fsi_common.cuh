@@ -175,6 +175,10 @@ struct BcArgs {
     const double *u;
     int zlo, zhi;         // x/y faces: the z range they act on (the z faces the
                           // step kernel wrote are left to it)
+    // offset forms, code 101 with a face velocity uniform over the face: the
+    // face's 19 offset equilibrium populations, formed on the host in FP64
+    int uni;
+    float gq[19];
 };
 
 }  // namespace fsi

@@ -2591,6 +2591,13 @@ __device__ __forceinline__ void bc_off_body(const BcArgs &a, int fa, int fb) {
     };
     switch (a.code) {
     case BC_EQ: {
+        if (a.uni) {
+            // a uniform face: its populations from the host (no per-cell
+            // FP64 velocity, which GB300 issues at a small fraction of FP32)
+#pragma unroll
+            for (int i = 0; i < Q; i++) stq(c1, i, a.gq[i]);
+            break;
+        }
         double v[3];
         face_vel(a, fa, fb, false, v);
         const float u0 = (float)v[0], u1 = (float)v[1], u2 = (float)v[2];
