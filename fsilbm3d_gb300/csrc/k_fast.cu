@@ -720,8 +720,18 @@ __global__ void __launch_bounds__(TPB) k_step_fast(StepArgs a, MatsT<typename ST
 constexpr int TPB_DW2 = 128;
 struct SdT { dw2 sd[Q]; };
 
-template <int MODEL, typename IT>
-__global__ void __launch_bounds__(TPB_DW2) k_step_dw2(StepArgs a, Offs<IT> of, Scal<dw2> sc, SdT sdt) {
+// resident CTAs per SM (the register budget), measured on GB300 (256^3 TGV):
+// SRT 3 (165 registers, no spill); unforced MRT 4 (128 registers with about
+// 450 bytes of spill: 6.7k MLUPS, against 6.3k at 2 CTAs with 244 registers
+// and 6.1k at 3); forced MRT 2
+#ifndef FSI_DW2_MINB_MRT
+#define FSI_DW2_MINB_MRT 4
+#endif
+// FORCED (MRT): a nonzero volume force, compiled apart, so that the
+// unforced step does not carry the forcing terms' registers
+template <int MODEL, typename IT, bool FORCED>
+__global__ void __launch_bounds__(TPB_DW2, MODEL == CM_SRT ? 3 : (FORCED ? 2 : FSI_DW2_MINB_MRT))
+k_step_dw2(StepArgs a, Offs<IT> of, Scal<dw2> sc, SdT sdt) {
     const int zp = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int x = blockIdx.z;
@@ -745,10 +755,11 @@ __global__ void __launch_bounds__(TPB_DW2) k_step_dw2(StepArgs a, Offs<IT> of, S
     dw2 rho, drho, u0, u1, u2;
     macro_fast<PDW2>(g, sc.vf, sc.dh, rho, drho, u0, u1, u2);
     if constexpr (MODEL == CM_SRT) {
+        // (one SRT kernel with the forcing branch measured faster than two)
         if (sc.forced) collide_srt<PDW2, true>(g, rho, drho, u0, u1, u2, sc.vf[0], sc.vf[1], sc.vf[2], sc.om, sc.dh3);
         else collide_srt_free<PDW2>(g, rho, drho, u0, u1, u2, sc.om);
     } else {
-        collide_mrt_mom<PDW2>(g, rho, drho, u0, u1, u2, sc.vf[0], sc.vf[1], sc.vf[2], sc.forced != 0, sc.dh3, sdt.sd);
+        collide_mrt_mom<PDW2>(g, rho, drho, u0, u1, u2, sc.vf[0], sc.vf[1], sc.vf[2], FORCED, sc.dh3, sdt.sd);
     }
     // push: destination = c + st[i] + the periodic wrap of each cell
     const IT ZY = (IT)Z * (IT)Y, NN = (IT)N;
@@ -799,7 +810,8 @@ cudaError_t dw2_launch(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     sc.forced = (a.vf[0] != 0.0 || a.vf[1] != 0.0 || a.vf[2] != 0.0) ? 1 : 0;
     SdT sdt{};
     for (int k = 0; k < Q; k++) sdt.sd[k] = dw2(mm->sd[k]);
-    k_step_dw2<MODEL, IT><<<grd, blk, 0, st>>>(a, of, sc, sdt);
+    if (sc.forced && MODEL != CM_SRT) k_step_dw2<MODEL, IT, true><<<grd, blk, 0, st>>>(a, of, sc, sdt);
+    else k_step_dw2<MODEL, IT, false><<<grd, blk, 0, st>>>(a, of, sc, sdt);
     return cudaGetLastError();
 }
 #endif
