@@ -522,6 +522,34 @@ def fsi_period_case(F, steps=None, periods=5):
     return out
 
 
+def c_plate_loop(F, grid, dh, nu, steps, async_mode, plate, warmup=20):
+    """fsilbm3d_gb300/csrc/plate_loop.c, built against the in-tree library,
+    over the same plate case; returns its MLUPS and ms per step (wall clock
+    of the host loop), or the reason it could not run"""
+    import shutil
+    import subprocess
+    import tempfile
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        return {"unavailable": "no C compiler on this host"}
+    here = os.path.dirname(os.path.abspath(__file__))
+    lib = F.library_path()
+    exe = os.path.join(tempfile.mkdtemp(prefix="plate_loop_"), "plate_loop")
+    r = subprocess.run([cc, "-std=c99", "-D_POSIX_C_SOURCE=200112L", "-O2", "-I" + os.path.join(here, "include"),
+                        os.path.join(here, "fsilbm3d_gb300", "csrc", "plate_loop.c"), "-o", exe, lib, "-lm",
+                        "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
+    if r.returncode != 0:
+        return {"unavailable": "build failed: " + r.stderr.strip()[:200]}
+    X, Y, Z = grid
+    args = [exe, X, Y, Z, dh, nu, U, NTOL, DTOL, steps, warmup, async_mode, plate.n_chord, plate.n_span, plate.chord,
+            plate.span, plate.XYZo[0], plate.XYZo[1], plate.XYZo[2], plate.ampl[1], plate.freq]
+    r = subprocess.run([str(v) for v in args], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"unavailable": "run failed: " + r.stderr.strip()[:200]}
+    ms, mlups, cd, cl = (float(v) for v in r.stdout.split())
+    return {"mlups": round(mlups, 1), "ms_per_step": ms, "cd_cl_last": [cd, cl]}
+
+
 def ib160_case(F, steps):
     """160x96x96 block, 17x17-marker rigid plate in heave (dh = L/16, Re = 200)."""
     from fsilbm3d_gb300.bodies import RigidPlate, force_coefficients
@@ -569,6 +597,10 @@ def ib160_case(F, steps):
     out["f16_async"] = {"mlups": round(X * Y * Z * steps / (ms * 1e-3) / 1e6, 1), "ms_per_step": ms / steps,
                         "cd_cl_max_rel_diff_vs_f16": [float(v) for v in np.max(np.abs(fa - forces["f16"]), axis=0) /
                                                       np.maximum(np.max(np.abs(forces["f16"]), axis=0), 1e-30)]}
+    # the same FP16 case from a compiled host loop (no interpreter between
+    # the calls), one call per step and the async pair
+    for key, mode in (("f16_c_host", 0), ("f16_c_host_async", 1)):
+        out[key] = c_plate_loop(F, (X, Y, Z), dh, nu, steps, mode, plate)
     ref = forces["f64"]
     err = np.max(np.abs(forces["f16"] - ref), axis=0) / np.maximum(np.max(np.abs(ref), axis=0), 1e-30)
     out["cd_cl_max_rel_err_f16_vs_f64"] = [float(err[0]), float(err[1])]
@@ -584,7 +616,8 @@ def ib160_case(F, steps):
     out["steps"] = steps
     out["workload"] = ("160x96x96 MRT, dh=L/16, Re=200, 17x17-marker rigid plate heave A=0.5L f*=0.25; FP64 plain vs "
                        "FP16 mixed from the same start; f16_async: the FP16 run with the next step's markers formed "
-                       "on the host while the GPU steps")
+                       "on the host while the GPU steps; f16_c_host(_async): the FP16 run from a compiled host loop "
+                       "(fsilbm3d_gb300/csrc/plate_loop.c), wall clock")
     return out
 
 

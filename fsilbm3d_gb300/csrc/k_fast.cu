@@ -2529,11 +2529,16 @@ cudaError_t step_launch(const StepArgs &a, const MatsT<typename ST<P>::C> &m, cu
 template <int P, int MODEL>
 cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
     using C = typename ST<P>::C;
-    MatsT<C> m{};
-    if (MODEL == 3) {
-        for (int i = 0; i < 361; i++) { m.mc[i] = (C)mm->mc[i]; m.mf[i] = (C)mm->mf[i]; }
-        for (int k = 0; k < Q; k++) m.sd[k] = (C)mm->sd[k];
-    }
+    // the one-cell kernels' matrices in the arithmetic type, formed only for
+    // them (the paired kernels take the rates alone, every step)
+    auto mats = [&]() {
+        MatsT<C> m{};
+        if (MODEL == 3) {
+            for (int i = 0; i < 361; i++) { m.mc[i] = (C)mm->mc[i]; m.mf[i] = (C)mm->mf[i]; }
+            for (int k = 0; k < Q; k++) m.sd[k] = (C)mm->sd[k];
+        }
+        return m;
+    };
     // the hook-free variant serves blocks without IB window, half-way faces
     // and non-equilibrium extrapolation faces
     bool hooks = a.win.x1 >= a.win.x0;
@@ -2552,16 +2557,16 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
         }
 #endif
         if constexpr (MODEL == CM_SRT) {
-            if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
-            return hooks ? step_launch<P, MODEL, true, long long>(a, m, st)
-                         : step_launch<P, MODEL, false, long long>(a, m, st);
+            if (small) return hooks ? step_launch<P, MODEL, true, int>(a, mats(), st) : step_launch<P, MODEL, false, int>(a, mats(), st);
+            return hooks ? step_launch<P, MODEL, true, long long>(a, mats(), st)
+                         : step_launch<P, MODEL, false, long long>(a, mats(), st);
         } else if constexpr (MODEL == CM_MRT) {
             if (!mm->diag) return cudaErrorInvalidValue;
             if (small)
-                return hooks ? step_launch<P, CM_MRT_MOM, true, int>(a, m, st)
-                             : step_launch<P, CM_MRT_MOM, false, int>(a, m, st);
-            return hooks ? step_launch<P, CM_MRT_MOM, true, long long>(a, m, st)
-                         : step_launch<P, CM_MRT_MOM, false, long long>(a, m, st);
+                return hooks ? step_launch<P, CM_MRT_MOM, true, int>(a, mats(), st)
+                             : step_launch<P, CM_MRT_MOM, false, int>(a, mats(), st);
+            return hooks ? step_launch<P, CM_MRT_MOM, true, long long>(a, mats(), st)
+                         : step_launch<P, CM_MRT_MOM, false, long long>(a, mats(), st);
         } else {
             return cudaErrorInvalidValue;
         }
@@ -2572,11 +2577,11 @@ cudaError_t step_inst(const StepArgs &a, const MrtMats *mm, cudaStream_t st) {
         // moment space: about 80 operations for the transform each way
         // instead of two dense 19x19 products
         constexpr int MM = MODEL == CM_MRT ? CM_MRT_MOM : MODEL;
-        if (small) return hooks ? step_launch<P, MM, true, int>(a, m, st) : step_launch<P, MM, false, int>(a, m, st);
-        return hooks ? step_launch<P, MM, true, long long>(a, m, st) : step_launch<P, MM, false, long long>(a, m, st);
+        if (small) return hooks ? step_launch<P, MM, true, int>(a, mats(), st) : step_launch<P, MM, false, int>(a, mats(), st);
+        return hooks ? step_launch<P, MM, true, long long>(a, mats(), st) : step_launch<P, MM, false, long long>(a, mats(), st);
     }
-    if (small) return hooks ? step_launch<P, MODEL, true, int>(a, m, st) : step_launch<P, MODEL, false, int>(a, m, st);
-    return hooks ? step_launch<P, MODEL, true, long long>(a, m, st) : step_launch<P, MODEL, false, long long>(a, m, st);
+    if (small) return hooks ? step_launch<P, MODEL, true, int>(a, mats(), st) : step_launch<P, MODEL, false, int>(a, mats(), st);
+    return hooks ? step_launch<P, MODEL, true, long long>(a, mats(), st) : step_launch<P, MODEL, false, long long>(a, mats(), st);
     }
 }
 
