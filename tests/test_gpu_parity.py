@@ -418,10 +418,10 @@ def test_pipelined_kernel_needs_aligned_rows(gpu_lib):
                                            (F.PREC_F32, 1e-6, 2), (F.PREC_F16, 1e-3, 2), (F.PREC_F32, 1e-6, 3),
                                            (F.PREC_F16, 1e-3, 3), (F.PREC_F64, 0.0, 3)])
 def test_ib_step_equals_solve_then_step(gpu_lib, prec, tol, mode):
-    # mode 2: the IB stage on one cluster beside the bulk step; mode 3: the
-    # cooperative IB stage with the bulk step as its programmatic dependent
-    # (the fast forms' IB atomics sum in any order: agreement to rounding;
-    # the FP64 form runs its exact IB path)
+    # mode 1: the cooperative IB stage, then the bulk step; mode 2: the IB
+    # stage on one cluster beside the bulk step; mode 3: the cooperative IB
+    # stage beside the bulk step (the fast forms' IB atomics sum in any
+    # order: agreement to rounding; the FP64 form runs its exact IB path)
     dims = (40, 24, 20)
     blocks = []
     plate = plate_in(dims, n=5, heave=1.0, freq=0.02)
