@@ -186,7 +186,9 @@ struct fsi_block {
     double *hw[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int hw_ready[6] = {0, 0, 0, 0, 0, 0};
     cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_ib = nullptr;
+    // ev_ibk: the IB stage's kernel done (the fluid step's window fix-up
+    // waits for it); ev_ib: its force and status on the host as well
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_ib = nullptr, ev_ibk = nullptr;
     // the IB stage beside the bulk step (fsi_block_ib_step, FSI_IB_CLUSTER)
     int ib_mode = FSI_IB_AUTO;
     cudaStream_t st2 = nullptr;
@@ -501,6 +503,7 @@ void free_block(fsi_block *h) {
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->ev_ib) cudaEventDestroy(h->ev_ib);
+    if (h->ev_ibk) cudaEventDestroy(h->ev_ibk);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->st2) cudaStreamDestroy(h->st2);
     if (h->h_ef) cudaFreeHost(h->h_ef);
@@ -618,6 +621,7 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     chk(cudaEventCreate(&h->ev0));
     chk(cudaEventCreate(&h->ev1));
     chk(cudaEventCreateWithFlags(&h->ev_ib, cudaEventDisableTiming));
+    chk(cudaEventCreateWithFlags(&h->ev_ibk, cudaEventDisableTiming));
     chk(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
     {
         // the IB stage's stream is served first when SMs free up
@@ -1320,11 +1324,13 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
         } else {
             CK(launch_ib_cluster(a, h->prec, h->st2));
         }
+        // the window fix-up waits for the kernel only, not for the copies
+        CK(cudaEventRecord(h->ev_ibk, h->st2));
         CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st2));
         CK(cudaMemcpyAsync(h->h_stat, h->d_status, STAT_BYTES, cudaMemcpyDeviceToHost, h->st2));
         CK(cudaEventRecord(h->ev_ib, h->st2));
         h->win_valid = true;
-        int rc = enqueue_step(h, wm.step_vf, wm.step_time, true, h->ev_ib);
+        int rc = enqueue_step(h, wm.step_vf, wm.step_time, true, h->ev_ibk);
         h->win_valid = false;
         if (rc) return rc;
     } else {
@@ -1335,8 +1341,9 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
     const int grid = (int)std::max<long long>(1, std::min<long long>(need, h->coop_grid));
     CK(launch_ib_coop(a, h->prec, grid, h->st));
     if (wm.step) {
-        // force, status and residual into pinned staging, then the fluid step
-        // behind them on the stream; the host waits for the copies only
+        // force, status and residual into pinned staging on the second
+        // stream, while the fluid step follows the IB stage on this one; the
+        // host waits for the copies only
         if (h->h_ef_cap < h->Mtot) {
             if (h->h_ef) cudaFreeHost(h->h_ef);
             h->h_ef = nullptr;
@@ -1344,9 +1351,11 @@ int ib_solve_coop(fsi_block *h, const double vf[3], double denIn, double dt, dou
             CK(cudaHostAlloc((void **)&h->h_ef, sizeof(double) * 3 * h->Mtot, cudaHostAllocDefault));
             h->h_ef_cap = h->Mtot;
         }
-        CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(h->h_stat, h->d_status, STAT_BYTES, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaEventRecord(h->ev_ib, h->st));
+        CK(cudaEventRecord(h->ev_ibk, h->st));
+        CK(cudaStreamWaitEvent(h->st2, h->ev_ibk, 0));
+        CK(cudaMemcpyAsync(h->h_ef, h->d_eforce, sizeof(double) * 3 * h->Mtot, cudaMemcpyDeviceToHost, h->st2));
+        CK(cudaMemcpyAsync(h->h_stat, h->d_status, STAT_BYTES, cudaMemcpyDeviceToHost, h->st2));
+        CK(cudaEventRecord(h->ev_ib, h->st2));
         h->win_valid = true;
         int rc = enqueue_step(h, wm.step_vf, wm.step_time, true);
         h->win_valid = false;

@@ -119,3 +119,17 @@ def test_c_host_builds_against_the_header_and_gets_status_codes(gpu_lib, tmp_pat
         assert int(rc) == -1 and int(n) == len(msg) > 0, (name, rows[name])
     assert "RBGK" in rows["create_rbgk"][2] and "ELBM" in rows["create_elbm"][2]
     assert rows["destroy_null"][0] == "0"
+
+
+def test_plate_loop_host_builds_against_the_header(gpu_lib, tmp_path):
+    # the compiled host loop bench.py times (fsilbm3d_gb300/csrc/plate_loop.c)
+    # is plain C99 against include/fsi_gpu.h; it runs only on a GPU
+    import fsilbm3d_gb300 as F
+    lib = F.library_path()
+    exe = str(tmp_path / "plate_loop")
+    subprocess.run(["gcc", "-std=c99", "-D_POSIX_C_SOURCE=200112L", "-pedantic", "-Wall", "-Wextra", "-Werror",
+                    "-I" + os.path.join(ROOT, "include"), os.path.join(ROOT, "fsilbm3d_gb300", "csrc", "plate_loop.c"),
+                    "-o", exe, lib, "-lm", "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 2 and "usage" in out.stderr
+
