@@ -414,17 +414,24 @@ def test_pipelined_kernel_needs_aligned_rows(gpu_lib):
     b.set_kernel(F.abi.KERNEL_AUTO)
 
 
-@pytest.mark.parametrize("prec,tol,mode", [(F.PREC_F64, 0.0, 0), (F.PREC_F64_FAST, 1e-12, 0), (F.PREC_F32, 1e-6, 1),
-                                           (F.PREC_F32, 1e-6, 2), (F.PREC_F16, 1e-3, 2), (F.PREC_F32, 1e-6, 3),
-                                           (F.PREC_F16, 1e-3, 3), (F.PREC_F64, 0.0, 3)])
-def test_ib_step_equals_solve_then_step(gpu_lib, prec, tol, mode):
+@pytest.mark.parametrize("prec,tol,mode,where", [(F.PREC_F64, 0.0, 0, "interior"), (F.PREC_F64_FAST, 1e-12, 0, "interior"),
+                                                 (F.PREC_F32, 1e-6, 1, "interior"), (F.PREC_F32, 1e-6, 2, "interior"),
+                                                 (F.PREC_F16, 1e-3, 2, "interior"), (F.PREC_F32, 1e-6, 3, "interior"),
+                                                 (F.PREC_F16, 1e-3, 3, "interior"), (F.PREC_F64, 0.0, 3, "interior"),
+                                                 (F.PREC_F32, 1e-6, 2, "near_face"), (F.PREC_F32, 1e-6, 3, "near_face"),
+                                                 (F.PREC_F16, 1e-3, 3, "near_face")])
+def test_ib_step_equals_solve_then_step(gpu_lib, prec, tol, mode, where):
     # mode 1: the cooperative IB stage, then the bulk step; mode 2: the IB
     # stage on one cluster beside the bulk step; mode 3: the cooperative IB
     # stage beside the bulk step (the fast forms' IB atomics sum in any
-    # order: agreement to rounding; the FP64 form runs its exact IB path)
+    # order: agreement to rounding; the FP64 form runs its exact IB path).
+    # "interior": the window (x 10..19, y 11..16, z 6..15 of 40x24x20) stays
+    # clear of the face kernels' layers; "near_face": it reaches the z- face,
+    # whose face kernel must follow the window fix-up
     dims = (40, 24, 20)
     blocks = []
-    plate = plate_in(dims, n=5, heave=1.0, freq=0.02)
+    center = None if where == "interior" else (dims[0] * 0.35, dims[1] * 0.5 + 0.3, 4.17)
+    plate = plate_in(dims, n=5, heave=1.0, freq=0.02, center=center)
     for k in range(2):
         b = F.Block(*dims, bndConds=(101, 104, 101, 101, 101, 101), iCollidModel=3, nu=0.02, precision=prec,
                     uvwIn=(0.05, 0.0, 0.0))
