@@ -13,6 +13,7 @@
 #include <vector>
 #include <algorithm>
 #include <mutex>
+#include <new>
 
 #include <nvtx3/nvToolsExt.h>
 
@@ -570,7 +571,8 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
         if ((a == BC_PERIODIC || b == BC_PERIODIC) && a != b)
             return fail(FSI_E_BC, "Stop! Periodic boundaries must apper in pairs: %d %d", a, b);
     }
-    fsi_block *h = new fsi_block();
+    fsi_block *h = new (std::nothrow) fsi_block();
+    if (!h) return fail(FSI_E_ARG, "out of host memory");
     h->d = *d;
     h->d.m_collid = nullptr;
     h->d.m_force = nullptr;
@@ -591,7 +593,10 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
     if (d->iCollidModel == CM_TRT) {
         const double tmp = (d->params[0] * 4.0 - 1.0) * h->omega + 2.0;
         h->omega2 = (2.0 * (2.0 - h->omega)) / tmp;
-        if (!std::isfinite(h->omega2)) return fail(FSI_E_ARG, "TRT: Lambda %g gives no finite Omega2", d->params[0]);
+        if (!std::isfinite(h->omega2)) {
+            delete h;
+            return fail(FSI_E_ARG, "TRT: Lambda %g gives no finite Omega2", d->params[0]);
+        }
     }
     // CsmagConst, CWALEConst, CvremConst (ConstParams.f90:40-45), each
     // product rounded in turn
@@ -688,6 +693,8 @@ int fsi_block_create(fsi_block_t *out, const fsi_block_desc *d) {
 
 int fsi_block_destroy(fsi_block_t h) {
     if (!h) return FSI_OK;
+    // a queued IB step's copies run on the second stream
+    cudaStreamSynchronize(h->st2);
     cudaStreamSynchronize(h->st);
     free_block(h);
     return FSI_OK;
@@ -1101,15 +1108,20 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     if (!h || nbodies < 0 || (nbodies > 0 && !M)) return fail(FSI_E_ARG, "invalid argument");
     if (nbodies > 64) return fail(FSI_E_ARG, "at most 64 bodies per block");
     if (h->ib_pending) return fail(FSI_E_STATE, "an IB step is pending: fsi_block_ib_wait first");
-    h->nb = nbodies;
-    h->M.assign(M, M + nbodies);
-    h->offs.assign(nbodies + 1, 0);
+    // every argument checked before the block changes
+    long long total = 0;
     for (int b = 0; b < nbodies; b++) {
         if (M[b] <= 0) return fail(FSI_E_ARG, "body %d has no markers", b);
-        h->offs[b + 1] = h->offs[b] + M[b];
+        total += M[b];
+        if (total * 64 > 0x7fffffffLL) return fail(FSI_E_ARG, "too many markers");
     }
-    h->Mtot = h->offs[nbodies];
-    if ((long long)h->Mtot * 64 > 0x7fffffffLL) return fail(FSI_E_ARG, "too many markers");
+    // until the new arrays are in place the block has no bodies
+    h->nb = 0;
+    h->Mtot = 0;
+    h->win_valid = false;
+    h->M.assign(M, M + nbodies);
+    h->offs.assign(nbodies + 1, 0);
+    for (int b = 0; b < nbodies; b++) h->offs[b + 1] = h->offs[b] + M[b];
     for (int k = 0; k < 6; k++) h->ibbc[k] = bc ? bc[k] : h->d.bndConds[k];
     void *ptrs[] = {h->d_offs, h->d_xyz, h->d_eforce, h->d_fet, h->d_tolm, h->d_tol, h->d_ei, h->d_ew,
                     h->d_aux, h->d_feat, h->d_c64, h->d_w64};
@@ -1121,7 +1133,7 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     h->d_aux = nullptr;
     h->d_feat = nullptr;
     h->warm_cap = 0;
-    int Mt = std::max(1, h->Mtot);
+    const int Mt = std::max(1, (int)total);
     CK(cudaMalloc((void **)&h->d_offs, sizeof(int) * (nbodies + 1)));
     CK(cudaMalloc((void **)&h->d_xyz, sizeof(double) * 7 * Mt));
     h->d_vel = h->d_xyz + 3 * Mt;
@@ -1137,6 +1149,8 @@ int fsi_ib_set_bodies(fsi_block_t h, int nbodies, const int *M, const int bc[6])
     CK(cudaMalloc((void **)&h->d_w64, sizeof(double) * 64 * Mt));
     CK(cudaMemcpyAsync(h->d_offs, h->offs.data(), sizeof(int) * (nbodies + 1), cudaMemcpyHostToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
+    h->nb = nbodies;
+    h->Mtot = (int)total;
     return FSI_OK;
 }
 
@@ -1666,7 +1680,8 @@ int fsi_pair_create(fsi_pair_t *out, fsi_block_t fa, fsi_block_t so, int scheme)
     if (!out || !fa || !so) return fail(FSI_E_ARG, "null argument");
     *out = nullptr;
     if (fa->prec != so->prec) return fail(FSI_E_ARG, "father and son share one storage form");
-    fsi_pair *p = new fsi_pair();
+    fsi_pair *p = new (std::nothrow) fsi_pair();
+    if (!p) return fail(FSI_E_ARG, "out of host memory");
     p->fa = fa;
     p->so = so;
     p->scheme = scheme;
@@ -1927,7 +1942,8 @@ extern "C" {
 int fsi_mlp_create(fsi_mlp_t *out, unsigned long long seed) {
     if (!out) return fail(FSI_E_ARG, "null argument");
     *out = nullptr;
-    fsi_mlp *m = new fsi_mlp;
+    fsi_mlp *m = new (std::nothrow) fsi_mlp;
+    if (!m) return fail(FSI_E_ARG, "out of host memory");
     if (int rc = mlp_create(m, seed)) {
         free_mlp(m);
         return rc;
@@ -2312,7 +2328,8 @@ int fsi_batch_create(fsi_batch_t *out, int n, const fsi_block_t *blocks) {
         for (int c2 = 0; c2 < c; c2++)
             if (blocks[c2] == h) return fail(FSI_E_ARG, "block %d appears twice", c);
     }
-    fsi_batch *b = new fsi_batch;
+    fsi_batch *b = new (std::nothrow) fsi_batch;
+    if (!b) return fail(FSI_E_ARG, "out of host memory");
     b->n = n;
     b->blk.assign(blocks, blocks + n);
     b->prec = blocks[0]->prec;
@@ -2402,6 +2419,10 @@ int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const
     if (!b || !vf || !denIn || !dt || !Uref || !blktime || ntol < 0) return fail(FSI_E_ARG, "null argument");
     if (b->Mall > 0 && (!xyz || !vel || !area || !eforce)) return fail(FSI_E_ARG, "null marker array");
     const int n = b->n;
+    // the marker slices were laid out when the batch was made
+    for (int c = 0; c < n; c++)
+        if (b->blk[c]->Mtot != b->moff[c + 1] - b->moff[c])
+            return fail(FSI_E_STATE, "block %d: its bodies changed after fsi_batch_create", c);
     // the penalty residual sums of every block
     if (ntol > b->ntol_cap) {
         CK(cudaStreamSynchronize(b->st));

@@ -326,8 +326,10 @@ int fsi_batch_destroy(fsi_batch_t b);
  * Mtot), eforce (3, sum Mtot) out; vf (3, n), denIn, dt, Uref, blktime (n);
  * iters, residual (n) out (may be NULL). The device work of the step is one
  * CUDA graph: an upload of every block's tables and markers, the IB stage of
- * all blocks (one CTA per block), the bulk step of all blocks, their IB-window
- * fix-ups, one launch per face index and one download. */
+ * all blocks (one 8-CTA cluster per block), the bulk step of all blocks,
+ * their IB-window fix-ups, one launch per face index and one download.
+ * FSI_E_STATE when a block's bodies changed (fsi_ib_set_bodies) after
+ * fsi_batch_create. */
 int fsi_batch_ib_step(fsi_batch_t b, const double *xyz, const double *vel, const double *area,
                       const double *vf, const double *denIn, const double *dt, const double *Uref,
                       int ntol, double dtol, const double *blktime, double *eforce, int *iters,

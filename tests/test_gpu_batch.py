@@ -142,3 +142,16 @@ def test_batch_refusals(gpu_lib):
     with pytest.raises(F.FsiError) as e:  # the gradient models step alone
         F.Batch([v, F.Block(16, 12, 10, precision=F.PREC_F16, iCollidModel=15)])
     assert e.value.code == F.FSI_E_ARG
+
+
+def test_batch_refuses_changed_bodies(gpu_lib):
+    # the batch lays out every block's marker slice when it is made: a block
+    # whose bodies change afterwards is refused, not read past its slice
+    grouped, plates = _blocks(F.PREC_F16, 3, with_plates=True)
+    batch = F.Batch(grouped)
+    mk = [p.markers(0.0) if p is not None else None for p in plates]
+    batch.ib_step(mk, Uref=[0.04] * 4, ntol=2, dtol=0.0, blktime=[1.0] * 4)
+    grouped[0].ib_set_bodies([plates[0].M, 3])
+    with pytest.raises(F.FsiError) as e:
+        batch.ib_step(mk, Uref=[0.04] * 4, ntol=2, dtol=0.0, blktime=[2.0] * 4)
+    assert e.value.code == F.FSI_E_STATE

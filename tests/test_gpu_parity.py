@@ -320,6 +320,13 @@ def test_fast_ib_errors_are_status_codes(gpu_lib):
     assert e.value.code == -6
     b.step(blktime=1.0)
     assert np.all(np.isfinite(b.download_f()))
+    # a refused body list leaves the bodies as they were
+    for M in ([4, 0], [4, -2]):
+        with pytest.raises(F.FsiError) as e:
+            b.ib_set_bodies(M)
+        assert e.value.code == F.FSI_E_ARG
+    ef2, it2, res2 = b.ib_solve(xyz, vel, area, ntol=3, dtol=0.0, Uref=0.05)
+    assert it2 == 3 and ef2.shape == (4, 3) and np.all(np.isfinite(ef2))
 
 
 # --------------------------------------------------------------- error paths
